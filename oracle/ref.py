@@ -1,0 +1,224 @@
+"""Python face of the fem2d oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle is the checker for the GPU product: only tests/, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg may import this module. It wraps ``liboracle.so`` (a literal C++
+restatement of the reference's mesh, DoF enumeration, GLQ, basis spaces, 2-D quadrature integrals
+and galerkin assembly, see fem2d_oracle.cpp) and adds the FP64 eigen-solves the reference relies on:
+
+* ``reference_dense_solve``: restates ``nalgebra_solve_gep`` (src/fem_problem/linalg/nalgebra_solve.rs:14-50):
+  Cholesky inverse of B, the product B^-1 A, a symmetric eigen-decomposition that reads only the lower
+  triangle of that product (nalgebra 0.30.1 ``SymmetricEigen`` tridiagonalises from the lower triangle),
+  then the eigenvalue nearest the target.
+* ``gep_exact_dense``: LAPACK ``sygv`` on (A, B) through ``scipy.linalg.eigh`` (the "GEP-exact" solve).
+* ``sparse_shift_invert``: ARPACK shift-invert ``scipy.sparse.linalg.eigsh(A, k, M=B, sigma)``, the FP64
+  stand-in for the external SLEPc ``solve_gep`` (src/fem_problem/linalg/slepc_solve.rs:14-68).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+HREF_T, HREF_U, HREF_V = 0, 1, 2
+HIERPOLY, KOLEG = 0, 1
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            from . import build as _b  # noqa: F401  (lazy build for a fresh checkout)
+            _b.build_oracle()
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        f64p = ctypes.POINTER(ctypes.c_double)
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        L.oracle_last_error.restype = ctypes.c_char_p
+        L.oracle_mesh_new.restype = P
+        L.oracle_mesh_new.argtypes = [ctypes.c_int64, f64p, ctypes.c_int64, i64p, f64p]
+        L.oracle_free.argtypes = [P]
+        L.oracle_mesh_unit.restype = P
+        for name in ("oracle_set_orders", "oracle_p_refine", "oracle_h_refine"):
+            getattr(L, name).argtypes = [P, i64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+        for name in ("oracle_num_elems", "oracle_num_edges", "oracle_num_nodes", "oracle_num_specs"):
+            getattr(L, name).restype = ctypes.c_int64
+            getattr(L, name).argtypes = [P]
+        L.oracle_elem_info.argtypes = [P, i64p]
+        L.oracle_domain.argtypes = [P, i64p]
+        L.oracle_specs.argtypes = [P, i64p]
+        L.oracle_galerkin.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]
+        L.oracle_gep_export.argtypes = [P, i32p, i32p, f64p, f64p]
+        L.oracle_glq.argtypes = [ctypes.c_int, f64p, f64p]
+        L.oracle_shapes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, f64p]
+        L.oracle_default_ngq.argtypes = [ctypes.c_int]
+        _LIB = L
+    return _LIB
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError(lib().oracle_last_error().decode())
+
+
+def mesh_arrays_from_json(obj):
+    """Mesh JSON (the reference's format, src/fem_domain/domain/mesh.rs:100-141) to flat arrays."""
+    if isinstance(obj, str):
+        obj = json.loads(obj)
+    nodes = np.asarray(obj["Nodes"], dtype=np.float64).reshape(-1, 2)
+    els = obj["Elements"]
+    ids = np.asarray([e["node_ids"] for e in els], dtype=np.int64).reshape(-1, 4)
+    mats = np.asarray([e["materials"] for e in els], dtype=np.float64).reshape(-1, 4)
+    return nodes, ids, mats
+
+
+class OracleMesh:
+    """Restated ``Mesh`` + ``Domain`` + ``galerkin_sample_gep_hcurl`` (CPU, FP64)."""
+
+    def __init__(self, mesh_json=None):
+        if mesh_json is None:   # Mesh::unit()
+            self.h = lib().oracle_mesh_unit()
+            self.ndofs = None
+            return
+        nodes, ids, mats = mesh_arrays_from_json(mesh_json)
+        nodes = np.ascontiguousarray(nodes)
+        ids = np.ascontiguousarray(ids)
+        mats = np.ascontiguousarray(mats)
+        h = lib().oracle_mesh_new(len(nodes), _p(nodes, ctypes.c_double), len(ids), _p(ids, ctypes.c_int64),
+                                  _p(mats, ctypes.c_double))
+        if not h:
+            raise RuntimeError(lib().oracle_last_error().decode())
+        self.h = h
+        self.ndofs = None
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_free(self.h)
+            self.h = None
+
+    def _ids(self, ids):
+        if ids is None:
+            return None, 0
+        a = np.ascontiguousarray(np.asarray(ids, dtype=np.int64))
+        self._keep = a
+        return _p(a, ctypes.c_int64), len(a)
+
+    def set_orders(self, i, j, ids=None):
+        p, n = self._ids(ids)
+        _check(lib().oracle_set_orders(self.h, p, n, i, j))
+
+    def p_refine(self, di, dj, ids=None):
+        p, n = self._ids(ids)
+        _check(lib().oracle_p_refine(self.h, p, n, di, dj))
+
+    def h_refine(self, kind, ids=None, ext=-1):
+        p, n = self._ids(ids)
+        _check(lib().oracle_h_refine(self.h, p, n, kind, ext))
+
+    def num_elems(self):
+        return lib().oracle_num_elems(self.h)
+
+    def elem_info(self):
+        n = self.num_elems()
+        out = np.zeros((n, 14), dtype=np.int64)
+        _check(lib().oracle_elem_info(self.h, _p(out, ctypes.c_int64)))
+        return out
+
+    def domain(self):
+        nd = ctypes.c_int64(0)
+        _check(lib().oracle_domain(self.h, ctypes.byref(nd)))
+        self.ndofs = nd.value
+        return self.ndofs
+
+    def specs(self):
+        n = lib().oracle_num_specs(self.h)
+        out = np.zeros((n, 6), dtype=np.int64)
+        _check(lib().oracle_specs(self.h, _p(out, ctypes.c_int64)))
+        return out
+
+    def galerkin(self, basis=HIERPOLY, nu=0, nv=0, threads=1):
+        """Upper-triangle COO (rows, cols, a, b), sorted by (row, col) like the reference's BTreeMap."""
+        nnz = ctypes.c_int64(0)
+        _check(lib().oracle_galerkin(self.h, basis, nu, nv, threads, ctypes.byref(nnz)))
+        n = nnz.value
+        r = np.zeros(n, np.int32)
+        c = np.zeros(n, np.int32)
+        a = np.zeros(n, np.float64)
+        b = np.zeros(n, np.float64)
+        _check(lib().oracle_gep_export(self.h, _p(r, ctypes.c_int32), _p(c, ctypes.c_int32),
+                                       _p(a, ctypes.c_double), _p(b, ctypes.c_double)))
+        return r, c, a, b
+
+
+def glq(n):
+    p = np.zeros(n)
+    w = np.zeros(n)
+    _check(lib().oracle_glq(n, _p(p, ctypes.c_double), _p(w, ctypes.c_double)))
+    return p, w
+
+
+def shapes(basis, nmax, x):
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    out = np.zeros((4, nmax + 1, len(x)))
+    _check(lib().oracle_shapes(basis, nmax, len(x), _p(x, ctypes.c_double), _p(out, ctypes.c_double)))
+    return out
+
+
+def full_sym(n, rows, cols, vals):
+    """Mirror an upper-triangle COO into a full symmetric scipy CSR matrix."""
+    import scipy.sparse as sp
+
+    off = rows != cols
+    r = np.concatenate([rows, cols[off]])
+    c = np.concatenate([cols, rows[off]])
+    v = np.concatenate([vals, vals[off]])
+    return sp.csr_matrix((v, (r, c)), shape=(n, n))
+
+
+def reference_dense_solve(A, B, target):
+    """nalgebra_solve_gep restated (src/fem_problem/linalg/nalgebra_solve.rs:14-50)."""
+    import scipy.linalg as sl
+
+    A = np.asarray(A.todense() if hasattr(A, "todense") else A)
+    B = np.asarray(B.todense() if hasattr(B, "todense") else B)
+    L = np.linalg.cholesky(B)
+    Linv = sl.solve_triangular(L, np.eye(len(B)), lower=True)
+    Binv = Linv.T @ Linv
+    ba = Binv @ A
+    low = np.tril(ba)
+    sym = low + np.tril(ba, -1).T
+    w, v = np.linalg.eigh(sym)
+    if np.all(np.abs(w) < 1e-12):
+        raise RuntimeError("SpuriouslyConverged")
+    k = int(np.argmin(np.abs(w - target)))
+    return w[k], v[:, k]
+
+
+def gep_exact_dense(A, B, target, k=1):
+    """Generalized symmetric-definite solve by LAPACK (scipy.linalg.eigh), k pairs nearest target."""
+    import scipy.linalg as sl
+
+    A = np.asarray(A.todense() if hasattr(A, "todense") else A)
+    B = np.asarray(B.todense() if hasattr(B, "todense") else B)
+    w, v = sl.eigh(A, B)
+    order = np.argsort(np.abs(w - target), kind="stable")[:k]
+    return w[order], v[:, order]
+
+
+def sparse_shift_invert(A, B, target, k):
+    """k eigenpairs nearest target by ARPACK shift-invert (FP64, sparse LU of A - target*B)."""
+    import scipy.sparse.linalg as sla
+
+    w, v = sla.eigsh(A.tocsc(), k=k, M=B.tocsc(), sigma=target, which="LM", tol=1e-14)
+    order = np.argsort(np.abs(w - target), kind="stable")
+    return w[order], v[:, order]
