@@ -1,0 +1,499 @@
+"""fem_2d_gb300: GB300 implementation of fem_2d's Galerkin generalized-eigenproblem path.
+
+A thin Python face over the C ABI in ``include/fem2d_gb300.h`` (``libfem2d_gb300.so``, built in-tree
+by ``fem_2d_gb300/build.py``). Names follow the reference's prelude (src/lib.rs:14-39):
+
+    mesh = Mesh.from_file("mesh.json"); mesh.global_p_refinement(PRef.from_(3, 3))
+    mesh.global_h_refinement(HRef.T); mesh.h_refine_elems([6, 9, 12], HRef.T)
+    domain = Domain.from_mesh(mesh, ContinuityCondition.HCurl)
+    gep = galerkin_sample_gep_hcurl(HierPoly, CurlCurl, L2Inner, domain, [8, 8])
+    pair = gpu_solve_gep(gep, 1.475)            # stands beside slepc_solve_gep
+    pair = nalgebra_solve_gep(gep, 2.64)        # nalgebra_solve_gep restated on the device
+
+There is no CPU fallback: the GPU entry points raise if the library or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfem2d_gb300.so")
+_lib = None
+
+
+class Fem2dError(RuntimeError):
+    """A failed call through the C ABI; ``code`` is one of the FEM2D_E_* status codes."""
+
+    def __init__(self, code, msg):
+        super().__init__("[%d] %s" % (code, msg))
+        self.code = code
+
+
+# status codes (include/fem2d_gb300.h)
+E_OK, E_INVALID_ARG, E_MESH, E_HREF, E_PREF, E_WRONG_CC, E_EMPTY_DOFS, E_INVALID_GLQ = range(8)
+E_B_NOT_SPD, E_SPURIOUS, E_TOO_LARGE, E_NOT_CONVERGED, E_CUDA, E_TIMEOUT, E_NO_DEVICE, E_IO = range(8, 16)
+
+
+class _fem2d_solve_opts(ctypes.Structure):
+    _fields_ = [("precond", ctypes.c_int), ("max_outer", ctypes.c_int), ("max_inner", ctypes.c_int),
+                ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("block", ctypes.c_int),
+                ("verbose", ctypes.c_int)]
+
+
+class _fem2d_solve_stats(ctypes.Structure):
+    _fields_ = [("outer_iters", ctypes.c_int), ("inner_iters_total", ctypes.c_int), ("converged", ctypes.c_int),
+                ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
+                ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64)]
+
+
+def lib():
+    """Load libfem2d_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libfem2d_gb300.so is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    P, i64, i32, d = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_double
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    i64p, i32p, dp = ctypes.POINTER(i64), ctypes.POINTER(i32), ctypes.POINTER(d)
+    sig = {
+        "fem2d_last_error": (ctypes.c_char_p, []),
+        "fem2d_version": (ctypes.c_char_p, []),
+        "fem2d_mesh_from_json": (ctypes.c_int, [ctypes.c_char_p, PP]),
+        "fem2d_mesh_from_file": (ctypes.c_int, [ctypes.c_char_p, PP]),
+        "fem2d_mesh_unit": (ctypes.c_int, [PP]),
+        "fem2d_mesh_clone": (ctypes.c_int, [P, PP]),
+        "fem2d_mesh_free": (None, [P]),
+        "fem2d_mesh_set_expansion_orders": (ctypes.c_int, [P, i64p, i64, ctypes.c_int, ctypes.c_int]),
+        "fem2d_mesh_p_refine": (ctypes.c_int, [P, i64p, i64, ctypes.c_int, ctypes.c_int]),
+        "fem2d_mesh_h_refine": (ctypes.c_int, [P, i64p, i64, ctypes.c_int, ctypes.c_int]),
+        "fem2d_mesh_execute_h_refinements": (ctypes.c_int, [P, i64p, i32p, i64]),
+        "fem2d_mesh_num_elems": (i64, [P]),
+        "fem2d_mesh_num_edges": (i64, [P]),
+        "fem2d_mesh_num_nodes": (i64, [P]),
+        "fem2d_mesh_elem_info": (ctypes.c_int, [P, i64p]),
+        "fem2d_mesh_elem_bounds": (ctypes.c_int, [P, dp]),
+        "fem2d_domain_from_mesh": (ctypes.c_int, [P, ctypes.c_int, PP]),
+        "fem2d_domain_free": (None, [P]),
+        "fem2d_domain_num_dofs": (i64, [P]),
+        "fem2d_domain_num_specs": (i64, [P]),
+        "fem2d_domain_basis_specs": (ctypes.c_int, [P, i64p]),
+        "fem2d_domain_pattern": (ctypes.c_int, [P, i64p, i32p, i32p]),
+        "fem2d_ctx_create": (ctypes.c_int, [ctypes.c_int, PP]),
+        "fem2d_ctx_destroy": (None, [P]),
+        "fem2d_ctx_synchronize": (ctypes.c_int, [P]),
+        "fem2d_ctx_flush_l2": (ctypes.c_int, [P]),
+        "fem2d_ctx_kernel_launches": (i64, [P]),
+        "fem2d_galerkin_sample_gep_hcurl": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, PP]),
+        "fem2d_gep_recompute": (ctypes.c_int, [P, P]),
+        "fem2d_gep_free": (None, [P]),
+        "fem2d_gep_dims": (ctypes.c_int, [P, i64p, i64p, i64p]),
+        "fem2d_gep_export_upper": (ctypes.c_int, [P, i32p, i32p, dp, dp]),
+        "fem2d_gep_export_csr": (ctypes.c_int, [P, ctypes.c_int, i64p, i32p, dp]),
+        "fem2d_gep_timings": (ctypes.c_int, [P, dp]),
+        "fem2d_gep_num_visits": (i64, [P]),
+        "fem2d_dense_solve_gep": (ctypes.c_int, [P, P, d, dp, dp]),
+        "fem2d_gpu_solve_gep": (ctypes.c_int, [P, P, d, ctypes.c_int, ctypes.POINTER(_fem2d_solve_opts), dp, dp, dp,
+                                                ctypes.POINTER(_fem2d_solve_stats)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise Fem2dError(rc, lib().fem2d_last_error().decode())
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None else None
+
+
+def _ids(ids):
+    if ids is None:
+        return None, None, 0
+    a = np.ascontiguousarray(np.asarray(list(ids), dtype=np.int64))
+    return a, _ptr(a, ctypes.c_int64), len(a)
+
+
+# ----------------------------------------------------------------------------- prelude-style types
+class ContinuityCondition:
+    HCurl, HDiv, Discontinuous = 0, 1, 2
+
+
+class HRef:
+    """h-refinement kinds (h_refinement.rs:56-61). Use HRef.T / HRef.U / HRef.V or HRef.u_extended(i)."""
+    T, U, V = (0, -1), (1, -1), (2, -1)
+
+    @staticmethod
+    def t():
+        return HRef.T
+
+    @staticmethod
+    def u():
+        return HRef.U
+
+    @staticmethod
+    def v():
+        return HRef.V
+
+    @staticmethod
+    def u_extended(child_idx):
+        if child_idx not in (0, 1):
+            raise Fem2dError(E_HREF, "Extended refinement index must be 0 or 1!")
+        return (1, child_idx)
+
+    @staticmethod
+    def v_extended(child_idx):
+        if child_idx not in (0, 1):
+            raise Fem2dError(E_HREF, "Extended refinement index must be 0 or 1!")
+        return (2, child_idx)
+
+
+@dataclass(frozen=True)
+class PRef:
+    di: int
+    dj: int
+
+    @staticmethod
+    def from_(di, dj):
+        return PRef(di, dj)
+
+
+@dataclass(frozen=True)
+class Orders:
+    i: int
+    j: int
+
+
+class HierPoly:
+    ID = 0
+
+
+class KOLeg:
+    ID = 1
+
+
+class CurlCurl:
+    pass
+
+
+class L2Inner:
+    pass
+
+
+class Mesh:
+    """RBS mesh (src/fem_domain/domain/mesh.rs), held by the native library."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fem2d_mesh_free(self._h)
+            self._h = None
+
+    @staticmethod
+    def from_file(path):
+        h = ctypes.c_void_p()
+        _check(lib().fem2d_mesh_from_file(os.fsencode(path), ctypes.byref(h)))
+        return Mesh(h.value)
+
+    @staticmethod
+    def from_json(text):
+        h = ctypes.c_void_p()
+        if not isinstance(text, (bytes, str)):
+            import json
+            text = json.dumps(text)
+        if isinstance(text, str):
+            text = text.encode()
+        _check(lib().fem2d_mesh_from_json(text, ctypes.byref(h)))
+        return Mesh(h.value)
+
+    @staticmethod
+    def unit():
+        h = ctypes.c_void_p()
+        _check(lib().fem2d_mesh_unit(ctypes.byref(h)))
+        return Mesh(h.value)
+
+    def clone(self):
+        h = ctypes.c_void_p()
+        _check(lib().fem2d_mesh_clone(self._h, ctypes.byref(h)))
+        return Mesh(h.value)
+
+    # p-refinement
+    def set_global_expansion_orders(self, orders):
+        _check(lib().fem2d_mesh_set_expansion_orders(self._h, None, 0, orders.i, orders.j))
+
+    def set_expansion_on_elems(self, elems, orders):
+        a, p, n = _ids(elems)
+        _check(lib().fem2d_mesh_set_expansion_orders(self._h, p, n, orders.i, orders.j))
+
+    def global_p_refinement(self, pref):
+        _check(lib().fem2d_mesh_p_refine(self._h, None, 0, pref.di, pref.dj))
+
+    def p_refine_elems(self, elems, pref):
+        a, p, n = _ids(elems)
+        _check(lib().fem2d_mesh_p_refine(self._h, p, n, pref.di, pref.dj))
+
+    # h-refinement
+    def global_h_refinement(self, href):
+        _check(lib().fem2d_mesh_h_refine(self._h, None, 0, href[0], href[1]))
+
+    def h_refine_elems(self, elems, href):
+        a, p, n = _ids(elems)
+        _check(lib().fem2d_mesh_h_refine(self._h, p, n, href[0], href[1]))
+
+    def execute_h_refinements(self, refinements):
+        """refinements: iterable of (elem_id, HRef) with HRef in {T, U, V} (mesh.rs:844-914)."""
+        refinements = list(refinements)
+        ids = np.ascontiguousarray(np.asarray([r[0] for r in refinements], dtype=np.int64))
+        kinds = np.ascontiguousarray(np.asarray([r[1][0] for r in refinements], dtype=np.int32))
+        _check(lib().fem2d_mesh_execute_h_refinements(self._h, _ptr(ids, ctypes.c_int64),
+                                                      _ptr(kinds, ctypes.c_int32), len(ids)))
+
+    def h_refine_with_filter(self, filt):
+        """mesh.rs:728-750: filt(elem_info_row) -> HRef or None, over refineable (leaf) Elems."""
+        info = self.elem_info()
+        refs = []
+        for e in range(len(info)):
+            if info[e, 0] == 1:
+                r = filt(e, info[e])
+                if r is not None:
+                    refs.append((e, r))
+        if refs:
+            self.execute_h_refinements(refs)
+
+    # queries
+    @property
+    def num_elems(self):
+        return lib().fem2d_mesh_num_elems(self._h)
+
+    @property
+    def num_edges(self):
+        return lib().fem2d_mesh_num_edges(self._h)
+
+    @property
+    def num_nodes(self):
+        return lib().fem2d_mesh_num_nodes(self._h)
+
+    def elem_info(self):
+        """Per Elem: [is_leaf, ni, nj, parent, nodes(4), edges(4), h_u, h_v]."""
+        out = np.zeros((self.num_elems, 14), dtype=np.int64)
+        _check(lib().fem2d_mesh_elem_info(self._h, _ptr(out, ctypes.c_int64)))
+        return out
+
+    def elem_bounds(self):
+        out = np.zeros((self.num_elems, 4), dtype=np.float64)
+        _check(lib().fem2d_mesh_elem_bounds(self._h, _ptr(out, ctypes.c_double)))
+        return out
+
+
+class Domain:
+    """DoF enumeration (src/fem_domain/domain.rs:69-159)."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fem2d_domain_free(self._h)
+            self._h = None
+
+    @staticmethod
+    def from_mesh(mesh, cc=ContinuityCondition.HCurl):
+        h = ctypes.c_void_p()
+        _check(lib().fem2d_domain_from_mesh(mesh._h, cc, ctypes.byref(h)))
+        return Domain(h.value)
+
+    @property
+    def num_dofs(self):
+        return lib().fem2d_domain_num_dofs(self._h)
+
+    def basis_specs(self):
+        """Per spec: [elem_id, elem_idx, i, j, dir(0=U,1=V), dof_id] in Domain::basis_specs order."""
+        n = lib().fem2d_domain_num_specs(self._h)
+        out = np.zeros((n, 6), dtype=np.int64)
+        _check(lib().fem2d_domain_basis_specs(self._h, _ptr(out, ctypes.c_int64)))
+        return out
+
+
+def domain_pattern(domain):
+    """Upper-triangle keys (rows, cols) of the GEP sparsity pattern, built on the host."""
+    nu = ctypes.c_int64()
+    _check(lib().fem2d_domain_pattern(domain._h, ctypes.byref(nu), None, None))
+    r = np.zeros(nu.value, np.int32)
+    c = np.zeros(nu.value, np.int32)
+    _check(lib().fem2d_domain_pattern(domain._h, ctypes.byref(nu), _ptr(r, ctypes.c_int32), _ptr(c, ctypes.c_int32)))
+    return r, c
+
+
+class Context:
+    """A CUDA device and stream owned by the native library."""
+
+    _default = None
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().fem2d_ctx_create(device, ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fem2d_ctx_destroy(self._h)
+            self._h = None
+
+    @classmethod
+    def default(cls):
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def synchronize(self):
+        _check(lib().fem2d_ctx_synchronize(self._h))
+
+    def flush_l2(self):
+        _check(lib().fem2d_ctx_flush_l2(self._h))
+
+    @property
+    def kernel_launches(self):
+        return lib().fem2d_ctx_kernel_launches(self._h)
+
+
+class GEP:
+    """A generalized eigenproblem whose A and B live in device memory (linalg.rs:29-57)."""
+
+    def __init__(self, handle, ctx):
+        self._h = ctypes.c_void_p(handle)
+        self.ctx = ctx
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fem2d_gep_free(self._h)
+            self._h = None
+
+    def dims(self):
+        n, u, f = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().fem2d_gep_dims(self._h, ctypes.byref(n), ctypes.byref(u), ctypes.byref(f)))
+        return n.value, u.value, f.value
+
+    @property
+    def dimension(self):
+        return self.dims()[0]
+
+    @property
+    def num_visits(self):
+        return lib().fem2d_gep_num_visits(self._h)
+
+    def recompute(self):
+        _check(lib().fem2d_gep_recompute(self.ctx._h, self._h))
+
+    def timings(self):
+        out = np.zeros(3)
+        _check(lib().fem2d_gep_timings(self._h, _ptr(out, ctypes.c_double)))
+        return out
+
+    def upper_coo(self):
+        n, nu, nf = self.dims()
+        r = np.zeros(nu, np.int32)
+        c = np.zeros(nu, np.int32)
+        a = np.zeros(nu)
+        b = np.zeros(nu)
+        _check(lib().fem2d_gep_export_upper(self._h, _ptr(r, ctypes.c_int32), _ptr(c, ctypes.c_int32),
+                                            _ptr(a, ctypes.c_double), _ptr(b, ctypes.c_double)))
+        return r, c, a, b
+
+    def csr(self, which):
+        n, nu, nf = self.dims()
+        rp = np.zeros(n + 1, np.int64)
+        col = np.zeros(nf, np.int32)
+        val = np.zeros(nf)
+        _check(lib().fem2d_gep_export_csr(self._h, 0 if which in ("A", 0) else 1, _ptr(rp, ctypes.c_int64),
+                                          _ptr(col, ctypes.c_int32), _ptr(val, ctypes.c_double)))
+        return rp, col, val
+
+    def scipy(self):
+        import scipy.sparse as sp
+
+        n = self.dimension
+        out = []
+        for w in ("A", "B"):
+            rp, col, val = self.csr(w)
+            out.append(sp.csr_matrix((val, col, rp), shape=(n, n)))
+        return tuple(out)
+
+
+def galerkin_sample_gep_hcurl(bspace, a_integral, b_integral, domain, glq_grid_dim=None, ctx=None):
+    """galerkin_sample_gep_hcurl::<BSpace, CurlCurl, L2Inner>(&domain, glq_grid_dim) (galerkin.rs:33-187)."""
+    if a_integral is not CurlCurl or b_integral is not L2Inner:
+        raise Fem2dError(E_INVALID_ARG, "only <CurlCurl, L2Inner> is provided")
+    ctx = ctx or Context.default()
+    nu, nv = (0, 0) if glq_grid_dim is None else (int(glq_grid_dim[0]), int(glq_grid_dim[1]))
+    h = ctypes.c_void_p()
+    _check(lib().fem2d_galerkin_sample_gep_hcurl(ctx._h, domain._h, bspace.ID, nu, nv, ctypes.byref(h)))
+    return GEP(h.value, ctx)
+
+
+@dataclass
+class EigenPair:
+    """linalg.rs:84-96"""
+    value: float
+    vector: np.ndarray
+    residual: float = float("nan")
+
+    def normalized_eigenvector(self):
+        return self.vector / np.linalg.norm(self.vector)
+
+
+@dataclass
+class SolveResult:
+    values: np.ndarray
+    vectors: np.ndarray
+    residuals: np.ndarray
+    stats: dict = field(default_factory=dict)
+
+    def pairs(self):
+        return [EigenPair(float(v), self.vectors[k], float(self.residuals[k])) for k, v in enumerate(self.values)]
+
+
+def nalgebra_solve_gep(gep, target_eigenvalue):
+    """nalgebra_solve_gep (nalgebra_solve.rs:14-50) computed on the device; ndofs <= 1000."""
+    n = gep.dimension
+    val = ctypes.c_double()
+    vec = np.zeros(n)
+    _check(lib().fem2d_dense_solve_gep(gep.ctx._h, gep._h, float(target_eigenvalue), ctypes.byref(val),
+                                       _ptr(vec, ctypes.c_double)))
+    return EigenPair(val.value, vec)
+
+
+PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
+
+
+def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOBI, tol=0.0, max_outer=0,
+                    max_inner=0, inner_tol=0.0, block=0, verbose=0):
+    """The n_pairs eigenpairs nearest target by the device shift-invert solver."""
+    n = gep.dimension
+    vals = np.zeros(n_pairs)
+    vecs = np.zeros((n_pairs, n))
+    res = np.zeros(n_pairs)
+    o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose)
+    st = _fem2d_solve_stats()
+    _check(lib().fem2d_gpu_solve_gep(gep.ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
+                                     _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),
+                                     _ptr(res, ctypes.c_double), ctypes.byref(st)))
+    stats = {k: getattr(st, k) for k, _ in _fem2d_solve_stats._fields_}
+    return SolveResult(vals, vecs, res, stats)
+
+
+def gpu_solve_gep(gep, target_eigenvalue, **kw):
+    """gpu_solve_gep(gep, target) -> EigenPair, beside slepc_solve_gep (slepc_solve.rs:14-68)."""
+    return gpu_solve_gep_n(gep, target_eigenvalue, 1, **kw).pairs()[0]

@@ -1,0 +1,227 @@
+// Device numeric phase of galerkin_sample_gep_hcurl.
+//
+// K1 fem2d_contract1d_kernel: the 1-D quadrature contractions (basis x quad-point x basis) between
+//    the shape-function families of an outer Elem sampled over a dyadic sub-interval and of the inner
+//    Elem (glq.rs:19-32 restricted to one axis; shape functions hierarchical_basis_fns.rs).
+// K2 fem2d_values_kernel: one thread per entry of the full symmetric CSR; sums its visits, each the
+//    product C * Gu * Gv that equals the reference's 2-D sum (integrals.rs:26-92, 292-354) for affine
+//    Elems. FP64 throughout, deterministic (fixed summation order, no atomics). HBM-bound: the
+//    traffic is the contribution list read and the two FP64 value arrays written.
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace fem2d {
+
+namespace {
+
+// Shape families at x: 0 N (norm), 1 N', 2 T (tang), 3 T'.
+// HierPoly: hierarchical_basis_fns.rs:102-162. KOLeg (Legendre, restating HierMaxOrtho):
+// hierarchical_basis_fns.rs:201-647.
+__constant__ double c_euc[12] = {0.968246, 2.561738, 0.838525, 4.248161, 0.816397, 5.882766,
+                                 0.808509, 1.0, 1.0, 1.0, 1.0, 1.0};
+__constant__ int c_qden[12] = {1, 3, 6, 10, 15, 21, 28, 36, 40, 55, 66, 72};
+
+// numerator k of Q-function row idx (idx = order - 2): entries alternate with zeros; the odd/even
+// pattern is -1, -5, -9, ... (even rows) or -3, -7, -11, ... (odd rows), the last entry is positive.
+__device__ __forceinline__ double q_numerator(int idx, int k) {
+  const int dim = idx + 3;
+  if (k == dim - 1) {
+    const int tops[12] = {1, 3, 6, 10, 15, 21, 28, 36, 40, 55, 66, 72};
+    return (double)tops[idx];
+  }
+  if ((idx & 1) == 0) return (k & 1) ? 0.0 : -(double)(2 * k + 1);
+  return (k & 1) ? -(double)(2 * k + 1) : 0.0;
+}
+
+__device__ double shape(int basis, int family, int a, double x) {
+  if (basis == FEM2D_BASIS_HIERPOLY) {
+    if (a == 0) {
+      switch (family) { case 0: return 1.0; case 1: return 0.0; case 2: return 1.0 - x; default: return -1.0; }
+    }
+    if (a == 1) {
+      switch (family) { case 0: return x; case 1: return 1.0; case 2: return 1.0 + x; default: return 1.0; }
+    }
+    double prev = x, pw = x;   // pows[a-1], pows[a]
+    for (int k = 2; k <= a; k++) {
+      prev = pw;
+      pw = prev * x;
+    }
+    const double d1 = (double)a * prev;
+    const bool even = (a % 2) == 0;
+    switch (family) {
+      case 0: return pw;
+      case 1: return d1;
+      case 2: return even ? pw - 1.0 : pw - x;
+      default: return even ? d1 : d1 - 1.0;
+    }
+  }
+  // KOLeg
+  if (family == 2 || family == 3) {
+    if (a == 0) return family == 2 ? 1.0 - x : -1.0;
+    if (a == 1) return family == 2 ? 1.0 + x : 1.0;
+  }
+  double l0 = 1.0, l1 = x, d0 = 0.0, d1 = 1.0;
+  double accv = 0.0, accd = 0.0;
+  const bool want_q = family >= 2;
+  const int idx = a - 2;
+  const int top = want_q ? a : a;   // Q_a uses L_0 .. L_a
+  for (int k = 0; k <= top; k++) {
+    double lk, dk;
+    if (k == 0) { lk = 1.0; dk = 0.0; }
+    else if (k == 1) { lk = x; dk = 1.0; }
+    else {
+      const double f = (double)k;
+      lk = ((2.0 * f - 1.0) * x * l1 - (f - 1.0) * l0) / f;
+      dk = f * l1 + x * d1;
+      l0 = l1; l1 = lk; d0 = d1; d1 = dk;
+    }
+    if (want_q) {
+      const double w = q_numerator(idx, k) / (double)c_qden[idx];
+      accv += w * lk;
+      accd += w * dk;
+    } else if (k == a) {
+      return family == 0 ? lk : dk;
+    }
+  }
+  (void)d0;
+  return family == 2 ? accv * c_euc[idx] : accd * c_euc[idx];
+}
+
+// kind -> (family of the outer Elem at the scaled points, family of the inner Elem)
+__constant__ int c_kind_fam[5][2] = {{0, 0}, {3, 3}, {2, 2}, {0, 3}, {3, 0}};
+
+__global__ void fem2d_contract1d_kernel(int basis, int P, int nivl, const double* __restrict__ ivl,
+                                        const double* __restrict__ glq, int nq_u, int nq_v,
+                                        double* __restrict__ tables) {
+  const int iv = blockIdx.x, axis = blockIdx.y, kind = blockIdx.z;
+  const int nq = axis == 0 ? nq_u : nq_v;
+  const double* xs = axis == 0 ? glq : glq + 2 * nq_u;
+  const double* ws = xs + nq;
+  const double s = ivl[2 * iv], o = ivl[2 * iv + 1];
+  const int fa = c_kind_fam[kind][0], fb = c_kind_fam[kind][1];
+  double* out = tables + (((size_t)axis * nivl + iv) * 5 + kind) * P * P;
+  for (int t = threadIdx.x; t < P * P; t += blockDim.x) {
+    const int a = t / P, b = t % P;
+    double acc = 0.0;
+    for (int m = 0; m < nq; m++) {
+      const double x = xs[m];
+      acc += ws[m] * shape(basis, fa, a, s * x + o) * shape(basis, fb, b, x);
+    }
+    out[t] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const int64_t* __restrict__ cptr,
+                                                           const uint64_t* __restrict__ codes,
+                                                           const GBlock* __restrict__ blocks,
+                                                           const uint32_t* __restrict__ specs,
+                                                           const double* __restrict__ tables, int P, int nivl,
+                                                           double* __restrict__ A, double* __restrict__ B) {
+  const size_t PP = (size_t)P * P;
+  const size_t axis_stride = (size_t)nivl * 5 * PP;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k0 = __ldg(cptr + e), k1 = __ldg(cptr + e + 1);
+    double sa = 0.0, sb = 0.0;
+    for (int64_t k = k0; k < k1; k++) {
+      const uint64_t code = __ldg(codes + k);
+      const GBlock* bl = blocks + (code >> 32);
+      const int2 sp = __ldg(reinterpret_cast<const int2*>(bl));
+      const int2 iv = __ldg(reinterpret_cast<const int2*>(bl) + 1);
+      const uint32_t p = __ldg(specs + sp.x + (int)((code >> 16) & 0xffff));
+      const uint32_t q = __ldg(specs + sp.y + (int)(code & 0xffff));
+      const int pi = p & 0xff, pj = (p >> 8) & 0xff, pd = (p >> 16) & 0xff;
+      const int qi = q & 0xff, qj = (q >> 8) & 0xff, qd = (q >> 16) & 0xff;
+      const double* gu = tables + (size_t)iv.x * 5 * PP + (size_t)pi * P + qi;
+      const double* gv = tables + axis_stride + (size_t)iv.y * 5 * PP + (size_t)pj * P + qj;
+      const int dd = pd * 2 + qd;   // 0 UU, 1 UV, 2 VU, 3 VV
+      const double ca = __ldg(bl->ca + dd);
+      double va, vb = 0.0;
+      if (dd == 0) {
+        const double nn = __ldg(gu + G_NN * PP);
+        va = ca * nn * __ldg(gv + G_DD * PP);
+        vb = __ldg(bl->cb) * nn * __ldg(gv + G_TT * PP);
+      } else if (dd == 3) {
+        const double nn = __ldg(gv + G_NN * PP);
+        va = ca * __ldg(gu + G_DD * PP) * nn;
+        vb = __ldg(bl->cb + 1) * __ldg(gu + G_TT * PP) * nn;
+      } else if (dd == 1) {
+        va = ca * __ldg(gu + G_ND * PP) * __ldg(gv + G_DN * PP);
+      } else {
+        va = ca * __ldg(gu + G_DN * PP) * __ldg(gv + G_ND * PP);
+      }
+      sa += va;
+      sb += vb;
+    }
+    A[e] = sa;
+    B[e] = sb;
+  }
+}
+
+}  // namespace
+
+void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
+  cudaStream_t s = c.stream;
+  d.row_ptr.upload(g.row_ptr, s);
+  d.col.upload(g.col, s);
+  d.cptr.upload(g.cptr, s);
+  d.codes.upload(g.codes, s);
+  d.blocks.upload(g.blocks, s);
+  d.specs.upload(g.specs, s);
+  std::vector<double> iv(2 * g.ivl_s.size());
+  for (size_t k = 0; k < g.ivl_s.size(); k++) {
+    iv[2 * k] = g.ivl_s[k];
+    iv[2 * k + 1] = g.ivl_o[k];
+  }
+  d.ivl.upload(iv, s);
+  d.nivl = (int)g.ivl_s.size();
+  std::vector<double> q;
+  q.insert(q.end(), g.glq_u_x.begin(), g.glq_u_x.end());
+  q.insert(q.end(), g.glq_u_w.begin(), g.glq_u_w.end());
+  q.insert(q.end(), g.glq_v_x.begin(), g.glq_v_x.end());
+  q.insert(q.end(), g.glq_v_w.begin(), g.glq_v_w.end());
+  d.glq.upload(q, s);
+  const int P = g.pmax + 1;
+  d.tables.alloc((size_t)2 * d.nivl * 5 * P * P);
+  d.a.alloc(g.nnz_full);
+  d.b.alloc(g.nnz_full);
+  d.h2d_bytes = (int64_t)(g.row_ptr.size() * 8 + g.col.size() * 4 + g.cptr.size() * 8 + g.codes.size() * 8 +
+                          g.blocks.size() * sizeof(GBlock) + g.specs.size() * 4 + iv.size() * 8 + q.size() * 8);
+}
+
+void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, float* ms_values) {
+  cudaStream_t s = c.stream;
+  cudaEvent_t e0, e1, e2;
+  FEM2D_CUDA(cudaEventCreate(&e0));
+  FEM2D_CUDA(cudaEventCreate(&e1));
+  FEM2D_CUDA(cudaEventCreate(&e2));
+  const int P = g.pmax + 1;
+  FEM2D_CUDA(cudaEventRecord(e0, s));
+  dim3 grid1(d.nivl, 2, 5);
+  fem2d_contract1d_kernel<<<grid1, 128, 0, s>>>(g.basis, P, d.nivl, d.ivl.p, d.glq.p, g.nq_u, g.nq_v, d.tables.p);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
+  FEM2D_CUDA(cudaEventRecord(e1, s));
+  if (g.nnz_full > 0) {
+    const int threads = 256;
+    int64_t want = (g.nnz_full + threads - 1) / threads;
+    int64_t cap = (int64_t)c.num_sms * 8 * 4;   // persistent-ish grid: 8 blocks/SM x 4 waves
+    int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+    fem2d_values_kernel<<<grid, threads, 0, s>>>(g.nnz_full, d.cptr.p, d.codes.p, d.blocks.p, d.specs.p,
+                                                 d.tables.p, P, d.nivl, d.a.p, d.b.p);
+    FEM2D_CUDA(cudaGetLastError());
+    c.launches++;
+  }
+  FEM2D_CUDA(cudaEventRecord(e2, s));
+  FEM2D_CUDA(cudaEventSynchronize(e2));
+  float t1 = 0, t2 = 0;
+  cudaEventElapsedTime(&t1, e0, e1);
+  cudaEventElapsedTime(&t2, e1, e2);
+  if (ms_tables) *ms_tables = t1;
+  if (ms_values) *ms_values = t2;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+}
+
+}  // namespace fem2d

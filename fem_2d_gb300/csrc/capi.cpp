@@ -1,0 +1,418 @@
+// extern "C" boundary of fem2d_gb300 (declared in include/fem2d_gb300.h).
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+
+#include "common.h"
+#include "device.h"
+#include "domain.h"
+#include "eigen.h"
+#include "gep.h"
+#include "mesh.h"
+
+namespace fem2d {
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g);
+}  // namespace fem2d
+
+using namespace fem2d;
+
+struct fem2d_mesh { Mesh m; };
+struct fem2d_domain { Domain d; };
+struct fem2d_ctx { Ctx c; };
+struct fem2d_gep {
+  HostGEP h;
+  DeviceGEP d;
+  Ctx* ctx = nullptr;
+  double t_symbolic_ms = 0, t_tables_ms = 0, t_values_ms = 0, t_upload_ms = 0;
+};
+
+#define API_BEGIN try {
+#define API_END                      \
+  }                                  \
+  catch (const Error& e) {           \
+    set_last_error(e.what());        \
+    return e.code;                   \
+  }                                  \
+  catch (const std::bad_alloc&) {    \
+    set_last_error("out of memory"); \
+    return FEM2D_E_INVALID_ARG;      \
+  }                                  \
+  catch (const std::exception& e) {  \
+    set_last_error(e.what());        \
+    return FEM2D_E_INVALID_ARG;      \
+  }                                  \
+  return FEM2D_OK;
+
+static std::vector<int64_t> id_list(const int64_t* ids, int64_t n) {
+  if (n < 0) fail(FEM2D_E_INVALID_ARG, "negative id count");
+  if (n > 0 && !ids) fail(FEM2D_E_INVALID_ARG, "null id list");
+  return std::vector<int64_t>(ids, ids + n);
+}
+
+extern "C" {
+
+const char* fem2d_last_error(void) { return g_last_error.c_str(); }
+const char* fem2d_version(void) { return "fem2d_gb300 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------ mesh
+int fem2d_mesh_from_json(const char* json_text, fem2d_mesh** out) {
+  API_BEGIN
+  if (!json_text || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  auto* m = new fem2d_mesh{Mesh::from_json(json_text)};
+  *out = m;
+  API_END
+}
+
+int fem2d_mesh_from_file(const char* path, fem2d_mesh** out) {
+  API_BEGIN
+  if (!path || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::ifstream f(path);
+  if (!f) fail(FEM2D_E_IO, std::string("cannot open mesh file ") + path);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  *out = new fem2d_mesh{Mesh::from_json(ss.str())};
+  API_END
+}
+
+int fem2d_mesh_unit(fem2d_mesh** out) {
+  API_BEGIN
+  if (!out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  *out = new fem2d_mesh{Mesh::unit()};
+  API_END
+}
+
+int fem2d_mesh_clone(const fem2d_mesh* m, fem2d_mesh** out) {
+  API_BEGIN
+  if (!m || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  *out = new fem2d_mesh{m->m};
+  API_END
+}
+
+void fem2d_mesh_free(fem2d_mesh* m) { delete m; }
+
+int fem2d_mesh_set_expansion_orders(fem2d_mesh* m, const int64_t* ids, int64_t n, int i, int j) {
+  API_BEGIN
+  if (!m) fail(FEM2D_E_INVALID_ARG, "null mesh");
+  std::vector<int64_t> v;
+  if (!ids)
+    for (size_t e = 0; e < m->m.elems.size(); e++) v.push_back((int64_t)e);
+  else
+    v = id_list(ids, n);
+  m->m.set_expansion(v, i, j);
+  API_END
+}
+
+int fem2d_mesh_p_refine(fem2d_mesh* m, const int64_t* ids, int64_t n, int di, int dj) {
+  API_BEGIN
+  if (!m) fail(FEM2D_E_INVALID_ARG, "null mesh");
+  if (!ids) {
+    std::vector<int64_t> v;
+    for (size_t e = 0; e < m->m.elems.size(); e++) v.push_back((int64_t)e);
+    m->m.p_refine(v, di, dj, true);
+  } else {
+    m->m.p_refine(id_list(ids, n), di, dj, false);
+  }
+  API_END
+}
+
+int fem2d_mesh_h_refine(fem2d_mesh* m, const int64_t* ids, int64_t n, int kind, int ext) {
+  API_BEGIN
+  if (!m) fail(FEM2D_E_INVALID_ARG, "null mesh");
+  if (kind < 0 || kind > 2 || ext < -1 || ext > 1 || (kind == 0 && ext != -1))
+    fail(FEM2D_E_HREF, "invalid h-refinement kind");
+  if (!ids) m->m.global_h_refinement(kind, ext);
+  else m->m.h_refine_elems(id_list(ids, n), kind, ext);
+  API_END
+}
+
+int fem2d_mesh_execute_h_refinements(fem2d_mesh* m, const int64_t* ids, const int32_t* kinds, int64_t n) {
+  API_BEGIN
+  if (!m || (n > 0 && (!ids || !kinds))) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::vector<int64_t> v = id_list(ids, n);
+  std::vector<int> k(kinds, kinds + n);
+  for (int x : k)
+    if (x < 0 || x > 2) fail(FEM2D_E_HREF, "invalid h-refinement kind");
+  m->m.execute_h_refinements(v, k, std::vector<int>(n, -1));
+  API_END
+}
+
+int64_t fem2d_mesh_num_elems(const fem2d_mesh* m) { return m ? (int64_t)m->m.elems.size() : -1; }
+int64_t fem2d_mesh_num_edges(const fem2d_mesh* m) { return m ? (int64_t)m->m.edges.size() : -1; }
+int64_t fem2d_mesh_num_nodes(const fem2d_mesh* m) { return m ? (int64_t)m->m.nodes.size() : -1; }
+
+int fem2d_mesh_elem_info(const fem2d_mesh* m, int64_t* out) {
+  API_BEGIN
+  if (!m || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  for (size_t e = 0; e < m->m.elems.size(); e++) {
+    const MElem& el = m->m.elems[e];
+    int64_t* o = out + 14 * e;
+    o[0] = el.leaf() ? 1 : 0;
+    o[1] = el.ni;
+    o[2] = el.nj;
+    o[3] = el.anc.empty() ? -1 : el.anc.back();
+    for (int k = 0; k < 4; k++) o[4 + k] = el.nodes[k];
+    for (int k = 0; k < 4; k++) o[8 + k] = el.edges[k];
+    o[12] = el.hu;
+    o[13] = el.hv;
+  }
+  API_END
+}
+
+int fem2d_mesh_elem_bounds(const fem2d_mesh* m, double* out) {
+  API_BEGIN
+  if (!m || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  for (size_t e = 0; e < m->m.elems.size(); e++) {
+    auto pr = m->m.param_range((int64_t)e);
+    const RootElement& r = m->m.roots[m->m.elems[e].root];
+    auto mr = [](double v, double lo, double hi) { return (v + 1.0) * (hi - lo) / 2.0 + lo; };
+    out[4 * e + 0] = mr(pr[0], r.x0, r.x3);
+    out[4 * e + 1] = mr(pr[2], r.y0, r.y3);
+    out[4 * e + 2] = mr(pr[1], r.x0, r.x3);
+    out[4 * e + 3] = mr(pr[3], r.y0, r.y3);
+  }
+  API_END
+}
+
+// ------------------------------------------------------------------ domain
+int fem2d_domain_from_mesh(const fem2d_mesh* m, int cc, fem2d_domain** out) {
+  API_BEGIN
+  if (!m || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (cc < 0 || cc > 2) fail(FEM2D_E_INVALID_ARG, "unknown continuity condition");
+  *out = new fem2d_domain{Domain::from_mesh(m->m, cc)};
+  API_END
+}
+void fem2d_domain_free(fem2d_domain* d) { delete d; }
+int64_t fem2d_domain_num_dofs(const fem2d_domain* d) { return d ? d->d.ndofs : -1; }
+int64_t fem2d_domain_num_specs(const fem2d_domain* d) { return d ? (int64_t)d->d.specs.size() : -1; }
+int fem2d_domain_basis_specs(const fem2d_domain* d, int64_t* out) {
+  API_BEGIN
+  if (!d || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  size_t k = 0;
+  for (size_t e = 0; e + 1 < d->d.spec_ptr.size(); e++)
+    for (int64_t s = d->d.spec_ptr[e]; s < d->d.spec_ptr[e + 1]; s++, k++) {
+      const Spec& sp = d->d.specs[s];
+      int64_t* o = out + 6 * k;
+      o[0] = (int64_t)e;
+      o[1] = s - d->d.spec_ptr[e];
+      o[2] = sp.i;
+      o[3] = sp.j;
+      o[4] = sp.dir;
+      o[5] = sp.dof;
+    }
+  API_END
+}
+
+int fem2d_domain_pattern(const fem2d_domain* d, int64_t* nnz_upper, int32_t* rows, int32_t* cols) {
+  API_BEGIN
+  if (!d || !nnz_upper) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (d->d.cc != FEM2D_CC_HCURL) fail(FEM2D_E_WRONG_CC, "Wrong Continuity Condition on Domain (required: H(Curl))");
+  if (d->d.ndofs == 0) fail(FEM2D_E_EMPTY_DOFS, "No Degrees-of-Freedom Defined over Domain");
+  HostGEP g;
+  build_symbolic(d->d, 0, 4, 4, g);
+  *nnz_upper = g.nnz_upper;
+  if (rows || cols) {
+    int64_t k = 0;
+    for (int64_t r = 0; r < g.n; r++)
+      for (int64_t e = g.row_ptr[r]; e < g.row_ptr[r + 1]; e++)
+        if (g.col[e] >= r) {
+          if (rows) rows[k] = (int32_t)r;
+          if (cols) cols[k] = g.col[e];
+          k++;
+        }
+  }
+  API_END
+}
+
+// ------------------------------------------------------------------ context
+int fem2d_ctx_create(int device, fem2d_ctx** out) {
+  API_BEGIN
+  if (!out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    fail(FEM2D_E_NO_DEVICE, "no CUDA device is visible");
+  }
+  if (device < 0 || device >= n) fail(FEM2D_E_INVALID_ARG, "device index out of range");
+  std::unique_ptr<fem2d_ctx> c(new fem2d_ctx);
+  c->c.device = device;
+  FEM2D_CUDA(cudaSetDevice(device));
+  FEM2D_CUDA(cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking));
+  FEM2D_CUDA(cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+  *out = c.release();
+  API_END
+}
+
+void fem2d_ctx_destroy(fem2d_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->c.device);
+  if (c->c.flush_buf) cudaFree(c->c.flush_buf);
+  if (c->c.stream) cudaStreamDestroy(c->c.stream);
+  delete c;
+}
+
+int fem2d_ctx_synchronize(fem2d_ctx* c) {
+  API_BEGIN
+  if (!c) fail(FEM2D_E_INVALID_ARG, "null context");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  FEM2D_CUDA(cudaStreamSynchronize(c->c.stream));
+  API_END
+}
+
+int fem2d_ctx_flush_l2(fem2d_ctx* c) {
+  API_BEGIN
+  if (!c) fail(FEM2D_E_INVALID_ARG, "null context");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  const size_t bytes = 256ull << 20;
+  if (!c->c.flush_buf) FEM2D_CUDA(cudaMalloc(&c->c.flush_buf, bytes));
+  FEM2D_CUDA(cudaMemsetAsync(c->c.flush_buf, c->c.launches & 0xff, bytes, c->c.stream));
+  API_END
+}
+
+int64_t fem2d_ctx_kernel_launches(const fem2d_ctx* c) { return c ? c->c.launches : -1; }
+
+// ------------------------------------------------------------------ galerkin
+int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int basis, int nq_u, int nq_v,
+                                    fem2d_gep** out) {
+  API_BEGIN
+  if (!c || !d || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  // galerkin.rs:42-59
+  if (d->d.cc != FEM2D_CC_HCURL)
+    fail(FEM2D_E_WRONG_CC, "Wrong Continuity Condition on Domain (required: H(Curl)); Cannot execute Galerkin Sampling!");
+  if (d->d.ndofs == 0)
+    fail(FEM2D_E_EMPTY_DOFS, "No Degrees-of-Freedom Defined over Domain; Cannot execute Galerkin Sampling!");
+  if ((nq_u != 0 || nq_v != 0) && (nq_u < 4 || nq_v < 4))
+    fail(FEM2D_E_INVALID_GLQ, "Invalid GLQ Settings (the number of GLQ points must be at least 4); Cannot execute Galerkin Sampling!");
+  if (basis != FEM2D_BASIS_HIERPOLY && basis != FEM2D_BASIS_KOLEG) fail(FEM2D_E_INVALID_ARG, "unknown basis space");
+  auto mo = d->d.mesh.max_orders();
+  if (basis == FEM2D_BASIS_KOLEG && std::max(mo[0], mo[1]) > 12)
+    fail(FEM2D_E_INVALID_ARG, "KOLeg is tabulated for expansion orders up to 12");
+  if (d->d.ndofs >= (1ll << 31)) fail(FEM2D_E_INVALID_ARG, "more than 2^31 DoFs");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  std::unique_ptr<fem2d_gep> g(new fem2d_gep);
+  g->ctx = &c->c;
+  auto t0 = std::chrono::steady_clock::now();
+  build_symbolic(d->d, basis, nq_u == 0 ? 0 : nq_u, nq_v == 0 ? 0 : nq_v, g->h);
+  auto t1 = std::chrono::steady_clock::now();
+  device_upload(c->c, g->h, g->d);
+  FEM2D_CUDA(cudaStreamSynchronize(c->c.stream));
+  auto t2 = std::chrono::steady_clock::now();
+  float mt = 0, mv = 0;
+  device_assemble(c->c, g->h, g->d, &mt, &mv);
+  g->t_symbolic_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  g->t_upload_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+  g->t_tables_ms = mt;
+  g->t_values_ms = mv;
+  *out = g.release();
+  API_END
+}
+
+int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g) {
+  API_BEGIN
+  if (!c || !g) fail(FEM2D_E_INVALID_ARG, "null argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  float mt = 0, mv = 0;
+  device_assemble(c->c, g->h, g->d, &mt, &mv);
+  g->t_tables_ms = mt;
+  g->t_values_ms = mv;
+  API_END
+}
+
+void fem2d_gep_free(fem2d_gep* g) {
+  if (!g) return;
+  if (g->ctx) cudaSetDevice(g->ctx->device);
+  delete g;
+}
+
+int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64_t* nnz_full) {
+  API_BEGIN
+  if (!g) fail(FEM2D_E_INVALID_ARG, "null gep");
+  if (ndofs) *ndofs = g->h.n;
+  if (nnz_upper) *nnz_upper = g->h.nnz_upper;
+  if (nnz_full) *nnz_full = g->h.nnz_full;
+  API_END
+}
+
+int64_t fem2d_gep_num_visits(const fem2d_gep* g) { return g ? g->h.visits : -1; }
+
+int fem2d_gep_timings(const fem2d_gep* g, double* out) {
+  API_BEGIN
+  if (!g || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  out[0] = g->t_tables_ms;
+  out[1] = g->t_values_ms;
+  out[2] = g->t_tables_ms + g->t_values_ms;
+  API_END
+}
+
+static void fetch_values(const fem2d_gep* g, std::vector<double>& a, std::vector<double>& b) {
+  FEM2D_CUDA(cudaSetDevice(g->ctx->device));
+  a.resize(g->h.nnz_full);
+  b.resize(g->h.nnz_full);
+  if (g->h.nnz_full) {
+    FEM2D_CUDA(cudaMemcpyAsync(a.data(), g->d.a.p, a.size() * 8, cudaMemcpyDeviceToHost, g->ctx->stream));
+    FEM2D_CUDA(cudaMemcpyAsync(b.data(), g->d.b.p, b.size() * 8, cudaMemcpyDeviceToHost, g->ctx->stream));
+  }
+  FEM2D_CUDA(cudaStreamSynchronize(g->ctx->stream));
+}
+
+int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, double* a, double* b) {
+  API_BEGIN
+  if (!g) fail(FEM2D_E_INVALID_ARG, "null gep");
+  std::vector<double> va, vb;
+  fetch_values(g, va, vb);
+  int64_t k = 0;
+  for (int64_t r = 0; r < g->h.n; r++)
+    for (int64_t e = g->h.row_ptr[r]; e < g->h.row_ptr[r + 1]; e++) {
+      if (g->h.col[e] < r) continue;
+      if (rows) rows[k] = (int32_t)r;
+      if (cols) cols[k] = g->h.col[e];
+      if (a) a[k] = va[e];
+      if (b) b[k] = vb[e];
+      k++;
+    }
+  API_END
+}
+
+int fem2d_gep_export_csr(const fem2d_gep* g, int which, int64_t* row_ptr, int32_t* col, double* val) {
+  API_BEGIN
+  if (!g) fail(FEM2D_E_INVALID_ARG, "null gep");
+  if (which != FEM2D_MAT_A && which != FEM2D_MAT_B) fail(FEM2D_E_INVALID_ARG, "which must be A or B");
+  if (row_ptr) std::memcpy(row_ptr, g->h.row_ptr.data(), g->h.row_ptr.size() * 8);
+  if (col) std::memcpy(col, g->h.col.data(), g->h.col.size() * 4);
+  if (val && g->h.nnz_full) {
+    FEM2D_CUDA(cudaSetDevice(g->ctx->device));
+    const double* src = which == FEM2D_MAT_A ? g->d.a.p : g->d.b.p;
+    FEM2D_CUDA(cudaMemcpyAsync(val, src, g->h.nnz_full * 8, cudaMemcpyDeviceToHost, g->ctx->stream));
+    FEM2D_CUDA(cudaStreamSynchronize(g->ctx->stream));
+  }
+  API_END
+}
+
+// ------------------------------------------------------------------ eigensolvers
+int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, double* value, double* vector) {
+  API_BEGIN
+  if (!c || !g) fail(FEM2D_E_INVALID_ARG, "null argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  dense_solve(c->c, g->h, g->d, target, value, vector);
+  API_END
+}
+
+int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_pairs, const fem2d_solve_opts* opts,
+                        double* values, double* vectors, double* residuals, fem2d_solve_stats* stats) {
+  API_BEGIN
+  if (!c || !g) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (n_pairs <= 0 || n_pairs > g->h.n) fail(FEM2D_E_INVALID_ARG, "n_pairs out of range");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  fem2d_solve_opts o{};
+  if (opts) o = *opts;
+  fem2d_solve_stats st{};
+  sparse_solve(c->c, g->h, g->d, target, n_pairs, o, values, vectors, residuals, &st);
+  if (stats) *stats = st;
+  API_END
+}
+
+}  // extern "C"

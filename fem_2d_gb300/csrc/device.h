@@ -1,0 +1,72 @@
+// Device context and device-resident GEP.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "gep.h"
+
+namespace fem2d {
+
+#define FEM2D_CUDA(call)                                                                          \
+  do {                                                                                            \
+    cudaError_t _e = (call);                                                                      \
+    if (_e != cudaSuccess)                                                                        \
+      ::fem2d::fail(FEM2D_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));            \
+  } while (0)
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;        // kernels launched by this library on this context
+  void* flush_buf = nullptr;   // 256 MiB, for L2 flushes between timed repetitions
+  int num_sms = 0;
+};
+
+// A device buffer owned by this library.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    FEM2D_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const std::vector<T>& v, cudaStream_t s) {
+    alloc(v.size());
+    if (!v.empty()) FEM2D_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+struct DeviceGEP {
+  DBuf<int64_t> row_ptr, cptr;
+  DBuf<int32_t> col;
+  DBuf<uint64_t> codes;
+  DBuf<GBlock> blocks;
+  DBuf<uint32_t> specs;
+  DBuf<double> ivl, glq, tables;   // ivl: (s, o) pairs; glq: u x, u w, v x, v w
+  DBuf<double> a, b;               // values, full symmetric CSR order
+  int nivl = 0;
+  int64_t h2d_bytes = 0;
+};
+
+// assemble.cu
+void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d);
+// launches the table kernel and the value kernel; returns device times in ms (tables, values)
+void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, float* ms_values);
+
+}  // namespace fem2d

@@ -1,0 +1,12 @@
+// Eigensolvers on the device: dense (nalgebra_solve_gep restated) and sparse shift-invert.
+#pragma once
+#include "device.h"
+
+namespace fem2d {
+
+void dense_solve(Ctx& c, const HostGEP& h, const DeviceGEP& d, double target, double* value, double* vector);
+void sparse_solve(Ctx& c, const HostGEP& h, const DeviceGEP& d, double target, int n_pairs,
+                  const fem2d_solve_opts& o, double* values, double* vectors, double* residuals,
+                  fem2d_solve_stats* st);
+
+}  // namespace fem2d

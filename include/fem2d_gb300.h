@@ -1,0 +1,169 @@
+/*
+ * fem2d_gb300 — C ABI of the GB300 implementation of fem_2d's Galerkin generalized-eigenproblem
+ * path (H(curl) Maxwell, refinement-by-superposition meshes).
+ *
+ * Conventions: every function returns an int status (FEM2D_OK = 0) unless it returns a handle
+ * count or pointer; fem2d_last_error() gives the message of the last failure on the calling thread.
+ * Handles are not thread-safe. Output buffers are owned by the caller. No C++ exception crosses
+ * this boundary. Matrix entries are FP64; row pointers int64; column indices int32.
+ *
+ * Each entry point cites the reference item (jeremiah-corrado/fem_2d, path:line) it stands in for.
+ */
+#ifndef FEM2D_GB300_H
+#define FEM2D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mirror GalerkinSamplingError galerkin.rs:190-195, NalgebraGEPError
+ *      nalgebra_solve.rs:52-56, SlepcGEPError slepc_solve.rs:70-81, HRefError/PRefError) ---- */
+enum {
+  FEM2D_OK = 0,
+  FEM2D_E_INVALID_ARG = 1,
+  FEM2D_E_MESH = 2,            /* malformed mesh file / inconsistent mesh (Mesh::from_file panics) */
+  FEM2D_E_HREF = 3,            /* HRefError (h_refinement.rs:290-302) */
+  FEM2D_E_PREF = 4,            /* PRefError (p_refinement.rs:274-283) */
+  FEM2D_E_WRONG_CC = 5,        /* GalerkinSamplingError::WrongContinuityCondition */
+  FEM2D_E_EMPTY_DOFS = 6,      /* GalerkinSamplingError::EmptyDOFSet */
+  FEM2D_E_INVALID_GLQ = 7,     /* GalerkinSamplingError::InvalidGLQSettings */
+  FEM2D_E_B_NOT_SPD = 8,       /* NalgebraGEPError::FailedToInvertB */
+  FEM2D_E_SPURIOUS = 9,        /* NalgebraGEPError::SpuriouslyConverged */
+  FEM2D_E_TOO_LARGE = 10,      /* NalgebraGEPError::ProblemTooLarge */
+  FEM2D_E_NOT_CONVERGED = 11,  /* SlepcGEPError::FailedToConverge */
+  FEM2D_E_CUDA = 12,           /* CUDA runtime failure */
+  FEM2D_E_TIMEOUT = 13,        /* a device-side bounded wait gave up */
+  FEM2D_E_NO_DEVICE = 14,
+  FEM2D_E_IO = 15
+};
+
+/* ContinuityCondition (domain.rs:17-23) */
+enum { FEM2D_CC_HCURL = 0, FEM2D_CC_HDIV = 1, FEM2D_CC_DISCONTINUOUS = 2 };
+/* HRef (h_refinement.rs:56-61): T, U, V; ext = -1 (None) or child index 0/1 for U->V / V->U */
+enum { FEM2D_HREF_T = 0, FEM2D_HREF_U = 1, FEM2D_HREF_V = 2 };
+/* Basis spaces: HierPoly (hierarchical_basis_fns.rs:1-199) and KOLeg, the Legendre space that
+ * restates HierMaxOrtho (hierarchical_basis_fns.rs:201-647) */
+enum { FEM2D_BASIS_HIERPOLY = 0, FEM2D_BASIS_KOLEG = 1 };
+/* GEP matrices */
+enum { FEM2D_MAT_A = 0, FEM2D_MAT_B = 1 };
+/* preconditioners of the sparse shift-invert solve */
+enum { FEM2D_PRECOND_BLOCK_JACOBI = 0, FEM2D_PRECOND_LEARNED = 1 };
+
+typedef struct fem2d_mesh fem2d_mesh;
+typedef struct fem2d_domain fem2d_domain;
+typedef struct fem2d_ctx fem2d_ctx;
+typedef struct fem2d_gep fem2d_gep;
+
+const char* fem2d_last_error(void);
+const char* fem2d_version(void);
+
+/* ---------------- Mesh (src/fem_domain/domain/mesh.rs) ---------------- */
+/* Mesh::from_file (mesh.rs:142-327): JSON text in the reference's format */
+int fem2d_mesh_from_json(const char* json_text, fem2d_mesh** out);
+/* Mesh::from_file with a path */
+int fem2d_mesh_from_file(const char* path, fem2d_mesh** out);
+/* Mesh::unit (mesh.rs:58-91) */
+int fem2d_mesh_unit(fem2d_mesh** out);
+/* Mesh::clone */
+int fem2d_mesh_clone(const fem2d_mesh* m, fem2d_mesh** out);
+void fem2d_mesh_free(fem2d_mesh* m);
+/* set_global_expansion_orders / set_expansion_on_elems (mesh.rs:1446-1468); ids == NULL: all Elems */
+int fem2d_mesh_set_expansion_orders(fem2d_mesh* m, const int64_t* ids, int64_t n, int i, int j);
+/* global_p_refinement (mesh.rs:1236-1253, ids == NULL, clamped) / p_refine_elems (mesh.rs:1266-1276) */
+int fem2d_mesh_p_refine(fem2d_mesh* m, const int64_t* ids, int64_t n, int di, int dj);
+/* global_h_refinement (mesh.rs:681-696, ids == NULL) / h_refine_elems (mesh.rs:716-726) */
+int fem2d_mesh_h_refine(fem2d_mesh* m, const int64_t* ids, int64_t n, int kind, int ext);
+/* execute_h_refinements (mesh.rs:844-914): per-Elem refinement kinds (kinds[k] applies to ids[k]) */
+int fem2d_mesh_execute_h_refinements(fem2d_mesh* m, const int64_t* ids, const int32_t* kinds, int64_t n);
+int64_t fem2d_mesh_num_elems(const fem2d_mesh* m);
+int64_t fem2d_mesh_num_edges(const fem2d_mesh* m);
+int64_t fem2d_mesh_num_nodes(const fem2d_mesh* m);
+/* per Elem, 14 int64: [is_leaf, ni, nj, parent(-1), nodes[4], edges[4], h_u, h_v] */
+int fem2d_mesh_elem_info(const fem2d_mesh* m, int64_t* out);
+/* per Elem: 4 doubles (x_min, y_min, x_max, y_max) of its real-space extent */
+int fem2d_mesh_elem_bounds(const fem2d_mesh* m, double* out);
+
+/* ---------------- Domain (src/fem_domain/domain.rs) ---------------- */
+/* Domain::from_mesh (domain.rs:69-159): the mesh is copied (the reference consumes it) */
+int fem2d_domain_from_mesh(const fem2d_mesh* m, int cc, fem2d_domain** out);
+void fem2d_domain_free(fem2d_domain* d);
+int64_t fem2d_domain_num_dofs(const fem2d_domain* d);
+int64_t fem2d_domain_num_specs(const fem2d_domain* d);
+/* Domain::basis_specs flattened in (elem, elem_idx) order: per spec 6 int64
+ * [elem_id, elem_idx, i, j, dir(0=U,1=V), dof_id] */
+int fem2d_domain_basis_specs(const fem2d_domain* d, int64_t* out);
+
+/* Sparsity pattern of A and B (both share it) as the upper-triangle keys, sorted by (row, col): the
+ * SparseMatrix BTreeMap keys (sparse_matrix.rs:12-15, 68-98) galerkin_sample_gep_hcurl would produce.
+ * Host-only (no device work). Call with rows == cols == NULL to get *nnz_upper first. */
+int fem2d_domain_pattern(const fem2d_domain* d, int64_t* nnz_upper, int32_t* rows, int32_t* cols);
+
+/* ---------------- device context ---------------- */
+int fem2d_ctx_create(int device, fem2d_ctx** out);
+void fem2d_ctx_destroy(fem2d_ctx* c);
+int fem2d_ctx_synchronize(fem2d_ctx* c);
+/* writes a 256 MiB device buffer so the next launch starts from a cold L2 */
+int fem2d_ctx_flush_l2(fem2d_ctx* c);
+/* number of kernels this library launched on the context since creation */
+int64_t fem2d_ctx_kernel_launches(const fem2d_ctx* c);
+
+/* ---------------- Galerkin sampling (src/fem_problem/galerkin.rs:33-187) ---------------- */
+/* galerkin_sample_gep_hcurl::<BSpace, CurlCurl, L2Inner>(&domain, Some([nq_u, nq_v])).
+ * nq_u = nq_v = 0 means None (default_ngq, basis.rs:172-177). The sparsity pattern of A and B is
+ * built on the host (bit-exact with the reference's BTreeMap keys); the values are computed on the
+ * GPU and stay resident in device memory. */
+int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int basis, int nq_u, int nq_v,
+                                    fem2d_gep** out);
+/* Numeric phase only: recompute the values of an existing GEP on the device (same domain and
+ * settings). Used to time the device kernels with inputs resident in device memory. */
+int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g);
+void fem2d_gep_free(fem2d_gep* g);
+/* dims: ndofs, upper-triangle entry count (SparseMatrix::entries), full symmetric nnz
+ * (SparseMatrix::num_entries, sparse_matrix.rs:32-35) */
+int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64_t* nnz_full);
+/* upper triangle as COO sorted by (row, col), like SparseMatrix::iter_upper_tri (sparse_matrix.rs:122-126) */
+int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, double* a, double* b);
+/* full symmetric CSR (row_ptr: ndofs+1, col/val: nnz_full) of A or B */
+int fem2d_gep_export_csr(const fem2d_gep* g, int which, int64_t* row_ptr, int32_t* col, double* val);
+/* device timings (ms) of the last galerkin/recompute call: [tables, values, total] */
+int fem2d_gep_timings(const fem2d_gep* g, double* out3);
+/* visit count P_visits = sum_E [n(E)(n(E)+1)/2 + n(E) sum_D n(D)] (the reference's integrate calls) */
+int64_t fem2d_gep_num_visits(const fem2d_gep* g);
+
+/* ---------------- Eigensolvers (src/fem_problem/linalg/{nalgebra_solve,slepc_solve}.rs) ---------------- */
+/* nalgebra_solve_gep (nalgebra_solve.rs:14-50) on the device: B = L L^T, the product B^-1 A, the
+ * symmetric eigen-decomposition of its lower triangle, the pair nearest target. ndofs <= 1000. */
+int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, double* value, double* vector);
+
+typedef struct fem2d_solve_opts {
+  int precond;          /* FEM2D_PRECOND_* */
+  int max_outer;        /* outer (eigen) iterations, 0 = default */
+  int max_inner;        /* inner solver iterations per application, 0 = default */
+  double tol;           /* relative residual ||Ax - lambda Bx|| / (|lambda| ||Bx||), 0 = default 1e-10 */
+  double inner_tol;     /* inner relative tolerance, 0 = default */
+  int block;            /* block size, 0 = default (n_pairs + guard) */
+  int verbose;
+} fem2d_solve_opts;
+
+typedef struct fem2d_solve_stats {
+  int outer_iters;
+  int inner_iters_total;
+  int converged;
+  double t_setup_ms, t_solve_ms;
+  double max_rel_residual;
+  int64_t spmv_count;
+} fem2d_solve_stats;
+
+/* gpu_solve_gep: the n_pairs eigenpairs of (A, B) nearest target, by a shift-invert block
+ * eigensolver on the device. Stands beside slepc_solve_gep (slepc_solve.rs:14-68).
+ * values: n_pairs, sorted by |lambda - target|; vectors: n_pairs x ndofs row-major, B-normalised;
+ * residuals: n_pairs relative residuals computed in FP64. Any output pointer may be NULL. */
+int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_pairs, const fem2d_solve_opts* opts,
+                        double* values, double* vectors, double* residuals, fem2d_solve_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

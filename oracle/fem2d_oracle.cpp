@@ -1360,6 +1360,14 @@ int oracle_h_refine(void* h, const int64_t* ids, int64_t n, int kind, int ext) {
     }
   })
 }
+int oracle_execute_h(void* h, const int64_t* ids, const int32_t* kinds, int64_t n) {
+  auto* s = (OracleState*)h;
+  ORACLE_TRY({
+    std::vector<std::pair<size_t, HRef>> refs;
+    for (int64_t k = 0; k < n; k++) refs.push_back({(size_t)ids[k], HRef{kinds[k], -1}});
+    s->mesh.execute_h_refinements(refs);
+  })
+}
 int64_t oracle_num_elems(void* h) { return (int64_t)((OracleState*)h)->mesh.elems.size(); }
 int64_t oracle_num_edges(void* h) { return (int64_t)((OracleState*)h)->mesh.edges.size(); }
 int64_t oracle_num_nodes(void* h) { return (int64_t)((OracleState*)h)->mesh.nodes.size(); }

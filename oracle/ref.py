@@ -51,6 +51,7 @@ def lib():
             getattr(L, name).restype = ctypes.c_int64
             getattr(L, name).argtypes = [P]
         L.oracle_elem_info.argtypes = [P, i64p]
+        L.oracle_execute_h.argtypes = [P, i64p, i32p, ctypes.c_int64]
         L.oracle_domain.argtypes = [P, i64p]
         L.oracle_specs.argtypes = [P, i64p]
         L.oracle_galerkin.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]
@@ -124,6 +125,28 @@ class OracleMesh:
     def h_refine(self, kind, ids=None, ext=-1):
         p, n = self._ids(ids)
         _check(lib().oracle_h_refine(self.h, p, n, kind, ext))
+
+    def execute_h(self, ids, kinds):
+        a = np.ascontiguousarray(np.asarray(ids, dtype=np.int64))
+        k = np.ascontiguousarray(np.asarray(kinds, dtype=np.int32))
+        _check(lib().oracle_execute_h(self.h, _p(a, ctypes.c_int64), _p(k, ctypes.c_int32), len(a)))
+
+    def apply_ops(self, ops):
+        """Replay a refinement script (the op format of fem_2d_gb300.configs)."""
+        for op in ops:
+            if op[0] == "orders":
+                self.set_orders(op[1], op[2], op[3])
+            elif op[0] == "pref":
+                self.p_refine(op[1], op[2], op[3])
+            elif op[0] == "href":
+                self.h_refine(op[1], op[2], op[3])
+            elif op[0] == "hmix":
+                self.execute_h(op[1], op[2])
+            elif op[0] == "ordersmap":
+                for (i, j), ids in op[1]:
+                    self.set_orders(i, j, ids)
+            else:
+                raise ValueError(op[0])
 
     def num_elems(self):
         return lib().oracle_num_elems(self.h)
