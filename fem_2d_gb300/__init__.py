@@ -84,6 +84,7 @@ def lib():
         "fem2d_domain_num_specs": (i64, [P]),
         "fem2d_domain_basis_specs": (ctypes.c_int, [P, i64p]),
         "fem2d_domain_pattern": (ctypes.c_int, [P, i64p, i32p, i32p]),
+        "fem2d_domain_factor_plan": (ctypes.c_int, [P, i64p, i32p, i64p, i32p, i64p, i64p, i64p, i64p, i32p]),
         "fem2d_ctx_create": (ctypes.c_int, [ctypes.c_int, PP]),
         "fem2d_ctx_destroy": (None, [P]),
         "fem2d_ctx_synchronize": (ctypes.c_int, [P]),
@@ -335,6 +336,28 @@ def domain_pattern(domain):
     c = np.zeros(nu.value, np.int32)
     _check(lib().fem2d_domain_pattern(domain._h, ctypes.byref(nu), _ptr(r, ctypes.c_int32), _ptr(c, ctypes.c_int32)))
     return r, c
+
+
+def factor_plan(domain):
+    """The multifrontal factorization plan (host-only), as a dict of numpy arrays."""
+    sz = np.zeros(8, np.int64)
+    L = lib()
+    _check(L.fem2d_domain_factor_plan(domain._h, _ptr(sz, ctypes.c_int64), *([None] * 8)))
+    nf, nd, na, ne = (int(x) for x in sz[:4])
+    fr = np.zeros((nf, 4), np.int32)
+    dp = np.zeros(nf + 1, np.int64)
+    dofs = np.zeros(nd, np.int32)
+    ap = np.zeros(nf + 1, np.int64)
+    apos = np.zeros(na, np.int64)
+    acsr = np.zeros(na, np.int64)
+    ep = np.zeros(nf + 1, np.int64)
+    emap = np.zeros(ne, np.int32)
+    c64, c32 = ctypes.c_int64, ctypes.c_int32
+    _check(L.fem2d_domain_factor_plan(domain._h, _ptr(sz, c64), _ptr(fr, c32), _ptr(dp, c64), _ptr(dofs, c32),
+                                      _ptr(ap, c64), _ptr(apos, c64), _ptr(acsr, c64), _ptr(ep, c64),
+                                      _ptr(emap, c32)))
+    return dict(sizes=sz, fronts=fr, dof_ptr=dp, dofs=dofs, asm_ptr=ap, asm_pos=apos, asm_csr=acsr, ea_ptr=ep,
+                ea_map=emap)
 
 
 class Context:

@@ -12,6 +12,7 @@
 #include "eigen.h"
 #include "gep.h"
 #include "mesh.h"
+#include "mf.h"
 
 namespace fem2d {
 static thread_local std::string g_last_error;
@@ -25,6 +26,7 @@ struct fem2d_mesh { Mesh m; };
 struct fem2d_domain { Domain d; };
 struct fem2d_ctx { Ctx c; };
 struct fem2d_gep {
+  Domain dom;   // the Domain the GEP was sampled from (its Elem trees drive the factorization)
   HostGEP h;
   DeviceGEP d;
   Ctx* ctx = nullptr;
@@ -228,6 +230,41 @@ int fem2d_domain_pattern(const fem2d_domain* d, int64_t* nnz_upper, int32_t* row
   API_END
 }
 
+int fem2d_domain_factor_plan(const fem2d_domain* d, int64_t* sizes, int32_t* fronts, int64_t* dof_ptr,
+                             int32_t* dofs, int64_t* asm_ptr, int64_t* asm_pos, int64_t* asm_csr, int64_t* ea_ptr,
+                             int32_t* ea_map) {
+  API_BEGIN
+  if (!d || !sizes) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (d->d.ndofs == 0) fail(FEM2D_E_EMPTY_DOFS, "No Degrees-of-Freedom Defined over Domain");
+  HostGEP g;
+  build_symbolic(d->d, 0, 4, 4, g);
+  MFSymbolic s;
+  mf_symbolic(d->d, g, s);
+  sizes[0] = s.nfronts;
+  sizes[1] = (int64_t)s.dofs.size();
+  sizes[2] = (int64_t)s.asm_pos.size();
+  sizes[3] = (int64_t)s.ea_map.size();
+  sizes[4] = s.nlevels;
+  sizes[5] = s.max_f;
+  sizes[6] = s.max_p;
+  sizes[7] = s.mat_total;
+  if (fronts)
+    for (int f = 0; f < s.nfronts; f++) {
+      fronts[4 * f] = s.parent[f];
+      fronts[4 * f + 1] = s.level[f];
+      fronts[4 * f + 2] = s.f[f];
+      fronts[4 * f + 3] = s.p[f];
+    }
+  if (dof_ptr) std::copy(s.dof_ptr.begin(), s.dof_ptr.end(), dof_ptr);
+  if (dofs) std::copy(s.dofs.begin(), s.dofs.end(), dofs);
+  if (asm_ptr) std::copy(s.asm_ptr.begin(), s.asm_ptr.end(), asm_ptr);
+  if (asm_pos) std::copy(s.asm_pos.begin(), s.asm_pos.end(), asm_pos);
+  if (asm_csr) std::copy(s.asm_csr.begin(), s.asm_csr.end(), asm_csr);
+  if (ea_ptr) std::copy(s.ea_ptr.begin(), s.ea_ptr.end(), ea_ptr);
+  if (ea_map) std::copy(s.ea_map.begin(), s.ea_map.end(), ea_map);
+  API_END
+}
+
 // ------------------------------------------------------------------ context
 int fem2d_ctx_create(int device, fem2d_ctx** out) {
   API_BEGIN
@@ -295,6 +332,7 @@ int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int bas
   FEM2D_CUDA(cudaSetDevice(c->c.device));
   std::unique_ptr<fem2d_gep> g(new fem2d_gep);
   g->ctx = &c->c;
+  g->dom = d->d;
   auto t0 = std::chrono::steady_clock::now();
   build_symbolic(d->d, basis, nq_u == 0 ? 0 : nq_u, nq_v == 0 ? 0 : nq_v, g->h);
   auto t1 = std::chrono::steady_clock::now();
@@ -397,7 +435,7 @@ int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, doubl
   API_BEGIN
   if (!c || !g) fail(FEM2D_E_INVALID_ARG, "null argument");
   FEM2D_CUDA(cudaSetDevice(c->c.device));
-  dense_solve(c->c, g->h, g->d, target, value, vector);
+  dense_solve(c->c, g->dom, g->h, g->d, target, value, vector);
   API_END
 }
 
@@ -410,7 +448,12 @@ int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_p
   fem2d_solve_opts o{};
   if (opts) o = *opts;
   fem2d_solve_stats st{};
-  sparse_solve(c->c, g->h, g->d, target, n_pairs, o, values, vectors, residuals, &st);
+  try {
+    sparse_solve(c->c, g->dom, g->h, g->d, target, n_pairs, o, values, vectors, residuals, &st);
+  } catch (...) {
+    if (stats) *stats = st;
+    throw;
+  }
   if (stats) *stats = st;
   API_END
 }

@@ -4,8 +4,10 @@
 
 namespace fem2d {
 
-void dense_solve(Ctx& c, const HostGEP& h, const DeviceGEP& d, double target, double* value, double* vector);
-void sparse_solve(Ctx& c, const HostGEP& h, const DeviceGEP& d, double target, int n_pairs,
+struct Domain;
+void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double target, double* value,
+                 double* vector);
+void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double target, int n_pairs,
                   const fem2d_solve_opts& o, double* values, double* vectors, double* residuals,
                   fem2d_solve_stats* st);
 

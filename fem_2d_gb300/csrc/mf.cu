@@ -1,0 +1,448 @@
+// Numeric multifrontal factorization and block solves on the device (plan: mf.h, mf_symbolic.cpp).
+//
+// Fronts are dense, column-major, processed level by level (all fronts of a level in one launch per
+// step). Per level: assemble from the CSR values of c_a*A + c_b*B, extend-add the children's Schur
+// complements (one launch per child slot, so no two threads add to one entry), then a blocked
+// right-looking LU of the first p columns with partial pivoting restricted to the fully-summed rows
+// (or no pivoting in Cholesky mode for SPD shifts): panel (one CTA per front), unit-lower TRSM for
+// the U12 rows, FP64 GEMM update of the trailing block. The trailing (f-p)x(f-p) block left in place
+// is the update matrix for the parent.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "mfdev.h"
+
+namespace fem2d {
+
+namespace {
+
+constexpr int PANEL = 32;
+
+struct FrontDesc {   // device copy of the per-front scalars
+  int32_t f, p, parent, kid0, kid1;
+  int64_t off, dptr, aptr, aend, eptr;
+};
+
+__global__ void mf_assemble_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
+                                   const int64_t* __restrict__ apos, const int64_t* __restrict__ acsr,
+                                   const double* __restrict__ va, const double* __restrict__ vb, double ca, double cb,
+                                   double* __restrict__ F) {
+  const FrontDesc d = fd[lf[blockIdx.y]];
+  for (int64_t k = d.aptr + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < d.aend;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = acsr[k];
+    F[d.off + apos[k]] = ca * va[c] + cb * vb[c];
+  }
+}
+
+// add the child's trailing block (rows/cols >= p_child) into the parent at mapped positions
+__global__ void mf_extend_add_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd, int slot,
+                                     const int32_t* __restrict__ emap, double* __restrict__ F) {
+  const FrontDesc par = fd[lf[blockIdx.y]];
+  const int32_t ch = slot == 0 ? par.kid0 : par.kid1;
+  if (ch < 0) return;
+  const FrontDesc c = fd[ch];
+  const int s = c.f - c.p;
+  const int64_t total = (int64_t)s * s;
+  const int32_t* m = emap + c.eptr;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % s), j = (int)(t / s);   // child (row p+i, col p+j), column-major
+    const double v = F[c.off + (int64_t)(c.p + j) * c.f + (c.p + i)];
+    F[par.off + (int64_t)m[j] * par.f + m[i]] += v;
+  }
+}
+
+// columns k0 .. k0+w-1 of every front with p > k0: pivot, swap full rows, scale, update the panel
+__global__ void __launch_bounds__(256) mf_panel_kernel(const int32_t* __restrict__ lf,
+                                                       const FrontDesc* __restrict__ fd, int k0, int pivoting,
+                                                       double* __restrict__ F, int32_t* __restrict__ piv,
+                                                       const int64_t* __restrict__ piv_off, int* __restrict__ flags) {
+  const int fr = lf[blockIdx.x];
+  const FrontDesc d = fd[fr];
+  if (d.p <= k0) return;
+  const int w = min(PANEL, d.p - k0);
+  const int f = d.f;
+  double* A = F + d.off;
+  __shared__ double sval[256];
+  __shared__ int sidx[256];
+  __shared__ int s_piv;
+  __shared__ double s_d;
+  for (int k = k0; k < k0 + w; k++) {
+    double* colk = A + (int64_t)k * f;
+    int best = k;
+    if (pivoting) {
+      double bv = -1.0;
+      int bi = k;
+      for (int i = k + threadIdx.x; i < d.p; i += blockDim.x) {
+        const double a = fabs(colk[i]);
+        if (a > bv) { bv = a; bi = i; }
+      }
+      sval[threadIdx.x] = bv;
+      sidx[threadIdx.x] = bi;
+      __syncthreads();
+      for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+          const double o = sval[threadIdx.x + st];
+          const int oi = sidx[threadIdx.x + st];
+          if (o > sval[threadIdx.x] || (o == sval[threadIdx.x] && oi < sidx[threadIdx.x])) {
+            sval[threadIdx.x] = o;
+            sidx[threadIdx.x] = oi;
+          }
+        }
+        __syncthreads();
+      }
+      best = sidx[0];
+    }
+    if (threadIdx.x == 0) {
+      s_piv = best;
+      piv[piv_off[fr] + k] = best;
+    }
+    __syncthreads();
+    const int pr = s_piv;
+    if (pr != k)
+      for (int j = threadIdx.x; j < f; j += blockDim.x) {
+        const double t = A[(int64_t)j * f + k];
+        A[(int64_t)j * f + k] = A[(int64_t)j * f + pr];
+        A[(int64_t)j * f + pr] = t;
+      }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double dk = colk[k];
+      if (!(fabs(dk) > 0.0) || (!pivoting && !(dk > 0.0))) {
+        atomicOr(flags, pivoting ? 1 : 2);   // 1: zero pivot (perturbed), 2: not positive definite
+        dk = dk == 0.0 ? 1e-300 : dk;
+        colk[k] = dk;
+      }
+      s_d = 1.0 / dk;
+    }
+    __syncthreads();
+    const double inv = s_d;
+    for (int i = k + 1 + threadIdx.x; i < f; i += blockDim.x) colk[i] *= inv;
+    __syncthreads();
+    // rank-1 update of the remaining panel columns
+    const int ncols = k0 + w - (k + 1);
+    const int nrows = f - (k + 1);
+    for (int64_t t = threadIdx.x; t < (int64_t)ncols * nrows; t += blockDim.x) {
+      const int jj = k + 1 + (int)(t / nrows);
+      const int ii = k + 1 + (int)(t % nrows);
+      A[(int64_t)jj * f + ii] -= colk[ii] * A[(int64_t)jj * f + k];
+    }
+    __syncthreads();
+  }
+}
+
+// U12 = L11^-1 A12 for rows k0..k0+w-1 and columns k0+w..f-1 (unit lower L11)
+__global__ void __launch_bounds__(128) mf_trsm_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
+                                                      int k0, double* __restrict__ F) {
+  const FrontDesc d = fd[lf[blockIdx.y]];
+  if (d.p <= k0) return;
+  const int w = min(PANEL, d.p - k0);
+  const int f = d.f;
+  const int j = k0 + w + blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double L[PANEL][PANEL + 1];
+  double* A = F + d.off;
+  if (k0 + w + blockIdx.x * blockDim.x >= f) return;
+  for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+    const int r = t % w, c = t / w;
+    L[r][c] = A[(int64_t)(k0 + c) * f + (k0 + r)];
+  }
+  __syncthreads();
+  if (j >= f) return;
+  double x[PANEL];
+  double* col = A + (int64_t)j * f + k0;
+#pragma unroll
+  for (int r = 0; r < PANEL; r++)
+    if (r < w) x[r] = col[r];
+#pragma unroll
+  for (int r = 0; r < PANEL; r++) {
+    if (r >= w) break;
+    double s = x[r];
+#pragma unroll
+    for (int c = 0; c < PANEL; c++)
+      if (c < r) s -= L[r][c] * x[c];
+    x[r] = s;
+  }
+#pragma unroll
+  for (int r = 0; r < PANEL; r++)
+    if (r < w) col[r] = x[r];
+}
+
+// trailing update: A22 -= L21 * U12, rows/cols k0+w .. f-1; 64x64 tile per CTA, K = w
+__global__ void __launch_bounds__(256) mf_gemm_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
+                                                      int k0, double* __restrict__ F) {
+  const FrontDesc d = fd[lf[blockIdx.z]];
+  if (d.p <= k0) return;
+  const int w = min(PANEL, d.p - k0);
+  const int f = d.f;
+  const int base = k0 + w;
+  const int r0 = base + blockIdx.x * 64, c0 = base + blockIdx.y * 64;
+  if (r0 >= f || c0 >= f) return;
+  double* A = F + d.off;
+  __shared__ double Ls[PANEL][64];
+  __shared__ double Us[PANEL][64 + 1];
+  for (int t = threadIdx.x; t < PANEL * 64; t += blockDim.x) {
+    const int r = t % 64, c = t / 64;
+    Ls[c][r] = (c < w && r0 + r < f) ? A[(int64_t)(k0 + c) * f + r0 + r] : 0.0;
+    const int uc = t / PANEL, ur = t % PANEL;   // U tile: PANEL rows x 64 cols, coalesced along rows
+    Us[ur][uc] = (ur < w && c0 + uc < f) ? A[(int64_t)(c0 + uc) * f + k0 + ur] : 0.0;
+  }
+  __syncthreads();
+  const int tr = threadIdx.x % 16, tc = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int t = 0; t < w; t++) {
+    double a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      a[q] = Ls[t][tr + 16 * q];
+      b[q] = Us[t][tc + 16 * q];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int s = 0; s < 4; s++) acc[q][s] += a[q] * b[s];
+  }
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const int c = c0 + tc + 16 * s;
+    if (c >= f) continue;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int r = r0 + tr + 16 * q;
+      if (r < f) A[(int64_t)c * f + r] -= acc[q][s];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ block solves
+// RHS/solution X: row-major n x nb (ld = ldx). Workspace per front: f x nb, column-major.
+__global__ void __launch_bounds__(256) mf_forward_kernel(const int32_t* __restrict__ lf,
+                                                         const FrontDesc* __restrict__ fd,
+                                                         const int32_t* __restrict__ dofs,
+                                                         const int32_t* __restrict__ emap,
+                                                         const int32_t* __restrict__ piv,
+                                                         const int64_t* __restrict__ piv_off,
+                                                         const int64_t* __restrict__ woff,
+                                                         const double* __restrict__ F, const double* __restrict__ B,
+                                                         int64_t ldb, int nb, double* __restrict__ W) {
+  const int fr = lf[blockIdx.x];
+  const FrontDesc d = fd[fr];
+  const int f = d.f, p = d.p;
+  double* v = W + woff[fr];
+  const int32_t* D = dofs + d.dptr;
+  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) {
+    const int i = t % f, c = t / f;
+    v[(int64_t)c * f + i] = i < p ? B[(int64_t)D[i] * ldb + c] : 0.0;
+  }
+  __syncthreads();
+  for (int slot = 0; slot < 2; slot++) {
+    const int ch = slot == 0 ? d.kid0 : d.kid1;
+    if (ch < 0) continue;
+    const FrontDesc cd = fd[ch];
+    const int s = cd.f - cd.p;
+    const double* cw = W + woff[ch];
+    const int32_t* m = emap + cd.eptr;
+    for (int t = threadIdx.x; t < s * nb; t += blockDim.x) {
+      const int i = t % s, c = t / s;
+      v[(int64_t)c * f + m[i]] += cw[(int64_t)c * cd.f + cd.p + i];
+    }
+    __syncthreads();
+  }
+  const int32_t* pv = piv + piv_off[fr];
+  for (int k = 0; k < p; k++) {
+    const int pr = pv[k];
+    if (pr != k)
+      for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+        const double t = v[(int64_t)c * f + k];
+        v[(int64_t)c * f + k] = v[(int64_t)c * f + pr];
+        v[(int64_t)c * f + pr] = t;
+      }
+    __syncthreads();
+  }
+  const double* A = F + d.off;
+  for (int k = 0; k < p; k++) {
+    const double* colk = A + (int64_t)k * f;
+    const int nr = f - k - 1;
+    for (int t = threadIdx.x; t < nr * nb; t += blockDim.x) {
+      const int i = k + 1 + t % nr, c = t / nr;
+      v[(int64_t)c * f + i] -= colk[i] * v[(int64_t)c * f + k];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) mf_backward_kernel(const int32_t* __restrict__ lf,
+                                                          const FrontDesc* __restrict__ fd,
+                                                          const int32_t* __restrict__ dofs,
+                                                          const int64_t* __restrict__ woff,
+                                                          const double* __restrict__ F, double* __restrict__ W,
+                                                          int nb, double* __restrict__ X, int64_t ldx) {
+  const int fr = lf[blockIdx.x];
+  const FrontDesc d = fd[fr];
+  const int f = d.f, p = d.p;
+  if (p == 0) return;
+  double* v = W + woff[fr];
+  const int32_t* D = dofs + d.dptr;
+  const double* A = F + d.off;
+  // y -= U12 x_struct
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    double s = v[(int64_t)c * f + i];
+    for (int j = p; j < f; j++) s -= A[(int64_t)j * f + i] * X[(int64_t)D[j] * ldx + c];
+    v[(int64_t)c * f + i] = s;
+  }
+  __syncthreads();
+  for (int k = p - 1; k >= 0; k--) {
+    const double* colk = A + (int64_t)k * f;
+    if (threadIdx.x < nb) v[(int64_t)threadIdx.x * f + k] /= colk[k];
+    __syncthreads();
+    for (int t = threadIdx.x; t < k * nb; t += blockDim.x) {
+      const int i = t % k, c = t / k;
+      v[(int64_t)c * f + i] -= colk[i] * v[(int64_t)c * f + k];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    X[(int64_t)D[i] * ldx + c] = v[(int64_t)c * f + i];
+  }
+}
+
+}  // namespace
+
+void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
+  cudaStream_t st = c.stream;
+  nf = s.nfronts;
+  nlevels = s.nlevels;
+  level_ptr = s.level_ptr;
+  max_f = s.max_f;
+  max_p = s.max_p;
+  nb_cap = nb_max;
+  // fronts laid out level by level so each level's storage is contiguous
+  std::vector<int64_t> off(nf, 0), poff(nf, 0), woff_h(nf, 0);
+  std::vector<int32_t> kid0(nf, -1), kid1(nf, -1);
+  for (int f = 0; f < nf; f++) {
+    int pa = s.parent[f];
+    if (pa >= 0) {
+      if (kid0[pa] < 0) kid0[pa] = f;
+      else kid1[pa] = f;
+    }
+  }
+  int64_t o = 0, po = 0, wo = 0;
+  level_off.assign(nlevels + 1, 0);
+  for (int l = 0; l < nlevels; l++) {
+    level_off[l] = o;
+    for (int k = s.level_ptr[l]; k < s.level_ptr[l + 1]; k++) {
+      int f = s.level_fronts[k];
+      off[f] = o;
+      o += (int64_t)s.f[f] * s.f[f];
+      poff[f] = po;
+      po += s.p[f];
+      woff_h[f] = wo;
+      wo += (int64_t)s.f[f] * nb_max;
+    }
+  }
+  level_off[nlevels] = o;
+  mat_total = o;
+  std::vector<FrontDesc> fdh(nf);
+  for (int f = 0; f < nf; f++) {
+    FrontDesc& x = fdh[f];
+    x.f = s.f[f];
+    x.p = s.p[f];
+    x.parent = s.parent[f];
+    x.kid0 = kid0[f];
+    x.kid1 = kid1[f];
+    x.off = off[f];
+    x.dptr = s.dof_ptr[f];
+    x.aptr = s.asm_ptr[f];
+    x.aend = s.asm_ptr[f + 1];
+    x.eptr = s.ea_ptr[f];
+  }
+  std::vector<uint8_t> raw(fdh.size() * sizeof(FrontDesc));
+  std::memcpy(raw.data(), fdh.data(), raw.size());
+  desc.upload(raw, st);
+  lfronts.upload(s.level_fronts, st);
+  dofs.upload(s.dofs, st);
+  asm_pos.upload(s.asm_pos, st);
+  asm_csr.upload(s.asm_csr, st);
+  ea_map.upload(s.ea_map, st);
+  piv_off.upload(poff, st);
+  woff.upload(woff_h, st);
+  piv_total = po;
+  work.alloc(std::max<int64_t>(wo, 1));
+  flags.alloc(1);
+  level_max_f.assign(nlevels, 0);
+  level_max_p.assign(nlevels, 0);
+  for (int l = 0; l < nlevels; l++)
+    for (int k = s.level_ptr[l]; k < s.level_ptr[l + 1]; k++) {
+      level_max_f[l] = std::max(level_max_f[l], s.f[s.level_fronts[k]]);
+      level_max_p[l] = std::max(level_max_p[l], s.p[s.level_fronts[k]]);
+    }
+}
+
+void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, double cb, bool cholesky,
+                      MFFactor& out) {
+  cudaStream_t st = c.stream;
+  DBuf<double>& Fbuf = out.F;
+  if (Fbuf.n != (size_t)std::max<int64_t>(mat_total, 1)) Fbuf.alloc(std::max<int64_t>(mat_total, 1));
+  if (out.piv.n != (size_t)std::max<int64_t>(piv_total, 1)) out.piv.alloc(std::max<int64_t>(piv_total, 1));
+  FEM2D_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), st));
+  const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
+  for (int l = 0; l < nlevels; l++) {
+    const int nfl = level_ptr[l + 1] - level_ptr[l];
+    const int32_t* lf = lfronts.p + level_ptr[l];
+    FEM2D_CUDA(cudaMemsetAsync(Fbuf.p + level_off[l], 0, (level_off[l + 1] - level_off[l]) * sizeof(double), st));
+    mf_assemble_kernel<<<dim3(8, nfl), 256, 0, st>>>(lf, fd, asm_pos.p, asm_csr.p, va, vb, ca, cb, Fbuf.p);
+    c.launches++;
+    if (l > 0) {
+      for (int slot = 0; slot < 2; slot++) {
+        mf_extend_add_kernel<<<dim3(16, nfl), 256, 0, st>>>(lf, fd, slot, ea_map.p, Fbuf.p);
+        c.launches++;
+      }
+    }
+    const int mf = level_max_f[l], mp = level_max_p[l];
+    for (int k0 = 0; k0 < mp; k0 += PANEL) {
+      mf_panel_kernel<<<nfl, 256, 0, st>>>(lf, fd, k0, cholesky ? 0 : 1, Fbuf.p, out.piv.p, piv_off.p, flags.p);
+      const int rest = mf - k0;   // upper bound of remaining columns
+      if (rest > 0) {
+        dim3 gt((rest + 127) / 128, nfl);
+        mf_trsm_kernel<<<gt, 128, 0, st>>>(lf, fd, k0, Fbuf.p);
+        dim3 gg((rest + 63) / 64, (rest + 63) / 64, nfl);
+        mf_gemm_kernel<<<gg, 256, 0, st>>>(lf, fd, k0, Fbuf.p);
+        c.launches += 2;
+      }
+      c.launches++;
+    }
+  }
+  FEM2D_CUDA(cudaGetLastError());
+  out.flags = read_flags(c);
+}
+
+void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, double* X, int64_t ldx, int nb) {
+  const DBuf<double>& Fbuf = fac.F;
+  cudaStream_t st = c.stream;
+  if (nb > nb_cap) fail(FEM2D_E_INVALID_ARG, "solve block wider than the workspace");
+  const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
+  for (int l = 0; l < nlevels; l++) {
+    const int nfl = level_ptr[l + 1] - level_ptr[l];
+    mf_forward_kernel<<<nfl, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, ea_map.p, fac.piv.p, piv_off.p, woff.p,
+                                           Fbuf.p, B, ldb, nb, work.p);
+    c.launches++;
+  }
+  for (int l = nlevels - 1; l >= 0; l--) {
+    const int nfl = level_ptr[l + 1] - level_ptr[l];
+    mf_backward_kernel<<<nfl, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, woff.p, Fbuf.p, work.p, nb, X, ldx);
+    c.launches++;
+  }
+  FEM2D_CUDA(cudaGetLastError());
+}
+
+int MFDevice::read_flags(Ctx& c) {
+  int h = 0;
+  FEM2D_CUDA(cudaMemcpyAsync(&h, flags.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+  return h;
+}
+
+}  // namespace fem2d

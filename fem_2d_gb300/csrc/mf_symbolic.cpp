@@ -1,0 +1,188 @@
+// Symbolic phase of the multifrontal factorization (see mf.h).
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <functional>
+
+#include "common.h"
+#include "domain.h"
+#include "gep.h"
+#include "mf.h"
+
+namespace fem2d {
+
+void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
+  const Mesh& m = d.mesh;
+  const int64_t n = g.n;
+  const int R = (int)m.roots.size();
+  s = MFSymbolic();
+  s.n = n;
+  if (n == 0) return;
+
+  // ---- nested dissection of the base Elems by coordinate bisection (postorder node ids)
+  std::vector<double> cx(R), cy(R);
+  for (int r = 0; r < R; r++) {
+    cx[r] = 0.5 * (m.roots[r].x0 + m.roots[r].x3);
+    cy[r] = 0.5 * (m.roots[r].y0 + m.roots[r].y3);
+  }
+  std::vector<int32_t> parent, first_desc;
+  std::vector<std::array<int32_t, 2>> kids;
+  std::vector<int32_t> leaf_of(R, -1);
+  std::function<int32_t(std::vector<int>&)> build = [&](std::vector<int>& roots) -> int32_t {
+    std::array<int32_t, 2> ch = {-1, -1};
+    int32_t first = (int32_t)parent.size();
+    if (roots.size() > 1) {
+      double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+      for (int r : roots) {
+        x0 = std::min(x0, cx[r]); x1 = std::max(x1, cx[r]);
+        y0 = std::min(y0, cy[r]); y1 = std::max(y1, cy[r]);
+      }
+      bool by_x = (x1 - x0) >= (y1 - y0);
+      std::stable_sort(roots.begin(), roots.end(), [&](int a, int b) {
+        double ka = by_x ? cx[a] : cy[a], kb = by_x ? cx[b] : cy[b];
+        if (ka != kb) return ka < kb;
+        double la = by_x ? cy[a] : cx[a], lb = by_x ? cy[b] : cx[b];
+        return la != lb ? la < lb : a < b;
+      });
+      size_t half = roots.size() / 2;
+      std::vector<int> lo(roots.begin(), roots.begin() + half), hi(roots.begin() + half, roots.end());
+      ch[0] = build(lo);
+      ch[1] = build(hi);
+    }
+    int32_t id = (int32_t)parent.size();
+    parent.push_back(-1);
+    first_desc.push_back(first);
+    kids.push_back(ch);
+    if (ch[0] >= 0) { parent[ch[0]] = id; parent[ch[1]] = id; }
+    if (roots.size() == 1) leaf_of[roots[0]] = id;
+    return id;
+  };
+  std::vector<int> all(R);
+  for (int r = 0; r < R; r++) all[r] = r;
+  build(all);
+  const int NF = (int)parent.size();
+  auto is_proper_anc = [&](int32_t a, int32_t x) { return a > x && first_desc[a] <= x; };
+  auto lca = [&](int32_t a, int32_t b) {
+    while (a != b) {
+      if (a < b) a = parent[a];
+      else b = parent[b];
+    }
+    return a;
+  };
+
+  // ---- DoF -> front: the leaf of its tree, or the common ancestor of the two trees it spans
+  std::vector<int32_t> node(n, -1);
+  for (size_t e = 0; e + 1 < d.spec_ptr.size(); e++) {
+    int32_t lf = leaf_of[m.elems[e].root];
+    for (int64_t k = d.spec_ptr[e]; k < d.spec_ptr[e + 1]; k++) {
+      int32_t dof = d.specs[k].dof;
+      node[dof] = node[dof] < 0 ? lf : lca(node[dof], lf);
+    }
+  }
+  std::vector<std::vector<int32_t>> piv(NF);
+  for (int64_t x = 0; x < n; x++) {
+    if (node[x] < 0) fail(FEM2D_E_INVALID_ARG, "a DoF has no basis spec");
+    piv[node[x]].push_back((int32_t)x);
+  }
+  std::vector<int64_t> order(n);
+  {
+    int64_t k = 0;
+    for (int f = 0; f < NF; f++)
+      for (int32_t x : piv[f]) order[x] = k++;
+  }
+
+  // ---- struct sets (bottom-up)
+  std::vector<std::vector<int32_t>> st(NF);
+  std::vector<int32_t> mark(n, -1);
+  for (int f = 0; f < NF; f++) {
+    std::vector<int32_t> cand;
+    auto add = [&](int32_t y) {
+      if (mark[y] == f) return;
+      if (!is_proper_anc(node[y], f)) return;
+      mark[y] = f;
+      cand.push_back(y);
+    };
+    for (int32_t x : piv[f])
+      for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) add(g.col[k]);
+    for (int c = 0; c < 2; c++)
+      if (kids[f][c] >= 0)
+        for (int32_t y : st[kids[f][c]]) add(y);
+    std::sort(cand.begin(), cand.end(), [&](int32_t a, int32_t b) { return order[a] < order[b]; });
+    st[f] = std::move(cand);
+  }
+
+  // ---- fronts, maps, levels
+  s.nfronts = NF;
+  s.parent = parent;
+  s.f.resize(NF);
+  s.p.resize(NF);
+  s.level.assign(NF, 0);
+  s.dof_ptr.assign(NF + 1, 0);
+  for (int f = 0; f < NF; f++) {
+    s.p[f] = (int32_t)piv[f].size();
+    s.f[f] = (int32_t)(piv[f].size() + st[f].size());
+    s.dof_ptr[f + 1] = s.dof_ptr[f] + s.f[f];
+    if (kids[f][0] >= 0) s.level[f] = 1 + std::max(s.level[kids[f][0]], s.level[kids[f][1]]);
+    s.max_f = std::max(s.max_f, s.f[f]);
+    s.max_p = std::max(s.max_p, s.p[f]);
+    double F = s.f[f], P = s.p[f];
+    s.flops += 2.0 * (F * F * F - (F - P) * (F - P) * (F - P)) / 3.0;
+  }
+  s.dofs.resize(s.dof_ptr[NF]);
+  s.mat_off.resize(NF + 1);
+  s.mat_off[0] = 0;
+  for (int f = 0; f < NF; f++) {
+    std::copy(piv[f].begin(), piv[f].end(), s.dofs.begin() + s.dof_ptr[f]);
+    std::copy(st[f].begin(), st[f].end(), s.dofs.begin() + s.dof_ptr[f] + piv[f].size());
+    s.mat_off[f + 1] = s.mat_off[f] + (int64_t)s.f[f] * s.f[f];
+  }
+  s.mat_total = s.mat_off[NF];
+  std::vector<int32_t> pos(n, -1);
+  s.asm_ptr.assign(NF + 1, 0);
+  s.ea_ptr.assign(NF + 1, 0);
+  std::vector<std::vector<int32_t>> ea(NF);
+  for (int f = 0; f < NF; f++) {
+    const int32_t* D = s.dofs.data() + s.dof_ptr[f];
+    const int F = s.f[f], P = s.p[f];
+    for (int i = 0; i < F; i++) pos[D[i]] = i;
+    for (int i = 0; i < P; i++) {
+      int32_t x = D[i];
+      for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) {
+        // entries whose column was eliminated in a descendant front were assembled there
+        const int32_t nc = node[g.col[k]];
+        if (nc < f && nc >= first_desc[f]) continue;
+        int32_t pc = pos[g.col[k]];
+        if (pc < 0) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: coupling outside the front");
+        s.asm_pos.push_back((int64_t)i * F + pc);
+        s.asm_csr.push_back(k);
+        if (pc >= P) {
+          s.asm_pos.push_back((int64_t)pc * F + i);
+          s.asm_csr.push_back(k);
+        }
+      }
+    }
+    s.asm_ptr[f + 1] = (int64_t)s.asm_pos.size();
+    for (int c = 0; c < 2; c++) {
+      int32_t ch = kids[f][c];
+      if (ch < 0) continue;
+      for (int32_t y : st[ch]) {
+        if (pos[y] < 0) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: child update outside the parent front");
+        ea[ch].push_back(pos[y]);
+      }
+    }
+    for (int i = 0; i < F; i++) pos[D[i]] = -1;
+  }
+  for (int f = 0; f < NF; f++) s.ea_ptr[f + 1] = s.ea_ptr[f] + (int64_t)ea[f].size();
+  s.ea_map.reserve(s.ea_ptr[NF]);
+  for (int f = 0; f < NF; f++) s.ea_map.insert(s.ea_map.end(), ea[f].begin(), ea[f].end());
+  s.nlevels = 0;
+  for (int f = 0; f < NF; f++) s.nlevels = std::max(s.nlevels, s.level[f] + 1);
+  s.level_ptr.assign(s.nlevels + 1, 0);
+  for (int f = 0; f < NF; f++) s.level_ptr[s.level[f] + 1]++;
+  for (int l = 0; l < s.nlevels; l++) s.level_ptr[l + 1] += s.level_ptr[l];
+  s.level_fronts.resize(NF);
+  std::vector<int32_t> cur(s.level_ptr.begin(), s.level_ptr.end() - 1);
+  for (int f = 0; f < NF; f++) s.level_fronts[cur[s.level[f]]++] = f;
+}
+
+}  // namespace fem2d

@@ -1,0 +1,38 @@
+// Device side of the multifrontal factorization (mf.cu).
+#pragma once
+#include <cstring>
+#include <vector>
+
+#include "device.h"
+#include "mf.h"
+
+namespace fem2d {
+
+// One numeric factorization: dense fronts and their row pivots.
+struct MFFactor {
+  DBuf<double> F;
+  DBuf<int32_t> piv;
+  int flags = 0;   // 1: a zero pivot was perturbed, 2: a non-positive pivot in Cholesky mode
+};
+
+struct MFDevice {
+  int nf = 0, nlevels = 0, max_f = 0, max_p = 0, nb_cap = 0;
+  int64_t mat_total = 0, piv_total = 0;
+  std::vector<int32_t> level_ptr;
+  std::vector<int64_t> level_off;
+  std::vector<int32_t> level_max_f, level_max_p;
+  DBuf<uint8_t> desc;
+  DBuf<int32_t> lfronts, dofs, ea_map;
+  DBuf<int64_t> asm_pos, asm_csr, piv_off, woff;
+  DBuf<double> work;
+  DBuf<int> flags;
+
+  void setup(Ctx& c, const MFSymbolic& s, int nb_max);
+  // factor c_a*A + c_b*B (values in full-CSR order); Cholesky mode skips pivoting (SPD shifts)
+  void factor(Ctx& c, const double* va, const double* vb, double ca, double cb, bool cholesky, MFFactor& out);
+  // X = K^-1 B for an n x nb row-major block (nb <= nb_cap); B and X must not alias
+  void solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, double* X, int64_t ldx, int nb);
+  int read_flags(Ctx& c);
+};
+
+}  // namespace fem2d

@@ -100,6 +100,15 @@ int fem2d_domain_basis_specs(const fem2d_domain* d, int64_t* out);
  * Host-only (no device work). Call with rows == cols == NULL to get *nnz_upper first. */
 int fem2d_domain_pattern(const fem2d_domain* d, int64_t* nnz_upper, int32_t* rows, int32_t* cols);
 
+/* Factorization plan of the shifted pencil (host-only): the nested dissection of the base Elems into
+ * dense fronts used by the sparse eigensolver. No reference counterpart (the reference hands the
+ * matrices to an external SLEPc process, slepc_solve.rs:26-36). Two-call pattern: with all array
+ * pointers NULL it fills sizes[8] = {nfronts, dofs_len, asm_len, ea_len, nlevels, max_f, max_p,
+ * factor_entries}; then fronts[4*nfronts] = {parent, level, f, p} and the CSR-style lists. */
+int fem2d_domain_factor_plan(const fem2d_domain* d, int64_t* sizes, int32_t* fronts, int64_t* dof_ptr,
+                             int32_t* dofs, int64_t* asm_ptr, int64_t* asm_pos, int64_t* asm_csr, int64_t* ea_ptr,
+                             int32_t* ea_map);
+
 /* ---------------- device context ---------------- */
 int fem2d_ctx_create(int device, fem2d_ctx** out);
 void fem2d_ctx_destroy(fem2d_ctx* c);
