@@ -1,0 +1,354 @@
+"""Benchmark: Galerkin GEP assembly + sparse eigensolve on one GB300 (fem_2d's hot path).
+
+Workload (default): the precision family - [0,2]x[0,1] meshed as 16x8 base Elems, expansion orders
+(6,6), three seeded rounds refining 30% of the leaves with T/U/V, KOLeg basis, GLQ [10,10]; the
+10 eigenpairs nearest 10.0. A step is one assembly (tables + values on the device) plus one
+gpu_solve_gep (two multifrontal factorizations + the shift-invert block eigensolver).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference] [--workload NAME]
+
+Prints one JSON line. `value` is DoFs/s with the GEP structures already resident in device memory;
+`e2e` is the same metric through the public API from host data (host symbolic phase, uploads and the
+eigenpair download inside the timed region). The reference arm times the CPU restatement of the
+reference's path (the oracle: literal 2-D quadrature assembly on all host threads + FP64 sparse
+shift-invert eigensolve) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "assembly+eigensolve s and DoFs/s, learned vs plain GPU, eig rel err<=1e-9"
+UNIT = "DoFs/s"
+
+
+def workload(name):
+    from fem_2d_gb300 import configs
+
+    if name == "precision":
+        return configs.precision(seed=0)
+    if name == "waveguide":
+        return configs.waveguide_small()
+    if name == "full_small":
+        return configs.full_scale(seed=0, nx=32, ny=16, rounds=3)
+    if name == "full":
+        return configs.full_scale(seed=0)
+    raise SystemExit("unknown workload " + name)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value, ws):
+    """max over ranks (host float); plain pass-through for one process"""
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(prefix="fem2d_clocks_", suffix=".csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for k, nm in enumerate(names):
+                    if p[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def oracle_check(w, gep, res):
+    """FP64 oracle (literal assembly + sparse shift-invert), outside every timed region."""
+    import numpy as np
+
+    from oracle import ref
+
+    om = ref.OracleMesh(w.mesh_json)
+    om.apply_ops(w.ops)
+    n = om.domain()
+    r, c, a, b = om.galerkin(w.basis, w.glq[0], w.glq[1], threads=os.cpu_count() or 4)
+    gr, gc, ga, gb = gep.upper_coo()
+    same = bool(np.array_equal(r, gr) and np.array_equal(c, gc))
+    ea = float(np.max(np.abs(ga - a)) / np.max(np.abs(a)))
+    eb = float(np.max(np.abs(gb - b)) / np.max(np.abs(b)))
+    A = ref.full_sym(n, r, c, a)
+    B = ref.full_sym(n, r, c, b)
+    ws, _, _ = ref.sparse_nearest_physical(A, B, w.target, w.n_pairs)
+    rel = float(np.max(np.abs(res.values - ws) / np.abs(ws)))
+    return {"pattern_bit_exact": same, "entry_err_A": ea, "entry_err_B": eb, "eig_rel_err_max": rel}
+
+
+def cpu_port_step(w, threads):
+    """One step of the CPU restatement: literal 2-D quadrature assembly + FP64 sparse shift-invert."""
+    from oracle import ref
+
+    t0 = time.perf_counter()
+    om = ref.OracleMesh(w.mesh_json)
+    om.apply_ops(w.ops)
+    n = om.domain()
+    r, c, a, b = om.galerkin(w.basis, w.glq[0], w.glq[1], threads=threads)
+    t1 = time.perf_counter()
+    A = ref.full_sym(n, r, c, a)
+    B = ref.full_sym(n, r, c, b)
+    ref.sparse_nearest_physical(A, B, w.target, w.n_pairs, block=w.n_pairs + max(4, w.n_pairs // 2), steps=2,
+                                tol=1e-10)
+    t2 = time.perf_counter()
+    return n, t1 - t0, t2 - t1
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from oracle import build as ob
+
+    ob.build_oracle()
+    w = workload(args.workload)
+    threads = os.cpu_count() or 4
+    for _ in range(args.warmup):
+        cpu_port_step(w, threads)
+    tot, ta, te, n = 0.0, 0.0, 0.0, 0
+    for _ in range(args.steps):
+        n, a, e = cpu_port_step(w, threads)
+        tot += a + e
+        ta += a
+        te += e
+    v = n * args.steps / tot
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh family)",
+           "config": {"workload": w.name, "ndofs": n, "n_pairs": w.n_pairs, "target": w.target},
+           "t_assembly_s": ta / args.steps, "t_eigensolve_s": te / args.steps,
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": "full workload per step: literal 2-D quadrature assembly on %d threads + "
+                                      "FP64 sparse shift-invert (SuperLU + block Krylov, the GPU path's block and depth)" % threads},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_native(args, ws, rank, local):
+    import numpy as np
+
+    import fem_2d_gb300 as fg
+    from fem_2d_gb300 import configs
+
+    w = workload(args.workload)
+    bs = fg.KOLeg if w.basis == 1 else fg.HierPoly
+    ctx = fg.Context(local)
+    mesh = configs.build_mesh(w)
+    dom = fg.Domain.from_mesh(mesh)
+    n = dom.num_dofs
+    gep = fg.galerkin_sample_gep_hcurl(bs, fg.CurlCurl, fg.L2Inner, dom, list(w.glq), ctx=ctx)
+    _, nnz_u, nnz_f = gep.dims()
+
+    def step():
+        ctx.timer_start()
+        gep.recompute()
+        ta = ctx.timer_stop()
+        ctx.timer_start()
+        res = fg.gpu_solve_gep_n(gep, w.target, w.n_pairs)
+        te = ctx.timer_stop()
+        return ta, te, res
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    barrier(ws)
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    l0 = ctx.kernel_launches
+    t_asm = t_eig = 0.0
+    res = None
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        ctx.synchronize()
+        ta, te, res = step()
+        t_asm += ta
+        t_eig += te
+    ctx.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = ctx.kernel_launches - l0
+    clocks = sampler.stop() if sampler else None
+    barrier(ws)
+    ms_step = barrier_max((t_asm + t_eig) / args.steps, ws)
+    value = ws * n / (ms_step / 1e3)
+
+    # end to end through the public API from host data
+    e2e_ms = 0.0
+    h2d = d2h = 0
+    for _ in range(max(1, args.steps)):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        d2 = fg.Domain.from_mesh(mesh)
+        g2 = fg.galerkin_sample_gep_hcurl(bs, fg.CurlCurl, fg.L2Inner, d2, list(w.glq), ctx=ctx)
+        r2 = fg.gpu_solve_gep_n(g2, w.target, w.n_pairs)
+        e2e_ms += 1e3 * (time.perf_counter() - t0)
+        h2d = g2.h2d_bytes + 8 * n * (w.n_pairs + max(4, w.n_pairs // 2))
+        d2h = 8 * w.n_pairs * (n + 2)
+        del g2, d2, r2
+    e2e_ms = barrier_max(e2e_ms / max(1, args.steps), ws)
+    e2e = ws * n / (e2e_ms / 1e3)
+
+    # profiling pass (one extra step, per-region CUDA events) for the roofline
+    ctx.profile_reset()
+    ctx.set_profiling(True)
+    step()
+    ctx.set_profiling(False)
+    regions = {}
+    for reg in ("assembly_values", "spmm", "mf_factor", "mf_forward", "mf_backward"):
+        regions[reg] = ctx.profile(reg)
+    dom_name = max(regions, key=lambda k: regions[k]["ms"])
+    hbm, peak_kind = peaks()
+
+    def roof(reg):
+        r = regions[reg]
+        if r["count"] == 0 or r["ms"] <= 0:
+            return None
+        achieved = r["bytes"] / (r["ms"] / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "launches": r["count"], "avg_launch_ms": r["ms"] / r["count"],
+                "alg_bytes_per_launch": r["bytes"] / r["count"], "peak_source": peak_kind}
+
+    roofline = roof(dom_name)
+    traffic = profile_traffic().get(dom_name)
+    roofline["kernel"] = dom_name
+    roofline["traffic"] = traffic
+    share = {k: regions[k]["ms"] for k in regions}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh family)",
+           "config": {"workload": w.name, "ndofs": n, "nnz_upper": nnz_u, "nnz_full": nnz_f,
+                      "visits": gep.num_visits, "basis": "KOLeg" if w.basis == 1 else "HierPoly",
+                      "glq": list(w.glq), "n_pairs": w.n_pairs, "target": w.target, "seed": w.seed,
+                      "precond": "exact multifrontal shift-invert (learned preconditioner not built)",
+                      "l2": "256 MiB device write between timed steps", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+           "t_assembly_s": t_asm / args.steps / 1e3, "t_eigensolve_s": t_eig / args.steps / 1e3,
+           "wall_s_timed": wall, "gpu_launches": launches,
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                   "ms_per_step": e2e_ms},
+           "roofline": roofline, "region_ms_profiled": share,
+           "assembly_roofline": roof("assembly_values"),
+           "solve_stats": res.stats if res is not None else None,
+           "max_rel_residual": float(np.max(res.residuals)) if res is not None else None,
+           "clocks": clocks}
+    if rank == 0 and not args.no_check:
+        out["parity"] = oracle_check(w, gep, res)
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 4
+        cn, ca_, ce = cpu_port_step(w, threads)
+        out["cpu_baseline"] = {"value": cn / (ca_ + ce), "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": "one full step of the workload: literal 2-D quadrature assembly "
+                                         "(%.2f s) + FP64 sparse shift-invert (%.2f s)" % (ca_, ce)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="precision")
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_native(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -98,7 +98,14 @@ def lib():
         "fem2d_gep_export_csr": (ctypes.c_int, [P, ctypes.c_int, i64p, i32p, dp]),
         "fem2d_gep_timings": (ctypes.c_int, [P, dp]),
         "fem2d_gep_num_visits": (i64, [P]),
+        "fem2d_gep_h2d_bytes": (i64, [P]),
+        "fem2d_ctx_timer_start": (ctypes.c_int, [P]),
+        "fem2d_ctx_timer_stop": (ctypes.c_int, [P, dp]),
+        "fem2d_ctx_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
+        "fem2d_ctx_profile_reset": (ctypes.c_int, [P]),
+        "fem2d_ctx_profile_query": (ctypes.c_int, [P, ctypes.c_char_p, dp, i64p, dp]),
         "fem2d_dense_solve_gep": (ctypes.c_int, [P, P, d, dp, dp]),
+        "fem2d_gep_shifted_solve": (ctypes.c_int, [P, P, d, d, ctypes.c_int, ctypes.c_int, dp, dp]),
         "fem2d_gpu_solve_gep": (ctypes.c_int, [P, P, d, ctypes.c_int, ctypes.POINTER(_fem2d_solve_opts), dp, dp, dp,
                                                 ctypes.POINTER(_fem2d_solve_stats)]),
     }
@@ -391,6 +398,26 @@ class Context:
     def kernel_launches(self):
         return lib().fem2d_ctx_kernel_launches(self._h)
 
+    def timer_start(self):
+        _check(lib().fem2d_ctx_timer_start(self._h))
+
+    def timer_stop(self):
+        ms = ctypes.c_double()
+        _check(lib().fem2d_ctx_timer_stop(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on):
+        _check(lib().fem2d_ctx_set_profiling(self._h, 1 if on else 0))
+
+    def profile_reset(self):
+        _check(lib().fem2d_ctx_profile_reset(self._h))
+
+    def profile(self, region):
+        ms, cnt, by = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        _check(lib().fem2d_ctx_profile_query(self._h, region.encode(), ctypes.byref(ms), ctypes.byref(cnt),
+                                             ctypes.byref(by)))
+        return {"ms": ms.value, "count": cnt.value, "bytes": by.value}
+
 
 class GEP:
     """A generalized eigenproblem whose A and B live in device memory (linalg.rs:29-57)."""
@@ -416,6 +443,10 @@ class GEP:
     @property
     def num_visits(self):
         return lib().fem2d_gep_num_visits(self._h)
+
+    @property
+    def h2d_bytes(self):
+        return lib().fem2d_gep_h2d_bytes(self._h)
 
     def recompute(self):
         _check(lib().fem2d_gep_recompute(self.ctx._h, self._h))
@@ -443,6 +474,16 @@ class GEP:
         _check(lib().fem2d_gep_export_csr(self._h, 0 if which in ("A", 0) else 1, _ptr(rp, ctypes.c_int64),
                                           _ptr(col, ctypes.c_int32), _ptr(val, ctypes.c_double)))
         return rp, col, val
+
+    def shifted_solve(self, c_a, c_b, rhs, spd=False):
+        """Solve (c_a A + c_b B) X = rhs (n or n x k) on the device with the multifrontal LU."""
+        r = np.ascontiguousarray(np.asarray(rhs, dtype=np.float64))
+        one = r.ndim == 1
+        r2 = r.reshape(len(r), -1)
+        x = np.zeros_like(r2)
+        _check(lib().fem2d_gep_shifted_solve(self.ctx._h, self._h, float(c_a), float(c_b), 1 if spd else 0,
+                                             r2.shape[1], _ptr(r2, ctypes.c_double), _ptr(x, ctypes.c_double)))
+        return x[:, 0] if one else x
 
     def scipy(self):
         import scipy.sparse as sp

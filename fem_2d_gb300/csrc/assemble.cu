@@ -61,7 +61,7 @@ __device__ double shape(int basis, int family, int a, double x) {
     if (a == 0) return family == 2 ? 1.0 - x : -1.0;
     if (a == 1) return family == 2 ? 1.0 + x : 1.0;
   }
-  double l0 = 1.0, l1 = x, d0 = 0.0, d1 = 1.0;
+  double l0 = 1.0, l1 = x, d1 = 1.0;
   double accv = 0.0, accd = 0.0;
   const bool want_q = family >= 2;
   const int idx = a - 2;
@@ -74,7 +74,7 @@ __device__ double shape(int basis, int family, int a, double x) {
       const double f = (double)k;
       lk = ((2.0 * f - 1.0) * x * l1 - (f - 1.0) * l0) / f;
       dk = f * l1 + x * d1;
-      l0 = l1; l1 = lk; d0 = d1; d1 = dk;
+      l0 = l1; l1 = lk; d1 = dk;
     }
     if (want_q) {
       const double w = q_numerator(idx, k) / (double)c_qden[idx];
@@ -84,7 +84,6 @@ __device__ double shape(int basis, int family, int a, double x) {
       return family == 0 ? lk : dk;
     }
   }
-  (void)d0;
   return family == 2 ? accv * c_euc[idx] : accd * c_euc[idx];
 }
 
@@ -203,6 +202,7 @@ void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, f
   c.launches++;
   FEM2D_CUDA(cudaEventRecord(e1, s));
   if (g.nnz_full > 0) {
+    ProfScope ps(c, "assembly_values", 16.0 * g.nnz_full + 8.0 * (g.nnz_full + 1) + 8.0 * g.codes.size());
     const int threads = 256;
     int64_t want = (g.nnz_full + threads - 1) / threads;
     int64_t cap = (int64_t)c.num_sms * 8 * 4;   // persistent-ish grid: 8 blocks/SM x 4 waves

@@ -287,6 +287,8 @@ int fem2d_ctx_create(int device, fem2d_ctx** out) {
 void fem2d_ctx_destroy(fem2d_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->c.device);
+  if (c->c.t0) cudaEventDestroy(c->c.t0);
+  if (c->c.t1) cudaEventDestroy(c->c.t1);
   if (c->c.flush_buf) cudaFree(c->c.flush_buf);
   if (c->c.stream) cudaStreamDestroy(c->c.stream);
   delete c;
@@ -311,6 +313,53 @@ int fem2d_ctx_flush_l2(fem2d_ctx* c) {
 }
 
 int64_t fem2d_ctx_kernel_launches(const fem2d_ctx* c) { return c ? c->c.launches : -1; }
+
+int fem2d_ctx_timer_start(fem2d_ctx* c) {
+  API_BEGIN
+  if (!c) fail(FEM2D_E_INVALID_ARG, "null context");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  if (!c->c.t0) FEM2D_CUDA(cudaEventCreate(&c->c.t0));
+  if (!c->c.t1) FEM2D_CUDA(cudaEventCreate(&c->c.t1));
+  FEM2D_CUDA(cudaEventRecord(c->c.t0, c->c.stream));
+  API_END
+}
+
+int fem2d_ctx_timer_stop(fem2d_ctx* c, double* ms) {
+  API_BEGIN
+  if (!c || !ms || !c->c.t0) fail(FEM2D_E_INVALID_ARG, "timer not started");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  FEM2D_CUDA(cudaEventRecord(c->c.t1, c->c.stream));
+  FEM2D_CUDA(cudaEventSynchronize(c->c.t1));
+  float f = 0;
+  FEM2D_CUDA(cudaEventElapsedTime(&f, c->c.t0, c->c.t1));
+  *ms = f;
+  API_END
+}
+
+int fem2d_ctx_set_profiling(fem2d_ctx* c, int on) {
+  API_BEGIN
+  if (!c) fail(FEM2D_E_INVALID_ARG, "null context");
+  c->c.profile = on != 0;
+  API_END
+}
+
+int fem2d_ctx_profile_reset(fem2d_ctx* c) {
+  API_BEGIN
+  if (!c) fail(FEM2D_E_INVALID_ARG, "null context");
+  c->c.prof.clear();
+  API_END
+}
+
+int fem2d_ctx_profile_query(const fem2d_ctx* c, const char* region, double* ms, int64_t* count, double* bytes) {
+  API_BEGIN
+  if (!c || !region) fail(FEM2D_E_INVALID_ARG, "null argument");
+  auto it = c->c.prof.find(region);
+  ProfRec r = it == c->c.prof.end() ? ProfRec() : it->second;
+  if (ms) *ms = r.ms;
+  if (count) *count = r.count;
+  if (bytes) *bytes = r.bytes;
+  API_END
+}
 
 // ------------------------------------------------------------------ galerkin
 int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int basis, int nq_u, int nq_v,
@@ -376,6 +425,7 @@ int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64
 }
 
 int64_t fem2d_gep_num_visits(const fem2d_gep* g) { return g ? g->h.visits : -1; }
+int64_t fem2d_gep_h2d_bytes(const fem2d_gep* g) { return g ? g->d.h2d_bytes : -1; }
 
 int fem2d_gep_timings(const fem2d_gep* g, double* out) {
   API_BEGIN
@@ -436,6 +486,15 @@ int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, doubl
   if (!c || !g) fail(FEM2D_E_INVALID_ARG, "null argument");
   FEM2D_CUDA(cudaSetDevice(c->c.device));
   dense_solve(c->c, g->dom, g->h, g->d, target, value, vector);
+  API_END
+}
+
+int fem2d_gep_shifted_solve(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, int spd, int nrhs,
+                            const double* rhs, double* x) {
+  API_BEGIN
+  if (!c || !g || !rhs || !x || nrhs <= 0) fail(FEM2D_E_INVALID_ARG, "invalid argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  shifted_solve(c->c, g->dom, g->h, g->d, c_a, c_b, spd != 0, nrhs, rhs, x);
   API_END
 }
 

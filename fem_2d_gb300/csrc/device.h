@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -18,12 +19,47 @@ namespace fem2d {
       ::fem2d::fail(FEM2D_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));            \
   } while (0)
 
+struct ProfRec {
+  double ms = 0, bytes = 0;
+  int64_t count = 0;
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int64_t launches = 0;        // kernels launched by this library on this context
   void* flush_buf = nullptr;   // 256 MiB, for L2 flushes between timed repetitions
   int num_sms = 0;
+  bool profile = false;        // time named regions with events (synchronising) when set
+  std::map<std::string, ProfRec> prof;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+// Times a region on the context's stream with CUDA events when profiling is enabled.
+struct ProfScope {
+  Ctx& c;
+  const char* name;
+  double bytes;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(Ctx& ctx, const char* n, double by) : c(ctx), name(n), bytes(by) {
+    if (!c.profile) return;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, c.stream);
+  }
+  ~ProfScope() {
+    if (!c.profile) return;
+    cudaEventRecord(b, c.stream);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    ProfRec& r = c.prof[name];
+    r.ms += ms;
+    r.bytes += bytes;
+    r.count++;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
 };
 
 // A device buffer owned by this library.

@@ -4,8 +4,10 @@
 // (A, B) nearest the target sigma among the non-spurious spectrum. The curl-curl operator has a large
 // null space (gradients, lambda = 0) which sits at distance |sigma| from the target; the reference
 // treats such modes as spurious (nalgebra_solve.rs:24-26). The search space is generated with
-//     T = (A - sigma B)^-1 A (A + sigma B)^-1 B,   eigenvalues lambda / (lambda^2 - sigma^2),
-// which maps null-space vectors to zero and damps high-frequency modes, using exact multifrontal
+//     T = (A - sigma B)^-1 A (A + c B)^-1 B
+// with c = 0.05 |sigma|: eigenvalue lambda / ((lambda - sigma)(lambda + c)), close to the plain
+// shift-invert 1 / (lambda - sigma) for every physical mode, zero on the null space (A kills it
+// whatever the accuracy of the SPD solve) and small for high-frequency modes; exact multifrontal
 // solves (mf.cu). Each cycle builds a block Krylov basis [X, TX, T^2 X] B-orthonormalised by CGS2
 // in FP64, then a Rayleigh-Ritz step on the pencil (A, B) itself (FP64); Ritz pairs with a relative
 // residual above 1 (mixtures of null-space and high-frequency directions that land near sigma) are
@@ -186,6 +188,8 @@ struct Dev {
   int grid_rows() const { return std::max(1, c.num_sms * 2); }
 
   void spmm(double ca, double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
+    const double nv = (ca != 0.0) + (cb != 0.0);
+    ProfScope ps(c, "spmm", (double)h.nnz_full * (4.0 + 8.0 * nv) + 8.0 * (h.n + 1) + 16.0 * h.n * nb);
     for (int c0 = 0; c0 < nb; c0 += 32) {
       const int w = std::min(32, nb - c0);
       int G = 1;
@@ -287,9 +291,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   mf.setup(c, sym, 32);
   MFFactor fm, fp;
   mf.factor(c, d.a.p, d.b.p, 1.0, -sigma, false, fm);
-  // A + |sigma| B is SPD: factored without pivoting
-  mf.factor(c, d.a.p, d.b.p, 1.0, std::fabs(sigma), true, fp);
-  if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + |sigma| B is not positive definite; B is likely ill-conditioned");
+  // A + c B (c > 0) is SPD: factored without pivoting
+  const double cshift = 0.05 * std::fabs(sigma);
+  mf.factor(c, d.a.p, d.b.p, 1.0, cshift, true, fp);
+  if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + c B is not positive definite; B is likely ill-conditioned");
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t1 = std::chrono::steady_clock::now();
 
@@ -530,6 +535,37 @@ void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d
   if (value) *value = w[best];
   if (vector)
     for (int64_t i = 0; i < n; i++) vector[i] = z[(size_t)i * n + best];
+}
+
+}  // namespace fem2d
+
+namespace fem2d {
+
+void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double ca, double cb, bool spd,
+                   int nrhs, const double* rhs, double* x) {
+  const int64_t n = h.n;
+  MFSymbolic sym;
+  mf_symbolic(dom, h, sym);
+  MFDevice mf;
+  mf.setup(c, sym, 32);
+  MFFactor fac;
+  mf.factor(c, d.a.p, d.b.p, ca, cb, spd, fac);
+  if (spd && (fac.flags & 2)) fail(FEM2D_E_B_NOT_SPD, "the shifted matrix is not positive definite");
+  DBuf<double> R, X;
+  R.alloc((size_t)n * 32);
+  X.alloc((size_t)n * 32);
+  std::vector<double> hr((size_t)n * 32), hx((size_t)n * 32);
+  for (int c0 = 0; c0 < nrhs; c0 += 32) {
+    const int w = std::min(32, nrhs - c0);
+    for (int64_t i = 0; i < n; i++)
+      for (int k = 0; k < w; k++) hr[(size_t)i * 32 + k] = rhs[(size_t)i * nrhs + c0 + k];
+    FEM2D_CUDA(cudaMemcpyAsync(R.p, hr.data(), hr.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    mf.solve(c, fac, R.p, 32, X.p, 32, w);
+    FEM2D_CUDA(cudaMemcpyAsync(hx.data(), X.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+    for (int64_t i = 0; i < n; i++)
+      for (int k = 0; k < w; k++) x[(size_t)i * nrhs + c0 + k] = hx[(size_t)i * 32 + k];
+  }
 }
 
 }  // namespace fem2d

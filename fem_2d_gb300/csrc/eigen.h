@@ -11,4 +11,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
                   const fem2d_solve_opts& o, double* values, double* vectors, double* residuals,
                   fem2d_solve_stats* st);
 
+void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double ca, double cb, bool spd,
+                   int nrhs, const double* rhs, double* x);
+
 }  // namespace fem2d

@@ -7,10 +7,13 @@
 // (or no pivoting in Cholesky mode for SPD shifts): panel (one CTA per front), unit-lower TRSM for
 // the U12 rows, FP64 GEMM update of the trailing block. The trailing (f-p)x(f-p) block left in place
 // is the update matrix for the parent.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
+
+namespace cg = cooperative_groups;
 
 #include "mfdev.h"
 
@@ -215,26 +218,56 @@ __global__ void __launch_bounds__(256) mf_gemm_kernel(const int32_t* __restrict_
   }
 }
 
-// ------------------------------------------------------------------ block solves
-// RHS/solution X: row-major n x nb (ld = ldx). Workspace per front: f x nb, column-major.
-__global__ void __launch_bounds__(256) mf_forward_kernel(const int32_t* __restrict__ lf,
-                                                         const FrontDesc* __restrict__ fd,
-                                                         const int32_t* __restrict__ dofs,
-                                                         const int32_t* __restrict__ emap,
-                                                         const int32_t* __restrict__ piv,
-                                                         const int64_t* __restrict__ piv_off,
-                                                         const int64_t* __restrict__ woff,
-                                                         const double* __restrict__ F, const double* __restrict__ B,
-                                                         int64_t ldb, int nb, double* __restrict__ W) {
-  const int fr = lf[blockIdx.x];
+// ------------------------------------------------------------------ cluster block solves
+// One 8-CTA thread-block cluster per front. Rows are owned in interleaved 32-row chunks
+// (chunk q belongs to CTA q % 8). The triangular factors are walked in 32-column blocks: every CTA
+// solves the 32 x nb diagonal block itself (from the rows finalised before the last cluster barrier),
+// then updates the rows it owns; cluster.sync() separates the blocks. The solved block is written
+// back after the barrier, when no CTA reads those rows any more.
+constexpr int CL = 8;
+
+// sequential LAPACK-style row swaps -> gather permutation (v'[i] = v[perm[i]])
+__global__ void mf_perm_kernel(int nf, const FrontDesc* __restrict__ fd, const int32_t* __restrict__ piv,
+                               const int64_t* __restrict__ piv_off, int32_t* __restrict__ perm,
+                               int32_t* __restrict__ iperm) {
+  const int fr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (fr >= nf) return;
+  const int p = fd[fr].p;
+  const int32_t* pv = piv + piv_off[fr];
+  int32_t* pm = perm + piv_off[fr];
+  for (int i = 0; i < p; i++) pm[i] = i;
+  for (int k = 0; k < p; k++) {
+    const int r = pv[k];
+    const int32_t t = pm[k];
+    pm[k] = pm[r];
+    pm[r] = t;
+  }
+  int32_t* ip = iperm + piv_off[fr];
+  for (int i = 0; i < p; i++) ip[pm[i]] = i;
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
+    mf_forward_cluster_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
+                              const int32_t* __restrict__ dofs, const int32_t* __restrict__ emap,
+                              const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
+                              const int64_t* __restrict__ piv_off,
+                              const int64_t* __restrict__ woff, const double* __restrict__ F,
+                              const double* __restrict__ B, int64_t ldb, int nb, double* __restrict__ W) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int fr = lf[blockIdx.x / CL];
   const FrontDesc d = fd[fr];
   const int f = d.f, p = d.p;
   double* v = W + woff[fr];
   const int32_t* D = dofs + d.dptr;
-  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) {
-    const int i = t % f, c = t / f;
-    v[(int64_t)c * f + i] = i < p ? B[(int64_t)D[i] * ldb + c] : 0.0;
-  }
+  const int32_t* pm = perm + piv_off[fr];
+  const int32_t* ipm = iperm + piv_off[fr];
+  const int nchunk = (f + 31) / 32;
+  for (int q = r; q < nchunk; q += CL)
+    for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+      const int i = q * 32 + (t & 31), c = t >> 5;
+      if (i < f) v[(int64_t)c * f + i] = i < p ? B[(int64_t)D[pm[i]] * ldb + c] : 0.0;
+    }
   __syncthreads();
   for (int slot = 0; slot < 2; slot++) {
     const int ch = slot == 0 ? d.kid0 : d.kid1;
@@ -245,67 +278,118 @@ __global__ void __launch_bounds__(256) mf_forward_kernel(const int32_t* __restri
     const int32_t* m = emap + cd.eptr;
     for (int t = threadIdx.x; t < s * nb; t += blockDim.x) {
       const int i = t % s, c = t / s;
-      v[(int64_t)c * f + m[i]] += cw[(int64_t)c * cd.f + cd.p + i];
+      const int row = m[i] < p ? ipm[m[i]] : m[i];   // pivot rows are stored permuted
+      if (((row >> 5) % CL) == r) v[(int64_t)c * f + row] += cw[(int64_t)c * cd.f + cd.p + i];
     }
     __syncthreads();
   }
-  const int32_t* pv = piv + piv_off[fr];
-  for (int k = 0; k < p; k++) {
-    const int pr = pv[k];
-    if (pr != k)
-      for (int c = threadIdx.x; c < nb; c += blockDim.x) {
-        const double t = v[(int64_t)c * f + k];
-        v[(int64_t)c * f + k] = v[(int64_t)c * f + pr];
-        v[(int64_t)c * f + pr] = t;
+  cluster.sync();
+  __shared__ double ys[32][33];
+  __shared__ double Ld[32][33];
+  for (int jb = 0; jb < p; jb += 32) {
+    const int bw = min(32, p - jb);
+    for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+      const int u = t & 31, c = t >> 5;
+      ys[u][c] = u < bw ? v[(int64_t)c * f + jb + u] : 0.0;
+    }
+    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+      const int u = t & 31, k = t >> 5;   // row jb+u, col jb+k
+      Ld[u][k] = (u < bw && k < bw) ? F[d.off + (int64_t)(jb + k) * f + jb + u] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < nb) {
+      const int c = threadIdx.x;
+      for (int u = 0; u < bw; u++) {
+        double s = ys[u][c];
+        for (int k = 0; k < u; k++) s -= Ld[u][k] * ys[k][c];
+        ys[u][c] = s;
       }
-    __syncthreads();
-  }
-  const double* A = F + d.off;
-  for (int k = 0; k < p; k++) {
-    const double* colk = A + (int64_t)k * f;
-    const int nr = f - k - 1;
-    for (int t = threadIdx.x; t < nr * nb; t += blockDim.x) {
-      const int i = k + 1 + t % nr, c = t / nr;
-      v[(int64_t)c * f + i] -= colk[i] * v[(int64_t)c * f + k];
     }
+    __syncthreads();
+    // update owned rows below the block
+    const int first = jb + bw;
+    for (int q = r; q < nchunk; q += CL) {
+      if (q * 32 + 31 < first) continue;
+      for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+        const int i = q * 32 + (t & 31), c = t >> 5;
+        if (i < first || i >= f) continue;
+        double acc = 0.0;
+        for (int u = 0; u < bw; u++) acc += F[d.off + (int64_t)(jb + u) * f + i] * ys[u][c];
+        v[(int64_t)c * f + i] -= acc;
+      }
+    }
+    cluster.sync();
+    // the owner stores the solved block (rows jb.. are read by nobody after the barrier)
+    if (((jb >> 5) % CL) == r)
+      for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+        const int u = t & 31, c = t >> 5;
+        if (u < bw) v[(int64_t)c * f + jb + u] = ys[u][c];
+      }
     __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(256) mf_backward_kernel(const int32_t* __restrict__ lf,
-                                                          const FrontDesc* __restrict__ fd,
-                                                          const int32_t* __restrict__ dofs,
-                                                          const int64_t* __restrict__ woff,
-                                                          const double* __restrict__ F, double* __restrict__ W,
-                                                          int nb, double* __restrict__ X, int64_t ldx) {
-  const int fr = lf[blockIdx.x];
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
+    mf_backward_cluster_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
+                               const int32_t* __restrict__ dofs, const int64_t* __restrict__ woff,
+                               const double* __restrict__ F, double* __restrict__ W, int nb, double* __restrict__ X,
+                               int64_t ldx) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int fr = lf[blockIdx.x / CL];
   const FrontDesc d = fd[fr];
   const int f = d.f, p = d.p;
-  if (p == 0) return;
+  if (p == 0) return;   // uniform across the cluster
   double* v = W + woff[fr];
   const int32_t* D = dofs + d.dptr;
-  const double* A = F + d.off;
-  // y -= U12 x_struct
-  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
-    const int i = t % p, c = t / p;
-    double s = v[(int64_t)c * f + i];
-    for (int j = p; j < f; j++) s -= A[(int64_t)j * f + i] * X[(int64_t)D[j] * ldx + c];
-    v[(int64_t)c * f + i] = s;
-  }
-  __syncthreads();
-  for (int k = p - 1; k >= 0; k--) {
-    const double* colk = A + (int64_t)k * f;
-    if (threadIdx.x < nb) v[(int64_t)threadIdx.x * f + k] /= colk[k];
-    __syncthreads();
-    for (int t = threadIdx.x; t < k * nb; t += blockDim.x) {
-      const int i = t % k, c = t / k;
-      v[(int64_t)c * f + i] -= colk[i] * v[(int64_t)c * f + k];
+  const int nchunk = (p + 31) / 32;
+  // y -= U12 x_struct on owned rows
+  for (int q = r; q < nchunk; q += CL)
+    for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+      const int i = q * 32 + (t & 31), c = t >> 5;
+      if (i >= p) continue;
+      double s = v[(int64_t)c * f + i];
+      for (int j = p; j < f; j++) s -= F[d.off + (int64_t)j * f + i] * X[(int64_t)D[j] * ldx + c];
+      v[(int64_t)c * f + i] = s;
+    }
+  cluster.sync();
+  __shared__ double xs[32][33];
+  __shared__ double Ud[32][33];
+  const int last = ((p - 1) / 32) * 32;
+  for (int jb = last; jb >= 0; jb -= 32) {
+    const int bw = min(32, p - jb);
+    for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+      const int u = t & 31, c = t >> 5;
+      xs[u][c] = u < bw ? v[(int64_t)c * f + jb + u] : 0.0;
+    }
+    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+      const int u = t & 31, k = t >> 5;
+      Ud[u][k] = (u < bw && k < bw) ? F[d.off + (int64_t)(jb + k) * f + jb + u] : 0.0;
     }
     __syncthreads();
-  }
-  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
-    const int i = t % p, c = t / p;
-    X[(int64_t)D[i] * ldx + c] = v[(int64_t)c * f + i];
+    if (threadIdx.x < nb) {
+      const int c = threadIdx.x;
+      for (int u = bw - 1; u >= 0; u--) {
+        double s = xs[u][c];
+        for (int k = u + 1; k < bw; k++) s -= Ud[u][k] * xs[k][c];
+        xs[u][c] = s / Ud[u][u];
+      }
+    }
+    __syncthreads();
+    for (int q = r; q * 32 < jb; q += CL)
+      for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+        const int i = q * 32 + (t & 31), c = t >> 5;
+        if (i >= jb) continue;
+        double acc = 0.0;
+        for (int u = 0; u < bw; u++) acc += F[d.off + (int64_t)(jb + u) * f + i] * xs[u][c];
+        v[(int64_t)c * f + i] -= acc;
+      }
+    if (((jb >> 5) % CL) == r)
+      for (int t = threadIdx.x; t < 32 * nb; t += blockDim.x) {
+        const int u = t & 31, c = t >> 5;
+        if (u < bw) X[(int64_t)D[jb + u] * ldx + c] = xs[u][c];
+      }
+    cluster.sync();
   }
 }
 
@@ -374,10 +458,13 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
   flags.alloc(1);
   level_max_f.assign(nlevels, 0);
   level_max_p.assign(nlevels, 0);
+  level_factor_bytes.assign(nlevels, 0.0);
   for (int l = 0; l < nlevels; l++)
     for (int k = s.level_ptr[l]; k < s.level_ptr[l + 1]; k++) {
+      const double F = s.f[s.level_fronts[k]], P = s.p[s.level_fronts[k]];
       level_max_f[l] = std::max(level_max_f[l], s.f[s.level_fronts[k]]);
       level_max_p[l] = std::max(level_max_p[l], s.p[s.level_fronts[k]]);
+      level_factor_bytes[l] += 8.0 * (0.5 * P * P + P * (F - P));
     }
 }
 
@@ -389,6 +476,7 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
   if (out.piv.n != (size_t)std::max<int64_t>(piv_total, 1)) out.piv.alloc(std::max<int64_t>(piv_total, 1));
   FEM2D_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), st));
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
+  ProfScope ps(c, "mf_factor", 8.0 * (double)mat_total);
   for (int l = 0; l < nlevels; l++) {
     const int nfl = level_ptr[l + 1] - level_ptr[l];
     const int32_t* lf = lfronts.p + level_ptr[l];
@@ -415,6 +503,10 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
       c.launches++;
     }
   }
+  if (out.perm.n != out.piv.n) out.perm.alloc(out.piv.n);
+  if (out.iperm.n != out.piv.n) out.iperm.alloc(out.piv.n);
+  mf_perm_kernel<<<(nf + 127) / 128, 128, 0, st>>>(nf, fd, out.piv.p, piv_off.p, out.perm.p, out.iperm.p);
+  c.launches++;
   FEM2D_CUDA(cudaGetLastError());
   out.flags = read_flags(c);
 }
@@ -426,13 +518,17 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
   for (int l = 0; l < nlevels; l++) {
     const int nfl = level_ptr[l + 1] - level_ptr[l];
-    mf_forward_kernel<<<nfl, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, ea_map.p, fac.piv.p, piv_off.p, woff.p,
-                                           Fbuf.p, B, ldb, nb, work.p);
+    ProfScope ps(c, "mf_forward", level_factor_bytes[l]);
+    mf_forward_cluster_kernel<<<nfl * CL, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, ea_map.p, fac.perm.p,
+                                                        fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, nb,
+                                                        work.p);
     c.launches++;
   }
   for (int l = nlevels - 1; l >= 0; l--) {
     const int nfl = level_ptr[l + 1] - level_ptr[l];
-    mf_backward_kernel<<<nfl, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, woff.p, Fbuf.p, work.p, nb, X, ldx);
+    ProfScope ps(c, "mf_backward", level_factor_bytes[l]);
+    mf_backward_cluster_kernel<<<nfl * CL, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, woff.p, Fbuf.p,
+                                                         work.p, nb, X, ldx);
     c.launches++;
   }
   FEM2D_CUDA(cudaGetLastError());

@@ -12,6 +12,8 @@ namespace fem2d {
 struct MFFactor {
   DBuf<double> F;
   DBuf<int32_t> piv;
+  DBuf<int32_t> perm;    // gather permutation equivalent to the row swaps
+  DBuf<int32_t> iperm;   // its inverse
   int flags = 0;   // 1: a zero pivot was perturbed, 2: a non-positive pivot in Cholesky mode
 };
 
@@ -21,6 +23,7 @@ struct MFDevice {
   std::vector<int32_t> level_ptr;
   std::vector<int64_t> level_off;
   std::vector<int32_t> level_max_f, level_max_p;
+  std::vector<double> level_factor_bytes;   // L (forward) or U (backward) bytes read per level
   DBuf<uint8_t> desc;
   DBuf<int32_t> lfronts, dofs, ea_map;
   DBuf<int64_t> asm_pos, asm_csr, piv_off, woff;

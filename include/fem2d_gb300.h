@@ -117,6 +117,14 @@ int fem2d_ctx_synchronize(fem2d_ctx* c);
 int fem2d_ctx_flush_l2(fem2d_ctx* c);
 /* number of kernels this library launched on the context since creation */
 int64_t fem2d_ctx_kernel_launches(const fem2d_ctx* c);
+/* device timer on the context's stream (CUDA events): start, then stop returns elapsed ms */
+int fem2d_ctx_timer_start(fem2d_ctx* c);
+int fem2d_ctx_timer_stop(fem2d_ctx* c, double* ms);
+/* per-region device timing (synchronising, for measurement runs): regions "assembly_values", "spmm",
+ * "mf_factor", "mf_forward", "mf_backward"; query returns total ms, launches and algorithmic bytes */
+int fem2d_ctx_set_profiling(fem2d_ctx* c, int on);
+int fem2d_ctx_profile_reset(fem2d_ctx* c);
+int fem2d_ctx_profile_query(const fem2d_ctx* c, const char* region, double* ms, int64_t* count, double* bytes);
 
 /* ---------------- Galerkin sampling (src/fem_problem/galerkin.rs:33-187) ---------------- */
 /* galerkin_sample_gep_hcurl::<BSpace, CurlCurl, L2Inner>(&domain, Some([nq_u, nq_v])).
@@ -140,11 +148,20 @@ int fem2d_gep_export_csr(const fem2d_gep* g, int which, int64_t* row_ptr, int32_
 int fem2d_gep_timings(const fem2d_gep* g, double* out3);
 /* visit count P_visits = sum_E [n(E)(n(E)+1)/2 + n(E) sum_D n(D)] (the reference's integrate calls) */
 int64_t fem2d_gep_num_visits(const fem2d_gep* g);
+/* bytes copied host -> device when the GEP was built (pattern, contribution lists, tables) */
+int64_t fem2d_gep_h2d_bytes(const fem2d_gep* g);
 
 /* ---------------- Eigensolvers (src/fem_problem/linalg/{nalgebra_solve,slepc_solve}.rs) ---------------- */
 /* nalgebra_solve_gep (nalgebra_solve.rs:14-50) on the device: B = L L^T, the product B^-1 A, the
  * symmetric eigen-decomposition of its lower triangle, the pair nearest target. ndofs <= 1000. */
 int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, double* value, double* vector);
+
+/* Solve (c_a A + c_b B) X = R for nrhs right-hand sides (host, row-major n x nrhs) with the device
+ * multifrontal LU (partial pivoting within fully-summed rows). No reference counterpart: the
+ * reference only forms the GEP; this is the linear solve its shift-invert eigensolve relies on.
+ * Returns FEM2D_E_B_NOT_SPD if spd != 0 and a non-positive pivot appears. */
+int fem2d_gep_shifted_solve(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, int spd, int nrhs,
+                            const double* rhs, double* x);
 
 typedef struct fem2d_solve_opts {
   int precond;          /* FEM2D_PRECOND_* */

@@ -265,7 +265,7 @@ def _borth_block(W, V, B, drop=1e-8):
 def sparse_nearest_physical(A, B, sigma, k, block=None, steps=3, tol=1e-11, max_cycles=40, spurious=1e-6):
     """FP64 oracle for gpu_solve_gep: the k eigenpairs nearest sigma excluding the curl null space.
 
-    Search space from T = (A - sigma B)^-1 A (A + sigma B)^-1 B with sparse LU solves (scipy SuperLU),
+    Search space from T = (A - sigma B)^-1 A (A + c B)^-1 B, c = 0.05 |sigma|, with sparse LU solves (SuperLU),
     block Krylov cycles with CGS2 B-orthogonalisation, Rayleigh-Ritz on (A, B), Ritz pairs with relative
     residual >= 1 or |theta| <= spurious*|sigma| not selected. Pinned against LAPACK dense solves on
     small meshes (tests/test_oracle_sparse.py).
@@ -273,9 +273,9 @@ def sparse_nearest_physical(A, B, sigma, k, block=None, steps=3, tol=1e-11, max_
     import scipy.sparse.linalg as sla
 
     n = A.shape[0]
-    b = block or min(n, k + max(4, k // 2))
+    b = block or min(n, k + max(8, k))
     luM = sla.splu((A - sigma * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
-    luP = sla.splu((A + abs(sigma) * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
+    luP = sla.splu((A + 0.05 * abs(sigma) * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
 
     def T(X):
         return luM.solve(A @ luP.solve(B @ X))
