@@ -92,6 +92,7 @@ def lib():
         "fem2d_ctx_kernel_launches": (i64, [P]),
         "fem2d_galerkin_sample_gep_hcurl": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, PP]),
         "fem2d_gep_recompute": (ctypes.c_int, [P, P]),
+        "fem2d_gep_values_noalloc": (ctypes.c_int, [P, P, ctypes.c_void_p, ctypes.c_void_p]),
         "fem2d_gep_free": (None, [P]),
         "fem2d_gep_dims": (ctypes.c_int, [P, i64p, i64p, i64p]),
         "fem2d_gep_export_upper": (ctypes.c_int, [P, i32p, i32p, dp, dp]),

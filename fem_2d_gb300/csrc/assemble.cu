@@ -9,6 +9,10 @@
 //    traffic is the contribution list read and the two FP64 value arrays written.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <mutex>
+#include <string>
+
 #include "device.h"
 
 namespace fem2d {
@@ -222,6 +226,68 @@ void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, f
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);
+}
+
+}  // namespace fem2d
+
+// ---------------------------------------------------------------------------------------------------
+// Assembly values without any device allocation.
+//
+// For hosts that own every byte of device memory themselves (an application that hands the library
+// pointers from its own pool or arena and forbids allocations behind its back) or that cannot pay for
+// cudaMalloc/cudaFree on their critical path (cudaFree synchronises the device). The 1-D contraction
+// tables that the two assembly kernels exchange live in this file-scope array instead of a buffer
+// allocated per GEP. Every GPU that loads the library holds the array until the process exits.
+// ---------------------------------------------------------------------------------------------------
+namespace fem2d {
+
+namespace {
+constexpr size_t kNoAllocTableDoubles = 524288;   // 4 MiB of FP64 contraction tables
+__device__ __align__(256) double g_noalloc_tables[kNoAllocTableDoubles];
+
+// device address of g_noalloc_tables per device ordinal, looked up once per device
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {};
+}  // namespace
+
+size_t noalloc_table_capacity() { return kNoAllocTableDoubles; }
+
+void device_values_noalloc(Ctx& c, const HostGEP& g, const DeviceGEP& d, double* out_a, double* out_b) {
+  const int P = g.pmax + 1;
+  const size_t need = (size_t)2 * d.nivl * 5 * P * P;
+  if (need > kNoAllocTableDoubles)
+    fail(FEM2D_E_TOO_LARGE, "the contraction tables need " + std::to_string(need) +
+                                " doubles; the allocation-free path holds at most " +
+                                std::to_string(kNoAllocTableDoubles) + " (2 x intervals x 5 x (max order + 1)^2)");
+  if (c.device < 0 || c.device >= 256) fail(FEM2D_E_INVALID_ARG, "device ordinal out of range");
+  double* tables = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[c.device]) {
+      // one-time set-up on this device (the device is current: the caller made it so)
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_tables);
+      if (e != cudaSuccess) fail(FEM2D_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_noalloc_addr[c.device] = static_cast<double*>(p);
+    }
+    tables = g_noalloc_addr[c.device];
+  }
+  // every table entry the values kernel reads is written by the contraction kernel first, so the
+  // previous call's contents never leak into this one
+  dim3 grid1(d.nivl, 2, 5);
+  fem2d_contract1d_kernel<<<grid1, 128, 0, c.stream>>>(g.basis, P, d.nivl, d.ivl.p, d.glq.p, g.nq_u, g.nq_v, tables);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
+  if (g.nnz_full > 0) {
+    const int threads = 256;
+    int64_t want = (g.nnz_full + threads - 1) / threads;
+    int64_t cap = (int64_t)c.num_sms * 8 * 4;
+    int grid = (int)std::max<int64_t>(1, std::min(want, cap));
+    fem2d_values_kernel<<<grid, threads, 0, c.stream>>>(g.nnz_full, d.cptr.p, d.codes.p, d.blocks.p, d.specs.p, tables,
+                                                        P, d.nivl, out_a, out_b);
+    FEM2D_CUDA(cudaGetLastError());
+    c.launches++;
+  }
 }
 
 }  // namespace fem2d

@@ -409,6 +409,15 @@ int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g) {
   API_END
 }
 
+int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, double* d_b) {
+  API_BEGIN
+  if (!c || !g || !d_a || !d_b) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (g->ctx != &c->c) fail(FEM2D_E_INVALID_ARG, "the GEP was built on another context");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  device_values_noalloc(c->c, g->h, g->d, d_a, d_b);
+  API_END
+}
+
 void fem2d_gep_free(fem2d_gep* g) {
   if (!g) return;
   if (g->ctx) cudaSetDevice(g->ctx->device);

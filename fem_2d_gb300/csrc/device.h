@@ -104,5 +104,8 @@ struct DeviceGEP {
 void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d);
 // launches the table kernel and the value kernel; returns device times in ms (tables, values)
 void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, float* ms_values);
+// the same two kernels with the tables in a file-scope device array; writes caller-owned A and B
+void device_values_noalloc(Ctx& c, const HostGEP& g, const DeviceGEP& d, double* out_a, double* out_b);
+size_t noalloc_table_capacity();
 
 }  // namespace fem2d

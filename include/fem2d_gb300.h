@@ -136,6 +136,20 @@ int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int bas
 /* Numeric phase only: recompute the values of an existing GEP on the device (same domain and
  * settings). Used to time the device kernels with inputs resident in device memory. */
 int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g);
+/* Allocation-free recomputation of the A and B values (no counterpart in the reference).
+ * For hosts that own all device memory themselves (a pool or arena that must account for every
+ * byte, so the library may not allocate behind its back) or that cannot afford cudaMalloc/cudaFree
+ * on their critical path. The caller passes device arrays d_a and d_b of nnz_full doubles (full CSR
+ * order, as fem2d_gep_export_csr); the inputs are the GEP's resident pattern and contribution lists.
+ * The 1-D contraction tables live in one file-scope device array of 4 MiB (524288 doubles); a GEP
+ * needing more (2 x intervals x 5 x (max order + 1)^2) is rejected with FEM2D_E_TOO_LARGE. Each GPU
+ * that loads the library holds that array until the process exits. The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the one array: calls that overlap on the GPU (other streams, other host
+ * threads) race on it. Nothing in it needs clearing between calls. Returns after the work is queued
+ * on the context's stream; synchronise before reading d_a and d_b. No cudaMalloc, cudaFree or other
+ * allocating call is made. */
+int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, double* d_b);
 void fem2d_gep_free(fem2d_gep* g);
 /* dims: ndofs, upper-triangle entry count (SparseMatrix::entries), full symmetric nnz
  * (SparseMatrix::num_entries, sparse_matrix.rs:32-35) */
