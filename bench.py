@@ -40,6 +40,10 @@ def workload(name):
         return configs.full_scale(seed=0, nx=32, ny=16, rounds=3)
     if name == "full":
         return configs.full_scale(seed=0)
+    if name == "full_koleg":
+        return configs.full_scale(seed=0, basis=1)
+    if name == "full_koleg_1m":
+        return configs.full_scale(seed=0, basis=1, fraction=0.44)
     raise SystemExit("unknown workload " + name)
 
 

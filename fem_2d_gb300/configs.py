@@ -153,9 +153,10 @@ def precision(seed=0, nx=16, ny=8, order=6, rounds=3, fraction=0.3):
     return Workload("precision_16x8_p6_koleg", mj, ops, basis=1, glq=(10, 10), target=10.0, n_pairs=10, seed=seed)
 
 
-def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8):
+def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8, basis=0):
     """[0,2]x[0,1], 64x32 Elems, per-Elem orders uniform in pmin..pmax per direction, `rounds` seeded rounds
-    of T/U/V refinement of `fraction` of the leaves; HierPoly, GLQ [10,10], 20 pairs nearest 10.0."""
+    of T/U/V refinement of `fraction` of the leaves; HierPoly (basis=0) or KOLeg (basis=1), GLQ [10,10],
+    20 pairs nearest 10.0."""
     from . import Mesh
 
     mj = grid_mesh_json(nx, ny, 0.0, 2.0, 0.0, 1.0)
@@ -168,7 +169,8 @@ def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8):
     m = Mesh.from_json(mj)
     apply_ops(m, ops)
     _random_rounds(m, ops, rng, rounds, fraction, [0, 1, 2])
-    return Workload("full_64x32_p3-8_hierpoly", mj, ops, basis=0, glq=(10, 10), target=10.0, n_pairs=20, seed=seed)
+    name = "full_%dx%d_p%d-%d_%s_r%d_f%g" % (nx, ny, pmin, pmax, "koleg" if basis else "hierpoly", rounds, fraction)
+    return Workload(name, mj, ops, basis=basis, glq=(10, 10), target=10.0, n_pairs=20, seed=seed)
 
 
 def batch_member(seed):

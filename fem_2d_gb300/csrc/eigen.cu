@@ -8,7 +8,8 @@
 // with c = 0.05 |sigma|: eigenvalue lambda / ((lambda - sigma)(lambda + c)), close to the plain
 // shift-invert 1 / (lambda - sigma) for every physical mode, zero on the null space (A kills it
 // whatever the accuracy of the SPD solve) and small for high-frequency modes; exact multifrontal
-// solves (mf.cu). Each cycle builds a block Krylov basis [X, TX, T^2 X] B-orthonormalised by CGS2
+// solves (mf.cu). Each cycle builds a block Krylov basis [X, TX_u, T^2 X_u, T^3 X_u] (X_u the
+// unconverged Ritz vectors; converged pairs are kept but not expanded), B-orthonormalised by CGS2
 // in FP64, then a Rayleigh-Ritz step on the pencil (A, B) itself (FP64); Ritz pairs with a relative
 // residual above 1 (mixtures of null-space and high-frequency directions that land near sigma) are
 // not selected. Residuals ||A x - lambda B x|| / (|lambda| ||B x||) are computed in FP64.
@@ -50,11 +51,28 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t n, const int64_t* __r
        row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     double acc = 0.0;
     const int64_t k1 = rp[row + 1];
-    for (int64_t k = rp[row] + sub; k < k1; k += groups) {
+    const bool live = c < nb;
+    int64_t k = rp[row] + sub;
+    for (; k + 3 * groups < k1; k += 4 * groups) {
+      int cc[4];
+      double v[4], x[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) cc[q] = __ldg(col + k + q * groups);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        v[q] = 0.0;
+        if (ca != 0.0) v[q] += ca * __ldg(va + k + q * groups);
+        if (cb != 0.0) v[q] += cb * __ldg(vb + k + q * groups);
+        x[q] = live ? __ldg(X + (int64_t)cc[q] * ldx + c) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc += v[q] * x[q];
+    }
+    for (; k < k1; k += groups) {
       double v = 0.0;
       if (ca != 0.0) v += ca * __ldg(va + k);
       if (cb != 0.0) v += cb * __ldg(vb + k);
-      if (c < nb) acc += v * __ldg(X + (int64_t)__ldg(col + k) * ldx + c);
+      if (live) acc += v * __ldg(X + (int64_t)__ldg(col + k) * ldx + c);
     }
     for (int off = G; off < 32; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
     if (sub == 0 && c < nb) Y[row * ldy + c] = acc;
@@ -170,6 +188,49 @@ __global__ void __launch_bounds__(256) resid_partial_kernel(int64_t n, const dou
   }
 }
 
+// s[i] = 1 / sqrt(B_ii) (B is SPD); one warp per row
+__global__ void jacobi_scale_kernel(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                    const double* __restrict__ vb, double* __restrict__ sc, int* __restrict__ bad) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32)
+      if (col[k] == row) {
+        const double dg = vb[k];
+        if (dg > 0.0) sc[row] = 1.0 / sqrt(dg);
+        else {
+          sc[row] = 1.0;
+          atomicOr(bad, 1);
+        }
+      }
+  }
+}
+
+// out = diag(s) M diag(s) for M in {A, B}, entry by entry in CSR order; one warp per row
+__global__ void scale_csr_kernel(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                 const double* __restrict__ va, const double* __restrict__ vb,
+                                 const double* __restrict__ sc, double* __restrict__ oa, double* __restrict__ ob) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const double sr = sc[row];
+    for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+      const double f = sr * sc[col[k]];
+      oa[k] = va[k] * f;
+      ob[k] = vb[k] * f;
+    }
+  }
+}
+
+// X[r][c] *= s[r] for a row-major block
+__global__ void scale_rows_kernel(int64_t n, int b, const double* __restrict__ sc, double* __restrict__ X, int64_t ld) {
+  const int64_t total = n * b;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / b;
+    X[r * ld + (t % b)] *= sc[r];
+  }
+}
+
 // dense n x n row-major from the full CSR (ca*A + cb*B)
 __global__ void densify_kernel(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                                const double* __restrict__ va, const double* __restrict__ vb, double ca, double cb,
@@ -183,6 +244,8 @@ struct Dev {
   Ctx& c;
   const HostGEP& h;
   const DeviceGEP& d;
+  const double* va;   // values used by spmm (the GEP's, or a scaled copy)
+  const double* vb;
   DBuf<double> part;
   DBuf<double> small;
   int grid_rows() const { return std::max(1, c.num_sms * 2); }
@@ -196,7 +259,7 @@ struct Dev {
       while (G < w) G <<= 1;
       const int64_t warps = h.n;
       const int64_t blocks = std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)c.num_sms * 16);
-      spmm_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, d.row_ptr.p, d.col.p, d.a.p, d.b.p, ca,
+      spmm_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, d.row_ptr.p, d.col.p, va, vb, ca,
                                                                            cb, X + c0, ldx, w, G, Y + c0, ldy);
       c.launches++;
     }
@@ -219,17 +282,25 @@ struct Dev {
     FEM2D_CUDA(cudaMemcpyAsync(C.data(), small.p, ab * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   }
-  // Z = beta Z + X * C (C host a x b)
+  // Z = beta Z + X * C (C host a x b), tiled over the columns of C so a tile fits in shared memory
   void gemm(const double* X, int64_t ldx, int a, const std::vector<double>& C, int b, double beta, double* Z,
             int64_t ldz) {
-    if (small.n < (size_t)a * b) small.alloc(std::max<size_t>((size_t)a * b, 16384));
-    FEM2D_CUDA(cudaMemcpyAsync(small.p, C.data(), (size_t)a * b * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    const size_t smem = (size_t)a * b * sizeof(double);
-    if (smem > 96 * 1024) fail(FEM2D_E_INVALID_ARG, "GEMM block too large");
-    const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
-    gemm_nn_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, smem, c.stream>>>(h.n, X, ldx, a, small.p, b, beta, Z,
-                                                                              ldz);
-    c.launches++;
+    if (a <= 0 || b <= 0) return;
+    const int chunk = std::max(1, std::min(b, (int)((96 * 1024) / (sizeof(double) * a))));
+    std::vector<double> Ct;
+    for (int j0 = 0; j0 < b; j0 += chunk) {
+      const int w = std::min(chunk, b - j0);
+      Ct.resize((size_t)a * w);
+      for (int i = 0; i < a; i++)
+        for (int j = 0; j < w; j++) Ct[(size_t)i * w + j] = C[(size_t)i * b + j0 + j];
+      if (small.n < Ct.size()) small.alloc(std::max<size_t>(Ct.size(), 16384));
+      FEM2D_CUDA(cudaMemcpyAsync(small.p, Ct.data(), Ct.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+      const size_t smem = Ct.size() * sizeof(double);
+      const int64_t blocks = std::min<int64_t>((h.n * w + 255) / 256, (int64_t)c.num_sms * 8);
+      gemm_nn_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, smem, c.stream>>>(h.n, X, ldx, a, small.p, w, beta,
+                                                                                Z + j0, ldz);
+      c.launches++;   // (pageable copies are staged before cudaMemcpyAsync returns: Ct may be reused)
+    }
   }
   void copy(const double* X, int64_t ldx, int b, double* Y, int64_t ldy) {
     const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
@@ -278,35 +349,53 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   int b = o.block > 0 ? o.block : std::min<int64_t>(k + guard, n);
   if (b < k) b = k;
   if (b > 32) fail(FEM2D_E_INVALID_ARG, "block size above 32 (n_pairs too large for one block)");
-  const int steps = 2;
+  const int steps = 3;
   const int mmax = b * (steps + 1);
   const double tol = o.tol > 0 ? o.tol : 1e-10;
   const int max_cycles = o.max_outer > 0 ? o.max_outer : 40;
   const double spur = 1e-6 * std::max(1.0, std::fabs(sigma));
   if (sigma == 0.0) fail(FEM2D_E_INVALID_ARG, "target 0 is the null space of the curl-curl operator");
 
+  // symmetric Jacobi scaling: the whole solve runs on (D A D, D B D), D = diag(B)^-1/2 (same
+  // eigenvalues, eigenvectors x = D x~); it keeps the unnormalised high-order bases well scaled
+  DBuf<double> sc, sa, sb;
+  DBuf<int> bad;
+  sc.alloc(n);
+  sa.alloc(h.nnz_full);
+  sb.alloc(h.nnz_full);
+  bad.alloc(1);
+  FEM2D_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), c.stream));
+  {
+    const int64_t blocks = std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 16);
+    jacobi_scale_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.b.p,
+                                                                                 sc.p, bad.p);
+    scale_csr_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.a.p, d.b.p,
+                                                                              sc.p, sa.p, sb.p);
+    c.launches += 2;
+    int hb = 0;
+    FEM2D_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+    if (hb) fail(FEM2D_E_B_NOT_SPD, "B has a non-positive diagonal entry");
+  }
   MFSymbolic sym;
   mf_symbolic(dom, h, sym);
   MFDevice mf;
   mf.setup(c, sym, 32);
   MFFactor fm, fp;
-  mf.factor(c, d.a.p, d.b.p, 1.0, -sigma, false, fm);
+  mf.factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
   // A + c B (c > 0) is SPD: factored without pivoting
   const double cshift = 0.05 * std::fabs(sigma);
-  mf.factor(c, d.a.p, d.b.p, 1.0, cshift, true, fp);
+  mf.factor(c, sa.p, sb.p, 1.0, cshift, true, fp);
   if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + c B is not positive definite; B is likely ill-conditioned");
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t1 = std::chrono::steady_clock::now();
 
-  Dev D{c, h, d};
-  DBuf<double> V, AV, BV, X, W1, W2, W3;
+  Dev D{c, h, d, sa.p, sb.p};
+  DBuf<double> V, AV, BV, X, AX, BX, G0, W1, W2, W3;
   V.alloc((size_t)n * mmax);
   AV.alloc((size_t)n * mmax);
   BV.alloc((size_t)n * mmax);
-  X.alloc((size_t)n * 32);
-  W1.alloc((size_t)n * 32);
-  W2.alloc((size_t)n * 32);
-  W3.alloc((size_t)n * 32);
+  for (DBuf<double>* buf : {&X, &AX, &BX, &G0, &W1, &W2, &W3}) buf->alloc((size_t)n * 32);
   int64_t spmv = 0, napply = 0;
 
   // Out (ld lo) = T In (ld li), nb columns; In and Out may not alias W1..W3
@@ -318,42 +407,52 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     spmv += 2 * nb;
     napply += nb;
   };
-  // B-orthonormalise columns [m0, m0+r) of V against [0, m0) and among themselves; returns kept count
-  auto borth = [&](int m0, int r) -> int {
+  // W = V[:, m0:m0+r]: B-orthogonalise against V[:, :m0] (CGS2, B*W tracked linearly), orthonormalise
+  // within the block (eigen-decomposition of its Gram matrix, rank-revealing), then store the exact
+  // products A*W and B*W in AV and BV. Returns the number of columns kept.
+  auto borth_new = [&](int m0, int r) -> int {
+    if (r <= 0) return 0;
     double* Wb = V.p + m0;
+    double* BWb = BV.p + m0;
+    D.spmm(0.0, 1.0, Wb, mmax, r, BWb, mmax);
+    spmv += r;
     std::vector<double> C, G, w, z;
-    for (int pass = 0; pass < 2; pass++) {
-      if (m0 > 0) {
-        D.spmm(0.0, 1.0, Wb, mmax, r, W1.p, 32);
-        D.gram(V.p, mmax, m0, W1.p, 32, r, C);
-        for (auto& x : C) x = -x;
-        D.gemm(V.p, mmax, m0, C, r, 1.0, Wb, mmax);
-      }
+    auto project = [&](int cols) {
+      D.gram(V.p, mmax, m0, BWb, mmax, cols, C);
+      for (auto& x : C) x = -x;
+      D.gemm(V.p, mmax, m0, C, cols, 1.0, Wb, mmax);
+      D.gemm(BV.p, mmax, m0, C, cols, 1.0, BWb, mmax);
+    };
+    if (m0 > 0) {
+      project(r);
+      project(r);
     }
     int keep = r;
     for (int pass = 0; pass < 2; pass++) {
-      D.spmm(0.0, 1.0, Wb, mmax, keep, W1.p, 32);
-      D.gram(Wb, mmax, keep, W1.p, 32, keep, G);
+      D.gram(Wb, mmax, keep, BWb, mmax, keep, G);
+      for (int i = 0; i < keep; i++)
+        for (int j = 0; j < i; j++)
+          G[(size_t)i * keep + j] = G[(size_t)j * keep + i] = 0.5 * (G[(size_t)i * keep + j] + G[(size_t)j * keep + i]);
       if (!symeig(keep, G, w, z)) fail(FEM2D_E_NOT_CONVERGED, "Gram eigen-decomposition failed");
       const double wmax = *std::max_element(w.begin(), w.end());
       std::vector<int> kept;
       for (int q = 0; q < keep; q++)
         if (w[q] > (pass == 0 ? 1e-8 : 1e-14) * wmax && w[q] > 0) kept.push_back(q);
       const int nk = (int)kept.size();
+      if (nk == 0) return 0;
       std::vector<double> T((size_t)keep * nk);
       for (int i = 0; i < keep; i++)
         for (int q = 0; q < nk; q++) T[(size_t)i * nk + q] = z[(size_t)i * keep + kept[q]] / std::sqrt(w[kept[q]]);
-      if (nk == 0) return 0;
       D.gemm(Wb, mmax, keep, T, nk, 0.0, W2.p, 32);
       D.copy(W2.p, 32, nk, Wb, mmax);
+      D.gemm(BWb, mmax, keep, T, nk, 0.0, W2.p, 32);
+      D.copy(W2.p, 32, nk, BWb, mmax);
       keep = nk;
-      if (m0 > 0) {
-        D.spmm(0.0, 1.0, Wb, mmax, keep, W1.p, 32);
-        D.gram(V.p, mmax, m0, W1.p, 32, keep, C);
-        for (auto& x : C) x = -x;
-        D.gemm(V.p, mmax, m0, C, keep, 1.0, Wb, mmax);
-      }
+      if (pass == 0 && m0 > 0) project(keep);
     }
+    D.spmm(0.0, 1.0, Wb, mmax, keep, BWb, mmax);
+    D.spmm(1.0, 0.0, Wb, mmax, keep, AV.p + m0, mmax);
+    spmv += 2 * keep;
     return keep;
   };
 
@@ -367,40 +466,94 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     apply_T(R.p, b, X.p, 32, b);
   }
   std::vector<double> theta_sel, rel_sel;
-  std::vector<int> sel;
-  int cycles = 0;
+  int cycles = 0, bx = b;
   bool converged = false;
-  int bx = b;
   for (; cycles < max_cycles; cycles++) {
-    D.copy(X.p, 32, bx, V.p, mmax);
-    int m = borth(0, bx);
-    int last0 = 0, lastn = m;
-    for (int s = 0; s < steps && m + lastn <= mmax; s++) {
+    int m, last0 = 0, lastn;
+    if (cycles == 0) {
+      D.copy(X.p, 32, b, V.p, mmax);
+      m = borth_new(0, b);
+      lastn = m;
+    } else {
+      // restart from the B-orthonormal Ritz vectors (and their exact products), expand the unconverged
+      D.copy(X.p, 32, bx, V.p, mmax);
+      D.copy(AX.p, 32, bx, AV.p, mmax);
+      D.copy(BX.p, 32, bx, BV.p, mmax);
+      m = bx;
+      std::vector<double> sel_cols;
+      int u = 0;
+      for (int q = 0; q < bx; q++)
+        if (rel_sel[q] >= tol) u++;
+      std::vector<double> Gsel((size_t)bx * u, 0.0);
+      for (int q = 0, k2 = 0; q < bx; q++)
+        if (rel_sel[q] >= tol) Gsel[(size_t)q * u + k2++] = 1.0;
+      int r = 0;
+      if (u > 0) {
+        // expand with T applied to the unconverged Ritz vectors: T kills their null-space part and
+        // damps high-frequency content, which also pushes spurious Ritz vectors out of the basis
+        D.gemm(X.p, 32, bx, Gsel, u, 0.0, G0.p, 32);
+        apply_T(G0.p, 32, V.p + m, mmax, u);
+        r = borth_new(m, u);
+      }
+      last0 = m;
+      lastn = r;
+      m += r;
+    }
+    for (int st2 = (cycles == 0 ? 0 : 1); st2 < steps && lastn > 0 && m + lastn <= mmax; st2++) {
       apply_T(V.p + last0, mmax, V.p + m, mmax, lastn);
-      int r = borth(m, lastn);
+      int r = borth_new(m, lastn);
       if (r == 0) break;
       last0 = m;
       lastn = r;
       m += r;
     }
-    D.spmm(1.0, 0.0, V.p, mmax, m, AV.p, mmax);
-    D.spmm(0.0, 1.0, V.p, mmax, m, BV.p, mmax);
-    spmv += 2 * m;
-    std::vector<double> GA, th, Y;
+    // Rayleigh-Ritz on (V^T A V, V^T B V)
+    std::vector<double> GA, GB, wb, zb;
     D.gram(V.p, mmax, m, AV.p, mmax, m, GA);
+    D.gram(V.p, mmax, m, BV.p, mmax, m, GB);
     for (int i = 0; i < m; i++)
-      for (int j = 0; j < i; j++) GA[(size_t)i * m + j] = GA[(size_t)j * m + i] = 0.5 * (GA[(size_t)i * m + j] + GA[(size_t)j * m + i]);
-    if (!symeig(m, GA, th, Y)) fail(FEM2D_E_NOT_CONVERGED, "Rayleigh-Ritz eigen-decomposition failed");
-    // Ritz residuals of all m pairs: AV*Y - BV*Y*theta
-    const int m2 = m;
-    DBuf<double> AY, BY;
+      for (int j = 0; j < i; j++) {
+        GA[(size_t)i * m + j] = GA[(size_t)j * m + i] = 0.5 * (GA[(size_t)i * m + j] + GA[(size_t)j * m + i]);
+        GB[(size_t)i * m + j] = GB[(size_t)j * m + i] = 0.5 * (GB[(size_t)i * m + j] + GB[(size_t)j * m + i]);
+      }
+    if (!symeig(m, GB, wb, zb)) fail(FEM2D_E_NOT_CONVERGED, "Gram eigen-decomposition failed");
+    const double wbmax = *std::max_element(wb.begin(), wb.end());
+    std::vector<int> kb;
+    for (int q = 0; q < m; q++)
+      if (wb[q] > 1e-12 * wbmax) kb.push_back(q);
+    const int m2 = (int)kb.size();
+    std::vector<double> Wh((size_t)m * m2);   // GB^-1/2 restricted to its numerical range
+    for (int i = 0; i < m; i++)
+      for (int q = 0; q < m2; q++) Wh[(size_t)i * m2 + q] = zb[(size_t)i * m + kb[q]] / std::sqrt(wb[kb[q]]);
+    std::vector<double> S((size_t)m2 * m2, 0.0), tmp((size_t)m * m2, 0.0);
+    for (int i = 0; i < m; i++)
+      for (int q = 0; q < m2; q++) {
+        double acc = 0.0;
+        for (int k2 = 0; k2 < m; k2++) acc += GA[(size_t)i * m + k2] * Wh[(size_t)k2 * m2 + q];
+        tmp[(size_t)i * m2 + q] = acc;
+      }
+    for (int p2 = 0; p2 < m2; p2++)
+      for (int q = 0; q < m2; q++) {
+        double acc = 0.0;
+        for (int i = 0; i < m; i++) acc += Wh[(size_t)i * m2 + p2] * tmp[(size_t)i * m2 + q];
+        S[(size_t)p2 * m2 + q] = acc;
+      }
+    std::vector<double> th, Z;
+    if (!symeig(m2, S, th, Z)) fail(FEM2D_E_NOT_CONVERGED, "Rayleigh-Ritz eigen-decomposition failed");
+    std::vector<double> Y((size_t)m * m2, 0.0);
+    for (int i = 0; i < m; i++)
+      for (int q = 0; q < m2; q++) {
+        double acc = 0.0;
+        for (int k2 = 0; k2 < m2; k2++) acc += Wh[(size_t)i * m2 + k2] * Z[(size_t)k2 * m2 + q];
+        Y[(size_t)i * m2 + q] = acc;
+      }
+    // Ritz residuals of all m2 pairs: AV*Y - BV*Y*theta
+    DBuf<double> AY, BY, th_d, P;
     AY.alloc((size_t)n * m2);
     BY.alloc((size_t)n * m2);
     D.gemm(AV.p, mmax, m, Y, m2, 0.0, AY.p, m2);
     D.gemm(BV.p, mmax, m, Y, m2, 0.0, BY.p, m2);
-    DBuf<double> th_d, P;
-    std::vector<double> thv(th);
-    th_d.upload(thv, c.stream);
+    th_d.upload(th, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
     P.alloc((size_t)nblk * 2 * m2);
@@ -431,13 +584,15 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       std::stable_sort(cand.begin(), cand.end(),
                        [&](int x, int y) { return std::fabs(th[x] - sigma) < std::fabs(th[y] - sigma); });
     }
-    sel.assign(cand.begin(), cand.begin() + std::min<size_t>(cand.size(), (size_t)b));
+    std::vector<int> sel(cand.begin(), cand.begin() + std::min<size_t>(cand.size(), (size_t)b));
     if ((int)sel.size() < k) fail(FEM2D_E_SPURIOUS, "only spurious (null-space) Ritz values were found");
     bx = (int)sel.size();
     std::vector<double> Ysel((size_t)m * bx);
     for (int i = 0; i < m; i++)
-      for (int q = 0; q < bx; q++) Ysel[(size_t)i * bx + q] = Y[(size_t)i * m + sel[q]];
+      for (int q = 0; q < bx; q++) Ysel[(size_t)i * bx + q] = Y[(size_t)i * m2 + sel[q]];
     D.gemm(V.p, mmax, m, Ysel, bx, 0.0, X.p, 32);
+    D.gemm(AV.p, mmax, m, Ysel, bx, 0.0, AX.p, 32);
+    D.gemm(BV.p, mmax, m, Ysel, bx, 0.0, BX.p, 32);
     theta_sel.resize(bx);
     rel_sel.resize(bx);
     for (int q = 0; q < bx; q++) {
@@ -467,6 +622,39 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     for (int q = 0; q < k; q++) w = std::max(w, rel_sel[q]);
     st->max_rel_residual = w;
     st->spmv_count = spmv;
+  }
+  // back to the original pencil: x = D x~ (B-orthonormal), residuals in the original norms
+  {
+    const int64_t blocks = std::min<int64_t>((n * bx + 255) / 256, (int64_t)c.num_sms * 8);
+    scale_rows_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, bx, sc.p, X.p, 32);
+    c.launches++;
+    D.va = d.a.p;
+    D.vb = d.b.p;
+    D.spmm(1.0, 0.0, X.p, 32, bx, AX.p, 32);
+    D.spmm(0.0, 1.0, X.p, 32, bx, BX.p, 32);
+    DBuf<double> th_d, P;
+    th_d.upload(theta_sel, c.stream);
+    const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
+    const int64_t rpb = (n + nblk - 1) / nblk;
+    P.alloc((size_t)nblk * 2 * bx);
+    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AX.p, BX.p, 32, bx, th_d.p, rpb, P.p);
+    c.launches++;
+    std::vector<double> Ph((size_t)nblk * 2 * bx);
+    FEM2D_CUDA(cudaMemcpyAsync(Ph.data(), P.p, Ph.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+    for (int j = 0; j < bx; j++) {
+      double sr = 0, sbb = 0;
+      for (int q = 0; q < nblk; q++) {
+        sr += Ph[(size_t)q * 2 * bx + j];
+        sbb += Ph[(size_t)q * 2 * bx + bx + j];
+      }
+      rel_sel[j] = std::sqrt(sr) / (std::fabs(theta_sel[j]) * std::sqrt(sbb) + 1e-300);
+    }
+    if (st) {
+      double w = 0;
+      for (int q = 0; q < k; q++) w = std::max(w, rel_sel[q]);
+      st->max_rel_residual = w;
+    }
   }
   // outputs: B-normalised (the Ritz vectors are B-orthonormal), sign fixed by the largest entry
   std::vector<double> Xh((size_t)n * 32);

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstring>
 
 namespace cg = cooperative_groups;
@@ -23,8 +24,11 @@ namespace {
 
 constexpr int PANEL = 32;
 
+constexpr int MAXKIDS = 4;   // binary dissection nodes; Elem nodes have 2 (U/V) or 4 (T) children
+
 struct FrontDesc {   // device copy of the per-front scalars
-  int32_t f, p, parent, kid0, kid1;
+  int32_t f, p, parent;
+  int32_t kid[MAXKIDS];
   int64_t off, dptr, aptr, aend, eptr;
 };
 
@@ -44,7 +48,7 @@ __global__ void mf_assemble_kernel(const int32_t* __restrict__ lf, const FrontDe
 __global__ void mf_extend_add_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd, int slot,
                                      const int32_t* __restrict__ emap, double* __restrict__ F) {
   const FrontDesc par = fd[lf[blockIdx.y]];
-  const int32_t ch = slot == 0 ? par.kid0 : par.kid1;
+  const int32_t ch = par.kid[slot];
   if (ch < 0) return;
   const FrontDesc c = fd[ch];
   const int s = c.f - c.p;
@@ -269,8 +273,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
       if (i < f) v[(int64_t)c * f + i] = i < p ? B[(int64_t)D[pm[i]] * ldb + c] : 0.0;
     }
   __syncthreads();
-  for (int slot = 0; slot < 2; slot++) {
-    const int ch = slot == 0 ? d.kid0 : d.kid1;
+  for (int slot = 0; slot < MAXKIDS; slot++) {
+    const int ch = d.kid[slot];
     if (ch < 0) continue;
     const FrontDesc cd = fd[ch];
     const int s = cd.f - cd.p;
@@ -405,12 +409,14 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
   nb_cap = nb_max;
   // fronts laid out level by level so each level's storage is contiguous
   std::vector<int64_t> off(nf, 0), poff(nf, 0), woff_h(nf, 0);
-  std::vector<int32_t> kid0(nf, -1), kid1(nf, -1);
+  std::vector<std::array<int32_t, MAXKIDS>> kids(nf);
+  for (auto& k : kids) k.fill(-1);
+  std::vector<int> nk(nf, 0);
   for (int f = 0; f < nf; f++) {
     int pa = s.parent[f];
     if (pa >= 0) {
-      if (kid0[pa] < 0) kid0[pa] = f;
-      else kid1[pa] = f;
+      if (nk[pa] >= MAXKIDS) fail(FEM2D_E_INVALID_ARG, "elimination tree node with more than 4 children");
+      kids[pa][nk[pa]++] = f;
     }
   }
   int64_t o = 0, po = 0, wo = 0;
@@ -435,8 +441,7 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
     x.f = s.f[f];
     x.p = s.p[f];
     x.parent = s.parent[f];
-    x.kid0 = kid0[f];
-    x.kid1 = kid1[f];
+    for (int k = 0; k < MAXKIDS; k++) x.kid[k] = kids[f][k];
     x.off = off[f];
     x.dptr = s.dof_ptr[f];
     x.aptr = s.asm_ptr[f];
@@ -484,7 +489,7 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
     mf_assemble_kernel<<<dim3(8, nfl), 256, 0, st>>>(lf, fd, asm_pos.p, asm_csr.p, va, vb, ca, cb, Fbuf.p);
     c.launches++;
     if (l > 0) {
-      for (int slot = 0; slot < 2; slot++) {
+      for (int slot = 0; slot < MAXKIDS; slot++) {
         mf_extend_add_kernel<<<dim3(16, nfl), 256, 0, st>>>(lf, fd, slot, ea_map.p, Fbuf.p);
         c.launches++;
       }

@@ -1,4 +1,11 @@
 // Symbolic phase of the multifrontal factorization (see mf.h).
+//
+// Elimination tree: a nested dissection of the base Elems by coordinate bisection (binary nodes);
+// below each base Elem its own refinement tree (an Elem node per Elem, with its 2 or 4 children).
+// A DoF is eliminated at the lowest common ancestor of the Elems it is attached to. Every Elem whose
+// functions couple with the DoF is an ancestor or a descendant of one of those Elems, so all its
+// couplings lie on root paths through that node: the tree is a valid elimination tree, and leaf
+// fronts are single leaf Elems (tens to ~150 DoFs) instead of whole refined trees.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -19,64 +26,77 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
   s.n = n;
   if (n == 0) return;
 
-  // ---- nested dissection of the base Elems by coordinate bisection (postorder node ids)
+  // ---- build the tree in postorder: ND over base Elems, Elem refinement trees below
   std::vector<double> cx(R), cy(R);
   for (int r = 0; r < R; r++) {
     cx[r] = 0.5 * (m.roots[r].x0 + m.roots[r].x3);
     cy[r] = 0.5 * (m.roots[r].y0 + m.roots[r].y3);
   }
   std::vector<int32_t> parent, first_desc;
-  std::vector<std::array<int32_t, 2>> kids;
-  std::vector<int32_t> leaf_of(R, -1);
-  std::function<int32_t(std::vector<int>&)> build = [&](std::vector<int>& roots) -> int32_t {
-    std::array<int32_t, 2> ch = {-1, -1};
-    int32_t first = (int32_t)parent.size();
-    if (roots.size() > 1) {
-      double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
-      for (int r : roots) {
-        x0 = std::min(x0, cx[r]); x1 = std::max(x1, cx[r]);
-        y0 = std::min(y0, cy[r]); y1 = std::max(y1, cy[r]);
-      }
-      bool by_x = (x1 - x0) >= (y1 - y0);
-      std::stable_sort(roots.begin(), roots.end(), [&](int a, int b) {
-        double ka = by_x ? cx[a] : cy[a], kb = by_x ? cx[b] : cy[b];
-        if (ka != kb) return ka < kb;
-        double la = by_x ? cy[a] : cx[a], lb = by_x ? cy[b] : cx[b];
-        return la != lb ? la < lb : a < b;
-      });
-      size_t half = roots.size() / 2;
-      std::vector<int> lo(roots.begin(), roots.begin() + half), hi(roots.begin() + half, roots.end());
-      ch[0] = build(lo);
-      ch[1] = build(hi);
-    }
+  std::vector<std::vector<int32_t>> kids;
+  std::vector<int32_t> elem_node(m.elems.size(), -1);
+  auto new_node = [&](int32_t first, const std::vector<int32_t>& ch) {
     int32_t id = (int32_t)parent.size();
     parent.push_back(-1);
     first_desc.push_back(first);
     kids.push_back(ch);
-    if (ch[0] >= 0) { parent[ch[0]] = id; parent[ch[1]] = id; }
-    if (roots.size() == 1) leaf_of[roots[0]] = id;
+    for (int32_t c : ch) parent[c] = id;
     return id;
+  };
+  std::function<int32_t(int64_t)> build_elem = [&](int64_t e) -> int32_t {
+    int32_t first = (int32_t)parent.size();
+    std::vector<int32_t> ch;
+    const MElem& el = m.elems[e];
+    for (int k = 0; k < el.nchild; k++) ch.push_back(build_elem(el.child[k]));
+    int32_t id = new_node(first, ch);
+    elem_node[e] = id;
+    return id;
+  };
+  std::function<int32_t(std::vector<int>&)> build = [&](std::vector<int>& roots) -> int32_t {
+    if (roots.size() == 1) return build_elem(roots[0]);   // base Elem r is Elem r
+    int32_t first = (int32_t)parent.size();
+    double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+    for (int r : roots) {
+      x0 = std::min(x0, cx[r]); x1 = std::max(x1, cx[r]);
+      y0 = std::min(y0, cy[r]); y1 = std::max(y1, cy[r]);
+    }
+    bool by_x = (x1 - x0) >= (y1 - y0);
+    std::stable_sort(roots.begin(), roots.end(), [&](int a, int b) {
+      double ka = by_x ? cx[a] : cy[a], kb = by_x ? cx[b] : cy[b];
+      if (ka != kb) return ka < kb;
+      double la = by_x ? cy[a] : cx[a], lb = by_x ? cy[b] : cx[b];
+      return la != lb ? la < lb : a < b;
+    });
+    size_t half = roots.size() / 2;
+    std::vector<int> lo(roots.begin(), roots.begin() + half), hi(roots.begin() + half, roots.end());
+    int32_t a = build(lo);
+    int32_t b = build(hi);
+    return new_node(first, {a, b});
   };
   std::vector<int> all(R);
   for (int r = 0; r < R; r++) all[r] = r;
   build(all);
   const int NF = (int)parent.size();
+  std::vector<int32_t> depth(NF, 0);
+  for (int f = NF - 1; f >= 0; f--)
+    if (parent[f] >= 0) depth[f] = depth[parent[f]] + 1;
   auto is_proper_anc = [&](int32_t a, int32_t x) { return a > x && first_desc[a] <= x; };
   auto lca = [&](int32_t a, int32_t b) {
     while (a != b) {
-      if (a < b) a = parent[a];
-      else b = parent[b];
+      if (depth[a] > depth[b]) a = parent[a];
+      else if (depth[b] > depth[a]) b = parent[b];
+      else { a = parent[a]; b = parent[b]; }
     }
     return a;
   };
 
-  // ---- DoF -> front: the leaf of its tree, or the common ancestor of the two trees it spans
+  // ---- DoF -> node: the lowest common ancestor of the Elems the DoF is attached to
   std::vector<int32_t> node(n, -1);
   for (size_t e = 0; e + 1 < d.spec_ptr.size(); e++) {
-    int32_t lf = leaf_of[m.elems[e].root];
+    int32_t en = elem_node[e];
     for (int64_t k = d.spec_ptr[e]; k < d.spec_ptr[e + 1]; k++) {
       int32_t dof = d.specs[k].dof;
-      node[dof] = node[dof] < 0 ? lf : lca(node[dof], lf);
+      node[dof] = node[dof] < 0 ? en : lca(node[dof], en);
     }
   }
   std::vector<std::vector<int32_t>> piv(NF);
@@ -104,9 +124,8 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
     };
     for (int32_t x : piv[f])
       for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) add(g.col[k]);
-    for (int c = 0; c < 2; c++)
-      if (kids[f][c] >= 0)
-        for (int32_t y : st[kids[f][c]]) add(y);
+    for (int32_t c : kids[f])
+      for (int32_t y : st[c]) add(y);
     std::sort(cand.begin(), cand.end(), [&](int32_t a, int32_t b) { return order[a] < order[b]; });
     st[f] = std::move(cand);
   }
@@ -122,7 +141,7 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
     s.p[f] = (int32_t)piv[f].size();
     s.f[f] = (int32_t)(piv[f].size() + st[f].size());
     s.dof_ptr[f + 1] = s.dof_ptr[f] + s.f[f];
-    if (kids[f][0] >= 0) s.level[f] = 1 + std::max(s.level[kids[f][0]], s.level[kids[f][1]]);
+    for (int32_t c : kids[f]) s.level[f] = std::max(s.level[f], 1 + s.level[c]);
     s.max_f = std::max(s.max_f, s.f[f]);
     s.max_p = std::max(s.max_p, s.p[f]);
     double F = s.f[f], P = s.p[f];
@@ -162,14 +181,11 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
       }
     }
     s.asm_ptr[f + 1] = (int64_t)s.asm_pos.size();
-    for (int c = 0; c < 2; c++) {
-      int32_t ch = kids[f][c];
-      if (ch < 0) continue;
+    for (int32_t ch : kids[f])
       for (int32_t y : st[ch]) {
         if (pos[y] < 0) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: child update outside the parent front");
         ea[ch].push_back(pos[y]);
       }
-    }
     for (int i = 0; i < F; i++) pos[D[i]] = -1;
   }
   for (int f = 0; f < NF; f++) s.ea_ptr[f + 1] = s.ea_ptr[f] + (int64_t)ea[f].size();
