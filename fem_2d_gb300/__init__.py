@@ -109,6 +109,20 @@ def lib():
         "fem2d_gep_shifted_solve": (ctypes.c_int, [P, P, d, d, ctypes.c_int, ctypes.c_int, dp, dp]),
         "fem2d_gpu_solve_gep": (ctypes.c_int, [P, P, d, ctypes.c_int, ctypes.POINTER(_fem2d_solve_opts), dp, dp, dp,
                                                 ctypes.POINTER(_fem2d_solve_stats)]),
+        "fem2d_gep_print_to_petsc_binary_files": (ctypes.c_int, [P, ctypes.c_char_p, ctypes.c_char_p]),
+        "fem2d_aij_write": (ctypes.c_int, [ctypes.c_char_p, i64, i64p, i32p, dp]),
+        "fem2d_aij_read": (ctypes.c_int, [ctypes.c_char_p, i64p, i64p, i64p, i32p, dp]),
+        "fem2d_petsc_vec_write": (ctypes.c_int, [ctypes.c_char_p, dp, i64]),
+        "fem2d_petsc_vec_read": (ctypes.c_int, [ctypes.c_char_p, dp, i64, i64p]),
+        "fem2d_petsc_scalar_write": (ctypes.c_int, [ctypes.c_char_p, d]),
+        "fem2d_petsc_scalar_read": (ctypes.c_int, [ctypes.c_char_p, dp]),
+        "fem2d_fields_create": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, PP]),
+        "fem2d_fields_free": (None, [P]),
+        "fem2d_fields_num_leaves": (i64, [P]),
+        "fem2d_fields_leaves": (ctypes.c_int, [P, i64p]),
+        "fem2d_fields_leaf_bounds": (ctypes.c_int, [P, dp]),
+        "fem2d_fields_xy": (ctypes.c_int, [P, dp, i64, dp, dp]),
+        "fem2d_fields_xy_device": (ctypes.c_int, [P, ctypes.c_void_p, i64, ctypes.c_void_p, ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -486,6 +500,10 @@ class GEP:
                                              r2.shape[1], _ptr(r2, ctypes.c_double), _ptr(x, ctypes.c_double)))
         return x[:, 0] if one else x
 
+    def print_to_petsc_binary_files(self, dir, prefix):
+        """GEP::print_to_petsc_binary_files (linalg.rs:44-52): {dir}/tmp/{prefix}_a.dat and _b.dat."""
+        _check(lib().fem2d_gep_print_to_petsc_binary_files(self._h, str(dir).encode(), str(prefix).encode()))
+
     def scipy(self):
         import scipy.sparse as sp
 
@@ -506,6 +524,59 @@ def galerkin_sample_gep_hcurl(bspace, a_integral, b_integral, domain, glq_grid_d
     h = ctypes.c_void_p()
     _check(lib().fem2d_galerkin_sample_gep_hcurl(ctx._h, domain._h, bspace.ID, nu, nv, ctypes.byref(h)))
     return GEP(h.value, ctx)
+
+
+# ----------------------------------------------------------------------------- external-solver files
+def aij_write(path, row_ptr, col, val):
+    """Full symmetric CSR -> the AIJMatrixBinary file layout (sparse_matrix.rs:184-265)."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    c = np.ascontiguousarray(col, dtype=np.int32)
+    v = np.ascontiguousarray(val, dtype=np.float64)
+    _check(lib().fem2d_aij_write(str(path).encode(), len(rp) - 1, _ptr(rp, ctypes.c_int64), _ptr(c, ctypes.c_int32),
+                                 _ptr(v, ctypes.c_double)))
+
+
+def aij_read(path):
+    """AIJMatrixBinary (or standard PETSc AIJ) file -> (row_ptr, col, val)."""
+    n, nnz = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().fem2d_aij_read(str(path).encode(), ctypes.byref(n), ctypes.byref(nnz), None, None, None))
+    rp = np.zeros(n.value + 1, dtype=np.int64)
+    c = np.zeros(nnz.value, dtype=np.int32)
+    v = np.zeros(nnz.value)
+    _check(lib().fem2d_aij_read(str(path).encode(), ctypes.byref(n), ctypes.byref(nnz), _ptr(rp, ctypes.c_int64),
+                                _ptr(c, ctypes.c_int32), _ptr(v, ctypes.c_double)))
+    return rp, c, v
+
+
+def petsc_vec_write(path, values):
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    _check(lib().fem2d_petsc_vec_write(str(path).encode(), _ptr(v, ctypes.c_double), len(v)))
+
+
+def retrieve_eigenvector(path):
+    """retrieve_eigenvector (slepc_solve.rs:114-135)."""
+    n = ctypes.c_int64()
+    _check(lib().fem2d_petsc_vec_read(str(path).encode(), None, 0, ctypes.byref(n)))
+    v = np.zeros(n.value)
+    _check(lib().fem2d_petsc_vec_read(str(path).encode(), _ptr(v, ctypes.c_double), len(v), ctypes.byref(n)))
+    return v
+
+
+def petsc_scalar_write(path, value):
+    _check(lib().fem2d_petsc_scalar_write(str(path).encode(), float(value)))
+
+
+def retrieve_eigenvalue(path):
+    """retrieve_eigenvalue (slepc_solve.rs:137-147)."""
+    x = ctypes.c_double()
+    _check(lib().fem2d_petsc_scalar_read(str(path).encode(), ctypes.byref(x)))
+    return x.value
+
+
+def retrieve_solution(dir, prefix):
+    """retrieve_solution (slepc_solve.rs:104-112): {dir}/tmp/{prefix}_evec.dat and _eval.dat."""
+    base = os.path.join(str(dir), "tmp", str(prefix))
+    return EigenPair(retrieve_eigenvalue(base + "_eval.dat"), retrieve_eigenvector(base + "_evec.dat"))
 
 
 @dataclass
@@ -562,3 +633,6 @@ def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOB
 def gpu_solve_gep(gep, target_eigenvalue, **kw):
     """gpu_solve_gep(gep, target) -> EigenPair, beside slepc_solve_gep (slepc_solve.rs:14-68)."""
     return gpu_solve_gep_n(gep, target_eigenvalue, 1, **kw).pairs()[0]
+
+
+from .fields import UniformFieldError, UniformFieldSpace  # noqa: E402

@@ -10,9 +10,11 @@
 #include "device.h"
 #include "domain.h"
 #include "eigen.h"
+#include "fields.h"
 #include "gep.h"
 #include "mesh.h"
 #include "mf.h"
+#include "petsc_io.h"
 
 namespace fem2d {
 static thread_local std::string g_last_error;
@@ -25,6 +27,7 @@ using namespace fem2d;
 struct fem2d_mesh { Mesh m; };
 struct fem2d_domain { Domain d; };
 struct fem2d_ctx { Ctx c; };
+struct fem2d_fields { FieldSpace f; };
 struct fem2d_gep {
   Domain dom;   // the Domain the GEP was sampled from (its Elem trees drive the factorization)
   HostGEP h;
@@ -489,6 +492,78 @@ int fem2d_gep_export_csr(const fem2d_gep* g, int which, int64_t* row_ptr, int32_
   API_END
 }
 
+// ------------------------------------------------------------------ PETSc-style files
+int fem2d_gep_print_to_petsc_binary_files(const fem2d_gep* g, const char* dir, const char* prefix) {
+  API_BEGIN
+  if (!g || !dir || !prefix) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::vector<double> v(g->h.nnz_full);
+  const std::string base = std::string(dir) + "/tmp/" + prefix;
+  for (int which = 0; which < 2; which++) {
+    if (g->h.nnz_full) {
+      FEM2D_CUDA(cudaSetDevice(g->ctx->device));
+      const double* src = which == 0 ? g->d.a.p : g->d.b.p;
+      FEM2D_CUDA(cudaMemcpyAsync(v.data(), src, g->h.nnz_full * 8, cudaMemcpyDeviceToHost, g->ctx->stream));
+      FEM2D_CUDA(cudaStreamSynchronize(g->ctx->stream));
+    }
+    aij_write(base + (which == 0 ? "_a.dat" : "_b.dat"), g->h.n, g->h.row_ptr.data(), g->h.col.data(), v.data());
+  }
+  API_END
+}
+
+int fem2d_aij_write(const char* path, int64_t n, const int64_t* row_ptr, const int32_t* col, const double* val) {
+  API_BEGIN
+  if (!path || !row_ptr || (n > 0 && row_ptr[n] > 0 && (!col || !val))) fail(FEM2D_E_INVALID_ARG, "null argument");
+  aij_write(path, n, row_ptr, col, val);
+  API_END
+}
+
+int fem2d_aij_read(const char* path, int64_t* n, int64_t* nnz, int64_t* row_ptr, int32_t* col, double* val) {
+  API_BEGIN
+  if (!path || !n || !nnz) fail(FEM2D_E_INVALID_ARG, "null argument");
+  AIJ m;
+  aij_read(path, m);
+  *n = m.n;
+  *nnz = (int64_t)m.col.size();
+  if (row_ptr) std::copy(m.row_ptr.begin(), m.row_ptr.end(), row_ptr);
+  if (col) std::copy(m.col.begin(), m.col.end(), col);
+  if (val) std::copy(m.val.begin(), m.val.end(), val);
+  API_END
+}
+
+int fem2d_petsc_vec_write(const char* path, const double* v, int64_t n) {
+  API_BEGIN
+  if (!path || (n > 0 && !v)) fail(FEM2D_E_INVALID_ARG, "null argument");
+  vec_write(path, v, n);
+  API_END
+}
+
+int fem2d_petsc_vec_read(const char* path, double* out, int64_t capacity, int64_t* n) {
+  API_BEGIN
+  if (!path || !n) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::vector<double> v;
+  vec_read(path, v);
+  *n = (int64_t)v.size();
+  if (out) {
+    if (capacity < (int64_t)v.size()) fail(FEM2D_E_INVALID_ARG, "output buffer too small");
+    std::copy(v.begin(), v.end(), out);
+  }
+  API_END
+}
+
+int fem2d_petsc_scalar_write(const char* path, double x) {
+  API_BEGIN
+  if (!path) fail(FEM2D_E_INVALID_ARG, "null argument");
+  scalar_write(path, x);
+  API_END
+}
+
+int fem2d_petsc_scalar_read(const char* path, double* x) {
+  API_BEGIN
+  if (!path || !x) fail(FEM2D_E_INVALID_ARG, "null argument");
+  *x = scalar_read(path);
+  API_END
+}
+
 // ------------------------------------------------------------------ eigensolvers
 int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, double* value, double* vector) {
   API_BEGIN
@@ -523,6 +598,75 @@ int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_p
     throw;
   }
   if (stats) *stats = st;
+  API_END
+}
+
+// ------------------------------------------------------------------ field evaluation
+int fem2d_fields_create(fem2d_ctx* c, const fem2d_domain* d, int basis, int d0, int d1, fem2d_fields** out) {
+  API_BEGIN
+  if (!c || !d || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  auto f = std::make_unique<fem2d_fields>();
+  fields_plan(c->c, d->d, basis, d0, d1, f->f);
+  *out = f.release();
+  API_END
+}
+
+void fem2d_fields_free(fem2d_fields* f) {
+  if (!f) return;
+  if (f->f.ctx) cudaSetDevice(f->f.ctx->device);
+  delete f;
+}
+
+int64_t fem2d_fields_num_leaves(const fem2d_fields* f) { return f ? (int64_t)f->f.leaves.size() : -1; }
+
+int fem2d_fields_leaves(const fem2d_fields* f, int64_t* ids) {
+  API_BEGIN
+  if (!f || !ids) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::copy(f->f.leaves.begin(), f->f.leaves.end(), ids);
+  API_END
+}
+
+int fem2d_fields_leaf_bounds(const fem2d_fields* f, double* out) {
+  API_BEGIN
+  if (!f || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::copy(f->f.leaf_bounds.begin(), f->f.leaf_bounds.end(), out);
+  API_END
+}
+
+static void check_solution_size(const FieldSpace& f, int64_t n) {
+  // fields.rs:68-72 MismatchedSolutionSize
+  if (n != f.ndofs)
+    fail(FEM2D_E_INVALID_ARG, "Domain size (" + std::to_string(f.ndofs) + ") does not match solution size (" +
+                                  std::to_string(n) + ")!");
+}
+
+int fem2d_fields_xy(fem2d_fields* f, const double* solution, int64_t n_solution, double* x_out, double* y_out) {
+  API_BEGIN
+  if (!f || !solution || !x_out || !y_out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  check_solution_size(f->f, n_solution);
+  FieldSpace& F = f->f;
+  Ctx& c = *F.ctx;
+  FEM2D_CUDA(cudaSetDevice(c.device));
+  const size_t pts = F.leaves.size() * (size_t)F.d0 * F.d1;
+  if (F.sol.n < (size_t)F.ndofs) F.sol.alloc((size_t)F.ndofs);
+  if (F.out.n < 2 * pts) F.out.alloc(2 * pts);
+  if (F.ndofs > 0)
+    FEM2D_CUDA(cudaMemcpyAsync(F.sol.p, solution, F.ndofs * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  fields_eval(F, F.sol.p, F.out.p, F.out.p + pts);
+  if (pts > 0) {
+    FEM2D_CUDA(cudaMemcpyAsync(x_out, F.out.p, pts * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaMemcpyAsync(y_out, F.out.p + pts, pts * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  }
+  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+  API_END
+}
+
+int fem2d_fields_xy_device(fem2d_fields* f, const double* d_solution, int64_t n_solution, double* d_x, double* d_y) {
+  API_BEGIN
+  if (!f || !d_x || !d_y || (!d_solution && n_solution > 0)) fail(FEM2D_E_INVALID_ARG, "null argument");
+  check_solution_size(f->f, n_solution);
+  FEM2D_CUDA(cudaSetDevice(f->f.ctx->device));
+  fields_eval(f->f, d_solution, d_x, d_y);
   API_END
 }
 

@@ -82,25 +82,6 @@ int default_ngq(int max_order) {   // basis.rs:172-177 (computed in f32 like the
 }
 
 namespace {
-// Jacobian data of an Elem over its own parametric range (element.rs:33-50, space.rs:137-147)
-struct Jac {
-  double a, b, det, ji_u0, ji_v1;
-};
-Jac elem_jac(const Mesh& m, int64_t e) {
-  auto pr = m.param_range(e);
-  const RootElement& r = m.roots[m.elems[e].root];
-  auto mr = [](double v, double lo, double hi) { return (v - -1.0) * (hi - lo) / (1.0 - -1.0) + lo; };
-  double xmin = mr(pr[0], r.x0, r.x3), xmax = mr(pr[1], r.x0, r.x3);
-  double ymin = mr(pr[2], r.y0, r.y3), ymax = mr(pr[3], r.y0, r.y3);
-  Jac j;
-  j.a = (xmax - xmin) / 2.0;
-  j.b = (ymax - ymin) / 2.0;
-  j.det = j.a * j.b - 0.0 * 0.0;
-  j.ji_u0 = j.b / j.det;
-  j.ji_v1 = j.a / j.det;
-  return j;
-}
-
 struct IvlKey {
   uint64_t s, o;
   bool operator<(const IvlKey& k) const { return s != k.s ? s < k.s : o < k.o; }
@@ -139,8 +120,8 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
     g.ivl_o.push_back(o);
     return id;
   };
-  std::vector<Jac> jac(ne);
-  for (int64_t e = 0; e < ne; e++) jac[e] = elem_jac(m, e);
+  std::vector<ElemJac> jac(ne);
+  for (int64_t e = 0; e < ne; e++) jac[e] = elem_jacobian(m, e);
   struct BInfo { int64_t p, q; int64_t nvis; bool local; };
   std::vector<BInfo> binfo;
   std::vector<int64_t> desc;
@@ -150,8 +131,8 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
     if (np == 0) continue;
     const RootElement& root = m.roots[m.elems[e].root];
     auto add_block = [&](int64_t q, bool local) {
-      const Jac& P = jac[e];
-      const Jac& Q = jac[q];
+      const ElemJac& P = jac[e];
+      const ElemJac& Q = jac[q];
       double su = 1.0, sv = 1.0, ou = 0.0, ov = 0.0;
       if (!local) {
         auto r = m.relative_range(q, e);

@@ -363,6 +363,21 @@ std::array<double, 4> Mesh::relative_range(int64_t e, int64_t a) const {
 
 std::array<double, 4> Mesh::param_range(int64_t e) const { return relative_range(e, -1); }
 
+ElemJac elem_jacobian(const Mesh& m, int64_t e) {
+  auto pr = m.param_range(e);
+  const RootElement& r = m.roots[m.elems[e].root];
+  auto mr = [](double v, double lo, double hi) { return (v - -1.0) * (hi - lo) / (1.0 - -1.0) + lo; };
+  double xmin = mr(pr[0], r.x0, r.x3), xmax = mr(pr[1], r.x0, r.x3);
+  double ymin = mr(pr[2], r.y0, r.y3), ymax = mr(pr[3], r.y0, r.y3);
+  ElemJac j;
+  j.a = (xmax - xmin) / 2.0;
+  j.b = (ymax - ymin) / 2.0;
+  j.det = j.a * j.b - 0.0 * 0.0;
+  j.ji_u0 = j.b / j.det;
+  j.ji_v1 = j.a / j.det;
+  return j;
+}
+
 void Mesh::descendants(int64_t e, std::vector<int64_t>& out) const {
   const MElem& el = elems[e];
   for (int k = 0; k < el.nchild; k++) {

@@ -106,4 +106,12 @@ class Mesh {
   bool activate_tree(int64_t e);
 };
 
+// Jacobian of an Elem's map from its own parametric square to real space (element.rs:33-50) and the
+// inverse-Jacobian diagonal the basis functions carry (space.rs:137-147): a = dx/du, b = dy/dv,
+// det = a*b, ji_u0 = b/det, ji_v1 = a/det (evaluated in exactly that order).
+struct ElemJac {
+  double a, b, det, ji_u0, ji_v1;
+};
+ElemJac elem_jacobian(const Mesh& m, int64_t e);
+
 }  // namespace fem2d

@@ -203,6 +203,47 @@ typedef struct fem2d_solve_stats {
 int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_pairs, const fem2d_solve_opts* opts,
                         double* values, double* vectors, double* residuals, fem2d_solve_stats* stats);
 
+/* ---------------- Files of the external-solver hand-off (linalg.rs, sparse_matrix.rs, slepc_solve.rs) -------- */
+/* GEP::print_to_petsc_binary_files (linalg.rs:44-52): writes {dir}/tmp/{prefix}_a.dat and _b.dat in the
+ * AIJMatrixBinary layout of sparse_matrix.rs:184-265 (bytes "\0{P", then u32 rows, cols, nnz, the
+ * per-row counts, the column indices, all big-endian, then the f64 values; both triangles, rows and
+ * columns ascending). The directory {dir}/tmp must exist. */
+int fem2d_gep_print_to_petsc_binary_files(const fem2d_gep* g, const char* dir, const char* prefix);
+/* the same layout from a host CSR (columns ascending within each row) */
+int fem2d_aij_write(const char* path, int64_t n, const int64_t* row_ptr, const int32_t* col, const double* val);
+/* reads that layout (or the standard PETSc one with the four-byte class id 1211216) into a CSR; call
+ * with NULL arrays first to learn n and nnz */
+int fem2d_aij_read(const char* path, int64_t* n, int64_t* nnz, int64_t* row_ptr, int32_t* col, double* val);
+/* retrieve_eigenvector (slepc_solve.rs:114-135): PETSc Vec binary (i32 class id 1211214, i32 m, m f64,
+ * big-endian); read: call with out == NULL to learn n */
+int fem2d_petsc_vec_write(const char* path, const double* v, int64_t n);
+int fem2d_petsc_vec_read(const char* path, double* out, int64_t capacity, int64_t* n);
+/* retrieve_eigenvalue (slepc_solve.rs:137-147): one big-endian f64 */
+int fem2d_petsc_scalar_write(const char* path, double x);
+int fem2d_petsc_scalar_read(const char* path, double* x);
+
+/* ---------------- Field evaluation (src/fem_domain/domain/fields.rs) ---------------- */
+typedef struct fem2d_fields fem2d_fields;
+/* UniformFieldSpace::new (fields.rs:29-39) plus the evaluation plan of xy_fields for one basis space
+ * (the reference's BSpace type parameter): a d0 x d1 grid of uniform_range(-1, 1, d) points
+ * (fields.rs:386-389) on every leaf Elem. Requires 2 <= d0, d1 <= 1024 and an H(curl) Domain. The
+ * reference indexes its per-leaf arrays as [d1][d0] but fills them [m < d0][n < d1], which only runs
+ * when d0 == d1; here the layout is [m][n] for every d0, d1, equal to the reference's when d0 == d1. */
+int fem2d_fields_create(fem2d_ctx* c, const fem2d_domain* d, int basis, int d0, int d1, fem2d_fields** out);
+void fem2d_fields_free(fem2d_fields* f);
+/* leaf Elems in ascending id (the reference's BTreeMap order, fields.rs:330-346) */
+int64_t fem2d_fields_num_leaves(const fem2d_fields* f);
+int fem2d_fields_leaves(const fem2d_fields* f, int64_t* ids);
+/* per leaf, 4 doubles: the real-space points of nodes[0] and nodes[3] (elem_diag_points, used for the
+ * VTK point grid of print_quantities_to_vkt, fields.rs:181-193) as (x0, y0, x3, y3) */
+int fem2d_fields_leaf_bounds(const fem2d_fields* f, double* out);
+/* xy_fields (fields.rs:63-122): x and y field values, each num_leaves x d0 x d1 doubles, [leaf][m][n]
+ * with m along u (x) and n along v (y). n_solution != num_dofs fails with FEM2D_E_INVALID_ARG
+ * (MismatchedSolutionSize). Host pointers; synchronous. */
+int fem2d_fields_xy(fem2d_fields* f, const double* solution, int64_t n_solution, double* x_out, double* y_out);
+/* the same on device pointers (an eigenvector left on the device); asynchronous on the context's stream */
+int fem2d_fields_xy_device(fem2d_fields* f, const double* d_solution, int64_t n_solution, double* d_x, double* d_y);
+
 #ifdef __cplusplus
 }
 #endif

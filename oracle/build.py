@@ -1,6 +1,7 @@
 """Build recipe for the oracle library (test infrastructure; no reference sources are compiled).
 
-``liboracle.so`` is built from ``fem2d_oracle.cpp`` with g++ only. It is rebuilt on the machine that
+``liboracle.so`` is built from ``fem2d_oracle.cpp`` with g++ only, without fused multiply-adds (the
+reference's Rust arithmetic rounds every product and sum). It is rebuilt on the machine that
 runs the tests, since nothing compiled on one architecture runs on the other.
 """
 import os
@@ -15,7 +16,7 @@ def build_oracle(force=False):
     out = os.path.join(HERE, "liboracle.so")
     if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
         return out
-    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-function",
+    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-function",
            src, "-o", out + ".tmp"]
     subprocess.check_call(cmd)
     os.replace(out + ".tmp", out)

@@ -1277,6 +1277,51 @@ static GEPResult galerkin(const Domain& dom, int basis, int nu, int nv, int nthr
   return r;
 }
 
+// fields.rs:386-389
+static std::vector<double> uniform_range(double min, double max, size_t n) {
+  double step = (max - min) / ((double)(n - 1));
+  std::vector<double> r(n);
+  for (size_t i = 0; i < n; i++) r[i] = ((double)i) * step + min;
+  return r;
+}
+
+// UniformFieldSpace::xy_fields (fields.rs:63-122). Leaves in ascending id; per leaf a d0 x d1 grid
+// [m][n] (m along u). The reference allocates its per-leaf arrays [d1][d0] and indexes them [m][n],
+// which only runs for d0 == d1; this restatement uses [m][n] for any d0, d1.
+static void xy_fields(const Domain& dom, int basis, size_t d0, size_t d1, const std::vector<double>& sol,
+                      std::vector<double>& xo, std::vector<double>& yo) {
+  if (sol.size() != dom.ndofs) throw std::runtime_error("MismatchedSolutionSize");
+  const Mesh& mesh = dom.mesh;
+  std::vector<double> pu = uniform_range(-1.0, 1.0, d0), pv = uniform_range(-1.0, 1.0, d1);
+  auto mo = mesh.max_expansion_orders();
+  xo.clear();
+  yo.clear();
+  for (const Elem& leaf : mesh.elems) {
+    if (leaf.has_children) continue;
+    std::vector<double> xv(d0 * d1, 0.0), yv(d0 * d1, 0.0);
+    // ancestor_elems(leaf, true) (mesh.rs:520-541): the leaf, then each parent up to the root
+    std::vector<size_t> chain{leaf.id};
+    for (auto it = leaf.ancestors.rbegin(); it != leaf.ancestors.rend(); ++it) chain.push_back(it->first);
+    for (size_t a : chain) {
+      BasisFn bf = defined_over(mesh, mesh.elems[a], &leaf, pu, pv, mo[0], mo[1], basis);
+      for (const BasisSpec& bs : dom.basis_specs[a]) {
+        for (size_t m = 0; m < d0; m++) {
+          for (size_t n = 0; n < d1; n++) {
+            V2 f = {0.0, 0.0};
+            if (bs.dir == BD_U) f = f_u(bf, bs.i, bs.j, (int)m, (int)n);
+            else if (bs.dir == BD_V) f = f_v(bf, bs.i, bs.j, (int)m, (int)n);
+            double c = sol[(size_t)bs.dof_id];
+            xv[m * d1 + n] += f.x * c;
+            yv[m * d1 + n] += f.y * c;
+          }
+        }
+      }
+    }
+    xo.insert(xo.end(), xv.begin(), xv.end());
+    yo.insert(yo.end(), yv.begin(), yv.end());
+  }
+}
+
 }  // namespace oracle
 
 // ---------------------------------------------------------------------------
@@ -1430,6 +1475,23 @@ int oracle_galerkin(void* h, int basis, int nu, int nv, int nthreads, int64_t* n
     if ((nu > 0 && nu < 4) || (nv > 0 && nv < 4)) throw std::runtime_error("InvalidGLQSettings");
     s->gep = galerkin(*s->dom, basis, nu, nv, nthreads);
     *nnz_upper = (int64_t)s->gep.rows.size();
+  })
+}
+int oracle_num_leaves(void* h) {
+  auto* s = (OracleState*)h;
+  int n = 0;
+  for (const Elem& e : s->mesh.elems) n += e.has_children ? 0 : 1;
+  return n;
+}
+int oracle_xy_fields(void* h, int basis, int d0, int d1, const double* sol, int64_t nsol, double* xo, double* yo) {
+  auto* s = (OracleState*)h;
+  ORACLE_TRY({
+    if (!s->dom) throw std::runtime_error("domain not built");
+    if (d0 < 2 || d1 < 2) throw std::runtime_error("densities below 2");
+    std::vector<double> v(sol, sol + nsol), x, y;
+    xy_fields(*s->dom, basis, (size_t)d0, (size_t)d1, v, x, y);
+    std::copy(x.begin(), x.end(), xo);
+    std::copy(y.begin(), y.end(), yo);
   })
 }
 int oracle_gep_export(void* h, int32_t* rows, int32_t* cols, double* a, double* b) {

@@ -59,6 +59,8 @@ def lib():
         L.oracle_glq.argtypes = [ctypes.c_int, f64p, f64p]
         L.oracle_shapes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, f64p]
         L.oracle_default_ngq.argtypes = [ctypes.c_int]
+        L.oracle_num_leaves.argtypes = [P]
+        L.oracle_xy_fields.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, ctypes.c_int64, f64p, f64p]
         _LIB = L
     return _LIB
 
@@ -168,6 +170,18 @@ class OracleMesh:
         out = np.zeros((n, 6), dtype=np.int64)
         _check(lib().oracle_specs(self.h, _p(out, ctypes.c_int64)))
         return out
+
+    def xy_fields(self, solution, d0, d1, basis=HIERPOLY):
+        """UniformFieldSpace::xy_fields restated (fields.rs:63-122): (x, y), each (leaves, d0, d1)."""
+        if self.ndofs is None:
+            self.domain()
+        nl = lib().oracle_num_leaves(self.h)
+        sol = np.ascontiguousarray(solution, dtype=np.float64)
+        x = np.zeros((nl, d0, d1))
+        y = np.zeros((nl, d0, d1))
+        _check(lib().oracle_xy_fields(self.h, basis, d0, d1, _p(sol, ctypes.c_double), len(sol),
+                                      _p(x, ctypes.c_double), _p(y, ctypes.c_double)))
+        return x, y
 
     def galerkin(self, basis=HIERPOLY, nu=0, nv=0, threads=1):
         """Upper-triangle COO (rows, cols, a, b), sorted by (row, col) like the reference's BTreeMap."""
@@ -315,3 +329,96 @@ def dense_nearest_physical(A, B, sigma, k, spurious=1e-6):
     ok = np.nonzero(np.abs(w) > spurious * abs(sigma))[0]
     ok = ok[np.argsort(np.abs(w[ok] - sigma), kind="stable")][:k]
     return w[ok], v[:, ok]
+
+
+def tangential_jumps(bounds, ex, ey):
+    """Largest jump of the tangential field across the interior lines shared by two leaf Elems.
+
+    ``bounds`` holds per leaf (x0, y0, x3, y3); ``ex``/``ey`` are (leaves, d0, d1) grids with m along x.
+    On a vertical line the tangential component is E_y, on a horizontal line E_x. Grid points are
+    matched where both leaves sample the same coordinate strictly inside the common segment (hanging
+    edges included). An H(curl)-conforming discrete space gives zero jumps for every coefficient vector.
+    Returns (max |jump| / max |E|, number of matched points).
+    """
+    nl, d0, d1 = ex.shape
+    gu = np.linspace(0.0, 1.0, d0)
+    gv = np.linspace(0.0, 1.0, d1)
+    scale = max(np.max(np.abs(ex)), np.max(np.abs(ey)), 1e-300)
+    worst, count = 0.0, 0
+    tol = 1e-12
+    key = lambda v: round(float(v), 9)   # noqa: E731
+    starts_x, starts_y = {}, {}
+    for b in range(nl):
+        starts_x.setdefault(key(bounds[b][0]), []).append(b)
+        starts_y.setdefault(key(bounds[b][1]), []).append(b)
+    for a in range(nl):
+        A = bounds[a]
+        for b in starts_x.get(key(A[2]), []):   # b to the right of a
+            B = bounds[b]
+            lo, hi = max(A[1], B[1]), min(A[3], B[3])
+            if b == a or hi - lo <= tol:
+                continue
+            ya = A[1] + gv * (A[3] - A[1])
+            yb = B[1] + gv * (B[3] - B[1])
+            for i, yy in enumerate(ya):
+                if lo + tol < yy < hi - tol:
+                    for j in np.nonzero(np.abs(yb - yy) < tol)[0]:
+                        worst = max(worst, abs(ey[a, d0 - 1, i] - ey[b, 0, j]))
+                        count += 1
+        for b in starts_y.get(key(A[3]), []):   # b above a
+            B = bounds[b]
+            lo, hi = max(A[0], B[0]), min(A[2], B[2])
+            if b == a or hi - lo <= tol:
+                continue
+            xa = A[0] + gu * (A[2] - A[0])
+            xb = B[0] + gu * (B[2] - B[0])
+            for i, xx in enumerate(xa):
+                if lo + tol < xx < hi - tol:
+                    for j in np.nonzero(np.abs(xb - xx) < tol)[0]:
+                        worst = max(worst, abs(ex[a, i, d1 - 1] - ex[b, j, 0]))
+                        count += 1
+    return worst / scale, count
+
+
+class OracleSparseMatrix:
+    """SparseMatrix restated (sparse_matrix.rs:12-127): upper-triangle map, r <= c keys, += on collision."""
+
+    def __init__(self, dimension):
+        self.dimension = int(dimension)
+        self.entries = {}
+
+    def insert(self, rc, value):
+        r, c = int(rc[0]), int(rc[1])
+        assert r < self.dimension and c < self.dimension
+        key = (r, c) if r <= c else (c, r)
+        if key in self.entries:
+            self.entries[key] += value
+        else:
+            self.entries[key] = value
+
+    def aij_bytes(self):
+        """From<SparseMatrix> for AIJMatrixBinary + print_to_petsc_binary_file (sparse_matrix.rs:184-265)."""
+        import struct
+
+        n = self.dimension
+        row_counts = [0] * n
+        for (r, c) in self.entries:
+            row_counts[r] += 1
+            if r != c:
+                row_counts[c] += 1
+        full = {(c, r): v for (r, c), v in self.entries.items()}
+        full.update(self.entries)
+        keys = sorted(full)
+        out = bytearray(b"\0{P")
+        out += struct.pack(">III", n, n, len(keys))
+        out += struct.pack(">%dI" % n, *row_counts)
+        out += struct.pack(">%dI" % len(keys), *[c for (_, c) in keys])
+        out += struct.pack(">%dd" % len(keys), *[full[k] for k in keys])
+        return bytes(out)
+
+
+def petsc_vec_bytes(values):
+    """The PETSc Vec binary retrieve_eigenvector reads (slepc_solve.rs:114-135)."""
+    import struct
+
+    return struct.pack(">ii", 1211214, len(values)) + struct.pack(">%dd" % len(values), *values)

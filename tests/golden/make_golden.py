@@ -5,11 +5,13 @@ test suite only read the committed kat.json. Contents:
 
 * the three mesh files of test_input/ (src/lib.rs:46-120 use a and b);
 * test_input/test_eval.dat (big-endian f64) and test_input/test_evec.dat (PETSc Vec, classid 1211214,
-  big-endian i32 header then f64 values), the slepc_problem known answer (src/lib.rs:83-120);
+  big-endian i32 header then f64 values), the slepc_problem known answer (src/lib.rs:83-120), and the
+  SHA-256 of both files (pins the byte layout that slepc_solve.rs:114-147 reads);
 * the 20-point Gauss-Legendre tables X_20, W_20 and X_20_SCALED, parsed from the test module of
   src/fem_problem/integration/glq.rs (lines 255-375) as text;
 * the scalar known answers asserted in src/lib.rs (2.6479657 at 1e-6, 1.4745880937 at 1e-9).
 """
+import hashlib
 import json
 import os
 import re
@@ -33,9 +35,13 @@ def main(root):
         with open(os.path.join(ti, "test_mesh_%s.json" % tag)) as f:
             out["mesh_" + tag] = json.load(f)
     with open(os.path.join(ti, "test_eval.dat"), "rb") as f:
-        out["slepc_eval"] = struct.unpack(">d", f.read(8))[0]
+        raw_eval = f.read()
+    out["slepc_eval"] = struct.unpack(">d", raw_eval[:8])[0]
+    out["slepc_eval_sha256"] = hashlib.sha256(raw_eval).hexdigest()
     with open(os.path.join(ti, "test_evec.dat"), "rb") as f:
         raw = f.read()
+    out["slepc_evec_sha256"] = hashlib.sha256(raw).hexdigest()
+    out["slepc_evec_bytes"] = len(raw)
     classid, m = struct.unpack(">ii", raw[:8])
     assert classid == 1211214
     out["slepc_evec"] = list(struct.unpack(">%dd" % m, raw[8:8 + 8 * m]))

@@ -136,3 +136,25 @@ def test_galerkin_errors(kat, ctx):
     with pytest.raises(fg.Fem2dError) as e:
         fg.galerkin_sample_gep_hcurl(fg.HierPoly, fg.CurlCurl, fg.L2Inner, fg.Domain.from_mesh(one), [8, 8], ctx=ctx)
     assert e.value.code == fg.E_EMPTY_DOFS
+
+
+def test_print_to_petsc_binary_files(oracle_lib, kat, ctx, tmp_path):
+    """GEP::print_to_petsc_binary_files (linalg.rs:44-52) from the device-assembled GEP: the two files
+    hold exactly the AIJMatrixBinary bytes of the exported CSR, and read back to the same CSR."""
+    import os
+
+    n, ref_coo, gep = _assemble_both(oracle_lib, kat["mesh_b"], [("pref", 3, 3, None), ("href", 0, None, -1),
+                                                                ("href", 0, [6, 9, 12], -1)], 0, (8, 8), ctx)
+    os.makedirs(os.path.join(tmp_path, "tmp"))
+    gep.print_to_petsc_binary_files(tmp_path, "p_00000001")
+    for which, tag in ((0, "a"), (1, "b")):
+        rp, col, val = gep.csr(which)
+        rp2, col2, val2 = fg.aij_read(os.path.join(tmp_path, "tmp", "p_00000001_%s.dat" % tag))
+        np.testing.assert_array_equal(rp2, rp)
+        np.testing.assert_array_equal(col2, col)
+        np.testing.assert_array_equal(val2, val)
+        sm = oracle_lib.OracleSparseMatrix(n)
+        r, c, a, b = gep.upper_coo()
+        for i, j, v in zip(r, c, a if which == 0 else b):
+            sm.insert((i, j), float(v))
+        assert open(os.path.join(tmp_path, "tmp", "p_00000001_%s.dat" % tag), "rb").read() == sm.aij_bytes()
