@@ -47,7 +47,8 @@ class _fem2d_solve_opts(ctypes.Structure):
 class _fem2d_solve_stats(ctypes.Structure):
     _fields_ = [("outer_iters", ctypes.c_int), ("inner_iters_total", ctypes.c_int), ("converged", ctypes.c_int),
                 ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
-                ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64)]
+                ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64),
+                ("refine_spd", ctypes.c_int), ("refine_indefinite", ctypes.c_int)]
 
 
 def lib():
@@ -93,6 +94,12 @@ def lib():
         "fem2d_galerkin_sample_gep_hcurl": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, PP]),
         "fem2d_gep_recompute": (ctypes.c_int, [P, P]),
         "fem2d_gep_values_noalloc": (ctypes.c_int, [P, P, ctypes.c_void_p, ctypes.c_void_p]),
+        "fem2d_galerkin_sample_gep_hcurl_batch": (ctypes.c_int, [P, PP, i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                          ctypes.c_int, PP, dp]),
+        "fem2d_gep_batch_recompute": (ctypes.c_int, [P, PP, i64, ctypes.c_int, dp]),
+        "fem2d_autotune_export": (ctypes.c_int, [ctypes.c_char_p, i64, i64p]),
+        "fem2d_autotune_import": (ctypes.c_int, [ctypes.c_char_p, i64p]),
+        "fem2d_autotune_clear": (ctypes.c_int, []),
         "fem2d_gep_free": (None, [P]),
         "fem2d_gep_dims": (ctypes.c_int, [P, i64p, i64p, i64p]),
         "fem2d_gep_export_upper": (ctypes.c_int, [P, i32p, i32p, dp, dp]),
@@ -109,6 +116,7 @@ def lib():
         "fem2d_gep_shifted_solve": (ctypes.c_int, [P, P, d, d, ctypes.c_int, ctypes.c_int, dp, dp]),
         "fem2d_gpu_solve_gep": (ctypes.c_int, [P, P, d, ctypes.c_int, ctypes.POINTER(_fem2d_solve_opts), dp, dp, dp,
                                                 ctypes.POINTER(_fem2d_solve_stats)]),
+        "fem2d_gep_spmm_device": (ctypes.c_int, [P, P, d, d, ctypes.c_void_p, i64, ctypes.c_int, ctypes.c_void_p, i64]),
         "fem2d_gep_print_to_petsc_binary_files": (ctypes.c_int, [P, ctypes.c_char_p, ctypes.c_char_p]),
         "fem2d_aij_write": (ctypes.c_int, [ctypes.c_char_p, i64, i64p, i32p, dp]),
         "fem2d_aij_read": (ctypes.c_int, [ctypes.c_char_p, i64p, i64p, i64p, i32p, dp]),
@@ -391,6 +399,7 @@ class Context:
         h = ctypes.c_void_p()
         _check(lib().fem2d_ctx_create(device, ctypes.byref(h)))
         self._h = h
+        self.device = device
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -500,6 +509,12 @@ class GEP:
                                              r2.shape[1], _ptr(r2, ctypes.c_double), _ptr(x, ctypes.c_double)))
         return x[:, 0] if one else x
 
+    def spmm_device(self, c_a, c_b, d_x, ldx, nb, d_y, ldy, ctx=None):
+        """Y = c_a A X + c_b B X on the device (raw device pointers, row-major n x nb blocks)."""
+        ctx = ctx or self.ctx
+        _check(lib().fem2d_gep_spmm_device(ctx._h, self._h, float(c_a), float(c_b), ctypes.c_void_p(d_x), int(ldx),
+                                           int(nb), ctypes.c_void_p(d_y), int(ldy)))
+
     def print_to_petsc_binary_files(self, dir, prefix):
         """GEP::print_to_petsc_binary_files (linalg.rs:44-52): {dir}/tmp/{prefix}_a.dat and _b.dat."""
         _check(lib().fem2d_gep_print_to_petsc_binary_files(self._h, str(dir).encode(), str(prefix).encode()))
@@ -524,6 +539,96 @@ def galerkin_sample_gep_hcurl(bspace, a_integral, b_integral, domain, glq_grid_d
     h = ctypes.c_void_p()
     _check(lib().fem2d_galerkin_sample_gep_hcurl(ctx._h, domain._h, bspace.ID, nu, nv, ctypes.byref(h)))
     return GEP(h.value, ctx)
+
+
+def _batch_report(rep):
+    return {"ms_tables": float(rep[0]), "ms_values": float(rep[1]), "threads": int(rep[2]),
+            "ctas_per_sm": int(rep[3]), "entries": int(rep[4]), "codes": int(rep[5])}
+
+
+def galerkin_sample_gep_hcurl_batch(bspace, a_integral, b_integral, domains, glq_grid_dim=None, ctx=None,
+                                    autotune=True):
+    """galerkin_sample_gep_hcurl for many Domains: one GEP per Domain, the device numeric phase of all of
+    them in one table launch plus one persistent value launch (launch shape autotuned and cached).
+
+    Returns (list of GEP, report dict with the two launches' device times and the chosen launch shape).
+    """
+    if a_integral is not CurlCurl or b_integral is not L2Inner:
+        raise Fem2dError(E_INVALID_ARG, "only <CurlCurl, L2Inner> is provided")
+    ctx = ctx or Context.default()
+    nu, nv = (0, 0) if glq_grid_dim is None else (int(glq_grid_dim[0]), int(glq_grid_dim[1]))
+    n = len(domains)
+    hs = (ctypes.c_void_p * max(n, 1))(*[d._h.value for d in domains])
+    out = (ctypes.c_void_p * max(n, 1))()
+    rep = np.zeros(6)
+    _check(lib().fem2d_galerkin_sample_gep_hcurl_batch(ctx._h, hs, n, bspace.ID, nu, nv, 1 if autotune else 0, out,
+                                                       _ptr(rep, ctypes.c_double)))
+    return [GEP(out[i], ctx) for i in range(n)], _batch_report(rep)
+
+
+def gep_batch_recompute(geps, ctx=None, autotune=True):
+    """Recompute the values of many GEPs (same device) with the two batched launches; returns the report."""
+    ctx = ctx or geps[0].ctx
+    hs = (ctypes.c_void_p * max(len(geps), 1))(*[g._h.value for g in geps])
+    rep = np.zeros(6)
+    _check(lib().fem2d_gep_batch_recompute(ctx._h, hs, len(geps), 1 if autotune else 0, _ptr(rep, ctypes.c_double)))
+    return _batch_report(rep)
+
+
+def autotune_cache():
+    """The autotuner's launch-shape cache as {key: (threads, ctas_per_sm)}."""
+    n = ctypes.c_int64()
+    _check(lib().fem2d_autotune_export(None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib().fem2d_autotune_export(buf, n.value + 1, ctypes.byref(n)))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        k, t, c = line.split()
+        out[k] = (int(t), int(c))
+    return out
+
+
+def autotune_save(path):
+    """Write the autotuner cache to a JSON file."""
+    import json
+
+    with open(path, "w") as f:
+        json.dump({k: list(v) for k, v in autotune_cache().items()}, f, indent=1, sort_keys=True)
+
+
+def autotune_load(path):
+    """Merge a JSON file written by autotune_save into the cache; returns the number of entries read."""
+    import json
+
+    with open(path) as f:
+        d = json.load(f)
+    text = "".join("%s %d %d\n" % (k, int(v[0]), int(v[1])) for k, v in d.items())
+    n = ctypes.c_int64()
+    _check(lib().fem2d_autotune_import(text.encode(), ctypes.byref(n)))
+    return n.value
+
+
+def autotune_clear():
+    _check(lib().fem2d_autotune_clear())
+
+
+def gpu_solve_gep_batch(geps, target, n_pairs, workers=8, device=None, **kw):
+    """gpu_solve_gep_n for many independent GEPs on one GPU: `workers` host threads, each with its own
+    Context (CUDA stream), so the small latency-bound solves of different meshes overlap on the device.
+    Returns the list of SolveResult in input order (an exception of any solve is re-raised)."""
+    import concurrent.futures as cf
+    import threading
+
+    dev = geps[0].ctx.device if device is None else device
+    local = threading.local()
+
+    def one(g):
+        if getattr(local, "ctx", None) is None:
+            local.ctx = Context(dev)
+        return gpu_solve_gep_n(g, target, n_pairs, ctx=local.ctx, **kw)
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        return list(ex.map(one, geps))
 
 
 # ----------------------------------------------------------------------------- external-solver files
@@ -615,15 +720,17 @@ PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
 
 
 def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOBI, tol=0.0, max_outer=0,
-                    max_inner=0, inner_tol=0.0, block=0, verbose=0):
-    """The n_pairs eigenpairs nearest target by the device shift-invert solver."""
+                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None):
+    """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
+    the context the GEP was built on)."""
+    ctx = ctx or gep.ctx
     n = gep.dimension
     vals = np.zeros(n_pairs)
     vecs = np.zeros((n_pairs, n))
     res = np.zeros(n_pairs)
     o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose)
     st = _fem2d_solve_stats()
-    _check(lib().fem2d_gpu_solve_gep(gep.ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
+    _check(lib().fem2d_gpu_solve_gep(ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
                                      _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),
                                      _ptr(res, ctypes.c_double), ctypes.byref(st)))
     stats = {k: getattr(st, k) for k, _ in _fem2d_solve_stats._fields_}

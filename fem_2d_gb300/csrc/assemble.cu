@@ -14,34 +14,16 @@
 #include <string>
 
 #include "device.h"
-#include "shape.cuh"
+#include "contract.cuh"
 
 namespace fem2d {
 
 namespace {
 
-// kind -> (family of the outer Elem at the scaled points, family of the inner Elem)
-__constant__ int c_kind_fam[5][2] = {{0, 0}, {3, 3}, {2, 2}, {0, 3}, {3, 0}};
-
 __global__ void fem2d_contract1d_kernel(int basis, int P, int nivl, const double* __restrict__ ivl,
                                         const double* __restrict__ glq, int nq_u, int nq_v,
                                         double* __restrict__ tables) {
-  const int iv = blockIdx.x, axis = blockIdx.y, kind = blockIdx.z;
-  const int nq = axis == 0 ? nq_u : nq_v;
-  const double* xs = axis == 0 ? glq : glq + 2 * nq_u;
-  const double* ws = xs + nq;
-  const double s = ivl[2 * iv], o = ivl[2 * iv + 1];
-  const int fa = c_kind_fam[kind][0], fb = c_kind_fam[kind][1];
-  double* out = tables + (((size_t)axis * nivl + iv) * 5 + kind) * P * P;
-  for (int t = threadIdx.x; t < P * P; t += blockDim.x) {
-    const int a = t / P, b = t % P;
-    double acc = 0.0;
-    for (int m = 0; m < nq; m++) {
-      const double x = xs[m];
-      acc += ws[m] * shape(basis, fa, a, s * x + o) * shape(basis, fb, b, x);
-    }
-    out[t] = acc;
-  }
+  contract1d_table(basis, P, nivl, blockIdx.x, blockIdx.y, blockIdx.z, ivl, glq, nq_u, nq_v, tables);
 }
 
 __global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const int64_t* __restrict__ cptr,
@@ -50,41 +32,9 @@ __global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const in
                                                            const uint32_t* __restrict__ specs,
                                                            const double* __restrict__ tables, int P, int nivl,
                                                            double* __restrict__ A, double* __restrict__ B) {
-  const size_t PP = (size_t)P * P;
-  const size_t axis_stride = (size_t)nivl * 5 * PP;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k0 = __ldg(cptr + e), k1 = __ldg(cptr + e + 1);
-    double sa = 0.0, sb = 0.0;
-    for (int64_t k = k0; k < k1; k++) {
-      const uint64_t code = __ldg(codes + k);
-      const GBlock* bl = blocks + (code >> 32);
-      const int2 sp = __ldg(reinterpret_cast<const int2*>(bl));
-      const int2 iv = __ldg(reinterpret_cast<const int2*>(bl) + 1);
-      const uint32_t p = __ldg(specs + sp.x + (int)((code >> 16) & 0xffff));
-      const uint32_t q = __ldg(specs + sp.y + (int)(code & 0xffff));
-      const int pi = p & 0xff, pj = (p >> 8) & 0xff, pd = (p >> 16) & 0xff;
-      const int qi = q & 0xff, qj = (q >> 8) & 0xff, qd = (q >> 16) & 0xff;
-      const double* gu = tables + (size_t)iv.x * 5 * PP + (size_t)pi * P + qi;
-      const double* gv = tables + axis_stride + (size_t)iv.y * 5 * PP + (size_t)pj * P + qj;
-      const int dd = pd * 2 + qd;   // 0 UU, 1 UV, 2 VU, 3 VV
-      const double ca = __ldg(bl->ca + dd);
-      double va, vb = 0.0;
-      if (dd == 0) {
-        const double nn = __ldg(gu + G_NN * PP);
-        va = ca * nn * __ldg(gv + G_DD * PP);
-        vb = __ldg(bl->cb) * nn * __ldg(gv + G_TT * PP);
-      } else if (dd == 3) {
-        const double nn = __ldg(gv + G_NN * PP);
-        va = ca * __ldg(gu + G_DD * PP) * nn;
-        vb = __ldg(bl->cb + 1) * __ldg(gu + G_TT * PP) * nn;
-      } else if (dd == 1) {
-        va = ca * __ldg(gu + G_ND * PP) * __ldg(gv + G_DN * PP);
-      } else {
-        va = ca * __ldg(gu + G_DN * PP) * __ldg(gv + G_ND * PP);
-      }
-      sa += va;
-      sb += vb;
-    }
+    double sa, sb;
+    entry_values(__ldg(cptr + e), __ldg(cptr + e + 1), codes, blocks, specs, tables, P, nivl, sa, sb);
     A[e] = sa;
     B[e] = sb;
   }

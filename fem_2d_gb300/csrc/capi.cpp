@@ -4,6 +4,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <mutex>
 #include <sstream>
 
 #include "common.h"
@@ -13,6 +14,7 @@
 #include "fields.h"
 #include "gep.h"
 #include "mesh.h"
+#include "batch.h"
 #include "mf.h"
 #include "petsc_io.h"
 
@@ -34,6 +36,7 @@ struct fem2d_gep {
   DeviceGEP d;
   Ctx* ctx = nullptr;
   double t_symbolic_ms = 0, t_tables_ms = 0, t_values_ms = 0, t_upload_ms = 0;
+  mutable MFPlan plan;   // factorization plan, built by the first solve and reused (pattern-only)
 };
 
 #define API_BEGIN try {
@@ -421,6 +424,108 @@ int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, doub
   API_END
 }
 
+static void check_galerkin_args(const fem2d_domain* d, int basis, int nq_u, int nq_v) {
+  // galerkin.rs:42-59
+  if (d->d.cc != FEM2D_CC_HCURL)
+    fail(FEM2D_E_WRONG_CC, "Wrong Continuity Condition on Domain (required: H(Curl)); Cannot execute Galerkin Sampling!");
+  if (d->d.ndofs == 0)
+    fail(FEM2D_E_EMPTY_DOFS, "No Degrees-of-Freedom Defined over Domain; Cannot execute Galerkin Sampling!");
+  if ((nq_u != 0 || nq_v != 0) && (nq_u < 4 || nq_v < 4))
+    fail(FEM2D_E_INVALID_GLQ, "Invalid GLQ Settings (the number of GLQ points must be at least 4); Cannot execute Galerkin Sampling!");
+  if (basis != FEM2D_BASIS_HIERPOLY && basis != FEM2D_BASIS_KOLEG) fail(FEM2D_E_INVALID_ARG, "unknown basis space");
+  auto mo = d->d.mesh.max_orders();
+  if (basis == FEM2D_BASIS_KOLEG && std::max(mo[0], mo[1]) > 12)
+    fail(FEM2D_E_INVALID_ARG, "KOLeg is tabulated for expansion orders up to 12");
+  if (d->d.ndofs >= (1ll << 31)) fail(FEM2D_E_INVALID_ARG, "more than 2^31 DoFs");
+}
+
+static void batch_report_out(const BatchReport& r, double* report) {
+  if (!report) return;
+  report[0] = r.ms_tables;
+  report[1] = r.ms_values;
+  report[2] = r.shape.threads;
+  report[3] = r.shape.ctas_per_sm;
+  report[4] = (double)r.total_entries;
+  report[5] = (double)r.total_codes;
+}
+
+int fem2d_galerkin_sample_gep_hcurl_batch(fem2d_ctx* c, const fem2d_domain* const* domains, int64_t count, int basis,
+                                          int nq_u, int nq_v, int autotune, fem2d_gep** out, double* report) {
+  API_BEGIN
+  if (!c || !out || (count > 0 && !domains)) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (count < 0 || count > (1 << 24)) fail(FEM2D_E_INVALID_ARG, "batch size out of range");
+  for (int64_t i = 0; i < count; i++) {
+    if (!domains[i]) fail(FEM2D_E_INVALID_ARG, "null domain in the batch");
+    check_galerkin_args(domains[i], basis, nq_u, nq_v);
+  }
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  std::vector<std::unique_ptr<fem2d_gep>> gs;
+  std::vector<BatchMember> members;
+  for (int64_t i = 0; i < count; i++) {
+    std::unique_ptr<fem2d_gep> g(new fem2d_gep);
+    g->ctx = &c->c;
+    g->dom = domains[i]->d;
+    auto t0 = std::chrono::steady_clock::now();
+    build_symbolic(domains[i]->d, basis, nq_u, nq_v, g->h);
+    auto t1 = std::chrono::steady_clock::now();
+    device_upload(c->c, g->h, g->d);
+    g->t_symbolic_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    gs.push_back(std::move(g));
+  }
+  for (auto& g : gs) members.push_back(BatchMember{&g->h, &g->d});
+  FEM2D_CUDA(cudaStreamSynchronize(c->c.stream));
+  BatchReport rep;
+  batch_assemble(c->c, members, autotune != 0, &rep);
+  batch_report_out(rep, report);
+  for (int64_t i = 0; i < count; i++) {
+    gs[i]->t_tables_ms = rep.ms_tables;   // shared by the whole batch
+    gs[i]->t_values_ms = rep.ms_values;
+    out[i] = gs[i].release();
+  }
+  API_END
+}
+
+int fem2d_gep_batch_recompute(fem2d_ctx* c, fem2d_gep* const* geps, int64_t count, int autotune, double* report) {
+  API_BEGIN
+  if (!c || (count > 0 && !geps)) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::vector<BatchMember> members;
+  for (int64_t i = 0; i < count; i++) {
+    if (!geps[i]) fail(FEM2D_E_INVALID_ARG, "null GEP in the batch");
+    if (geps[i]->ctx->device != c->c.device) fail(FEM2D_E_INVALID_ARG, "the batch spans devices");
+    members.push_back(BatchMember{&geps[i]->h, &geps[i]->d});
+  }
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  BatchReport rep;
+  batch_assemble(c->c, members, autotune != 0, &rep);
+  batch_report_out(rep, report);
+  API_END
+}
+
+int fem2d_autotune_export(char* buf, int64_t capacity, int64_t* length) {
+  API_BEGIN
+  const std::string t = tune_export();
+  if (length) *length = (int64_t)t.size();
+  if (buf) {
+    if (capacity < (int64_t)t.size() + 1) fail(FEM2D_E_INVALID_ARG, "buffer too small for the autotuner cache");
+    std::memcpy(buf, t.c_str(), t.size() + 1);
+  }
+  API_END
+}
+
+int fem2d_autotune_import(const char* text, int64_t* entries) {
+  API_BEGIN
+  if (!text) fail(FEM2D_E_INVALID_ARG, "null argument");
+  const int n = tune_import(text);
+  if (entries) *entries = n;
+  API_END
+}
+
+int fem2d_autotune_clear(void) {
+  API_BEGIN
+  tune_clear();
+  API_END
+}
+
 void fem2d_gep_free(fem2d_gep* g) {
   if (!g) return;
   if (g->ctx) cudaSetDevice(g->ctx->device);
@@ -569,7 +674,8 @@ int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, doubl
   API_BEGIN
   if (!c || !g) fail(FEM2D_E_INVALID_ARG, "null argument");
   FEM2D_CUDA(cudaSetDevice(c->c.device));
-  dense_solve(c->c, g->dom, g->h, g->d, target, value, vector);
+  std::lock_guard<std::mutex> lk(g->plan.mu);
+  dense_solve(c->c, g->dom, g->h, g->d, g->plan, target, value, vector);
   API_END
 }
 
@@ -578,7 +684,19 @@ int fem2d_gep_shifted_solve(fem2d_ctx* c, const fem2d_gep* g, double c_a, double
   API_BEGIN
   if (!c || !g || !rhs || !x || nrhs <= 0) fail(FEM2D_E_INVALID_ARG, "invalid argument");
   FEM2D_CUDA(cudaSetDevice(c->c.device));
-  shifted_solve(c->c, g->dom, g->h, g->d, c_a, c_b, spd != 0, nrhs, rhs, x);
+  std::lock_guard<std::mutex> lk(g->plan.mu);
+  shifted_solve(c->c, g->dom, g->h, g->d, g->plan, c_a, c_b, spd != 0, nrhs, rhs, x);
+  API_END
+}
+
+int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, const double* d_x, int64_t ldx,
+                          int nb, double* d_y, int64_t ldy) {
+  API_BEGIN
+  if (!c || !g || !d_x || !d_y) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (nb < 1 || nb > 32 || ldx < nb || ldy < nb) fail(FEM2D_E_INVALID_ARG, "block width must be 1..32 and fit both leading dimensions");
+  if (g->ctx->device != c->c.device) fail(FEM2D_E_INVALID_ARG, "the GEP lives on another device");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  gep_spmm(c->c, g->h, g->d, c_a, c_b, d_x, ldx, nb, d_y, ldy);
   API_END
 }
 
@@ -592,7 +710,8 @@ int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_p
   if (opts) o = *opts;
   fem2d_solve_stats st{};
   try {
-    sparse_solve(c->c, g->dom, g->h, g->d, target, n_pairs, o, values, vectors, residuals, &st);
+    std::lock_guard<std::mutex> lk(g->plan.mu);
+    sparse_solve(c->c, g->dom, g->h, g->d, g->plan, target, n_pairs, o, values, vectors, residuals, &st);
   } catch (...) {
     if (stats) *stats = st;
     throw;

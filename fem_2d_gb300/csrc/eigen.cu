@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <mutex>
 #include <numeric>
 
 #include "eigen.h"
@@ -39,47 +40,58 @@ namespace {
 // ---------------------------------------------------------------- dense block kernels
 // Y = ca*A*X + cb*B*X; X, Y row-major (ldx, ldy), nb <= 32 columns. One warp per row; the warp's
 // lanes split into (32 / G) groups of G >= nb lanes, each group walking a slice of the row's entries.
+// Y = (ca A + cb B) X for nb <= 32 columns, one warp per row. The warp first loads up to 128
+// (col, value) pairs of its row (four coalesced 32-entry chunks, issued back to back), then lane
+// (sub, c) gathers X[col_e][c] for the entries e = sub, sub + 32/G, ... of every chunk (G = columns
+// rounded up to a power of two). All gathers of the 128 entries are independent of each other, so a
+// row costs about two memory round trips instead of two per chunk. Partial sums of the 32/G entry
+// groups are combined with shuffles.
 __global__ void __launch_bounds__(256) spmm_kernel(int64_t n, const int64_t* __restrict__ rp,
                                                    const int32_t* __restrict__ col, const double* __restrict__ va,
                                                    const double* __restrict__ vb, double ca, double cb,
                                                    const double* __restrict__ X, int64_t ldx, int nb, int G,
                                                    double* __restrict__ Y, int64_t ldy) {
+  constexpr int CH = 4;   // chunks of 32 entries staged per pass
   const int lane = threadIdx.x & 31;
   const int groups = 32 / G;
   const int c = lane % G, sub = lane / G;
+  const bool live = c < nb;
   for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
        row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     double acc = 0.0;
     const int64_t k1 = rp[row + 1];
-    const bool live = c < nb;
-    int64_t k = rp[row] + sub;
-    for (; k + 3 * groups < k1; k += 4 * groups) {
-      int cc[4];
-      double v[4], x[4];
+    for (int64_t k0 = rp[row]; k0 < k1; k0 += 32 * CH) {
+      int mc[CH];
+      double mv[CH];
 #pragma unroll
-      for (int q = 0; q < 4; q++) cc[q] = __ldg(col + k + q * groups);
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        v[q] = 0.0;
-        if (ca != 0.0) v[q] += ca * __ldg(va + k + q * groups);
-        if (cb != 0.0) v[q] += cb * __ldg(vb + k + q * groups);
-        x[q] = live ? __ldg(X + (int64_t)cc[q] * ldx + c) : 0.0;
+      for (int q = 0; q < CH; q++) {
+        const int64_t kk = k0 + 32 * q + lane;
+        mc[q] = 0;
+        mv[q] = 0.0;
+        if (kk < k1) {
+          mc[q] = __ldg(col + kk);
+          if (ca != 0.0) mv[q] += ca * __ldg(va + kk);
+          if (cb != 0.0) mv[q] += cb * __ldg(vb + kk);
+        }
       }
+      const int cnt = (int)min((int64_t)(32 * CH), k1 - k0);
 #pragma unroll
-      for (int q = 0; q < 4; q++) acc += v[q] * x[q];
-    }
-    for (; k < k1; k += groups) {
-      double v = 0.0;
-      if (ca != 0.0) v += ca * __ldg(va + k);
-      if (cb != 0.0) v += cb * __ldg(vb + k);
-      if (live) acc += v * __ldg(X + (int64_t)__ldg(col + k) * ldx + c);
+      for (int q = 0; q < CH; q++) {
+        if (32 * q >= cnt) break;   // warp-uniform
+#pragma unroll 8
+        for (int e0 = 0; e0 < 32; e0 += groups) {
+          const int e = e0 + sub;
+          const int cj = __shfl_sync(0xffffffffu, mc[q], e);
+          const double vj = __shfl_sync(0xffffffffu, mv[q], e);
+          if (32 * q + e < cnt && live) acc += vj * __ldg(X + (int64_t)cj * ldx + c);
+        }
+      }
     }
     for (int off = G; off < 32; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if (sub == 0 && c < nb) Y[row * ldy + c] = acc;
+    if (sub == 0 && live) Y[row * ldy + c] = acc;
   }
 }
 
-// partial Gram: P[blk][i*b + j] = sum over the block's rows of X[r][i] * Y[r][j]
 __global__ void __launch_bounds__(256) gram_partial_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a,
                                                            const double* __restrict__ Y, int64_t ldy, int b,
                                                            int64_t rows_per_block, int e0, double* __restrict__ P) {
@@ -155,6 +167,17 @@ __global__ void copy_block_kernel(int64_t n, int b, const double* __restrict__ X
 }
 
 // R = AX - BX * diag(theta) column by column, accumulating column sums of squares of R and of BX
+// Y = alpha X + beta Y on an n x b row-major block
+__global__ void axpby_kernel(int64_t n, int b, double alpha, const double* __restrict__ X, int64_t ldx, double beta,
+                             double* __restrict__ Y, int64_t ldy) {
+  const int64_t total = n * b;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / b;
+    const int j = (int)(t % b);
+    Y[r * ldy + j] = alpha * X[r * ldx + j] + beta * Y[r * ldy + j];
+  }
+}
+
 __global__ void __launch_bounds__(256) resid_partial_kernel(int64_t n, const double* __restrict__ AX,
                                                             const double* __restrict__ BX, int64_t ld, int b,
                                                             const double* __restrict__ theta, int64_t rows_per_block,
@@ -302,6 +325,11 @@ struct Dev {
       c.launches++;   // (pageable copies are staged before cudaMemcpyAsync returns: Ct may be reused)
     }
   }
+  void axpby(double alpha, const double* X, int64_t ldx, int b, double beta, double* Y, int64_t ldy) {
+    const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
+    axpby_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, b, alpha, X, ldx, beta, Y, ldy);
+    c.launches++;
+  }
   void copy(const double* X, int64_t ldx, int b, double* Y, int64_t ldy) {
     const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
     copy_block_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, b, X, ldx, Y, ldy);
@@ -309,12 +337,15 @@ struct Dev {
   }
 };
 
-void setup_gemm_smem() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(gemm_nn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-  cudaFuncSetAttribute(gram_partial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-  done = true;
+// dynamic shared memory limits, once per device (a function attribute lives in the device's context)
+void setup_gemm_smem(int device) {
+  static std::mutex mu;
+  static bool done[256] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  if (device < 0 || device >= 256 || done[device]) return;
+  FEM2D_CUDA(cudaFuncSetAttribute(gemm_nn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  FEM2D_CUDA(cudaFuncSetAttribute(gram_partial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  done[device] = true;
 }
 
 // splitmix64 -> standard normal (Box-Muller), deterministic start blocks
@@ -338,12 +369,40 @@ void random_block(int64_t n, int b, uint64_t seed, std::vector<double>& out) {
 
 }  // namespace
 
+MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h) {
+  if (!p.ready || p.device != c.device) {
+    p.ready = false;
+    p.mf.reset();
+    p.sym.reset(new MFSymbolic);
+    if (p.dense) mf_symbolic_dense(h, *p.sym);
+    else mf_symbolic(dom, h, *p.sym);
+    p.mf.reset(new MFDevice);
+    p.mf->setup(c, *p.sym, 32);
+    p.device = c.device;
+    p.ready = true;
+  }
+  return *p.mf;
+}
+
+MFDevice& mf_plan_dense(MFPlan& p, Ctx& c, const HostGEP& h) {
+  p.ready = false;
+  p.mf.reset();
+  p.sym.reset(new MFSymbolic);
+  mf_symbolic_dense(h, *p.sym);
+  p.mf.reset(new MFDevice);
+  p.mf->setup(c, *p.sym, 32);
+  p.device = c.device;
+  p.dense = true;
+  p.ready = true;
+  return *p.mf;
+}
+
 // ================================================================ sparse shift-invert eigensolver
-void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double sigma, int k,
+void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double sigma, int k,
                   const fem2d_solve_opts& o, double* values, double* vectors, double* residuals,
                   fem2d_solve_stats* st) {
   auto t0 = std::chrono::steady_clock::now();
-  setup_gemm_smem();
+  setup_gemm_smem(c.device);
   const int64_t n = h.n;
   const int guard = std::max(4, k / 2);
   int b = o.block > 0 ? o.block : std::min<int64_t>(k + guard, n);
@@ -377,16 +436,16 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
     if (hb) fail(FEM2D_E_B_NOT_SPD, "B has a non-positive diagonal entry");
   }
-  MFSymbolic sym;
-  mf_symbolic(dom, h, sym);
-  MFDevice mf;
-  mf.setup(c, sym, 32);
+  MFDevice* M = &mf_plan(plan, c, dom, h);
   MFFactor fm, fp;
-  mf.factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
   // A + c B (c > 0) is SPD: factored without pivoting
   const double cshift = 0.05 * std::fabs(sigma);
-  mf.factor(c, sa.p, sb.p, 1.0, cshift, true, fp);
-  if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + c B is not positive definite; B is likely ill-conditioned");
+  auto factor_both = [&]() {
+    M->factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
+    M->factor(c, sa.p, sb.p, 1.0, cshift, true, fp);
+    if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + c B is not positive definite; B is likely ill-conditioned");
+  };
+  factor_both();
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t1 = std::chrono::steady_clock::now();
 
@@ -398,12 +457,73 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   for (DBuf<double>* buf : {&X, &AX, &BX, &G0, &W1, &W2, &W3}) buf->alloc((size_t)n * 32);
   int64_t spmv = 0, napply = 0;
 
+  // x = K^-1 rhs for K = ka A + kb B (factored as fac) followed by nref steps of iterative refinement
+  // in FP64 (r = rhs - K x, x += K^-1 r). The multifrontal LU pivots within each front only, which
+  // loses digits on indefinite pencils with ill-conditioned (monomial) bases; refinement restores
+  // them. R1, R2 are scratch blocks.
+  DBuf<double> R1, R2;
+  R1.alloc((size_t)n * 32);
+  R2.alloc((size_t)n * 32);
+  auto solve_ref = [&](const MFFactor& fac, double ka, double kb, const double* rhs, int64_t lr, double* x, int64_t lx,
+                       int nb, int nref) {
+    M->solve(c, fac, rhs, lr, x, lx, nb);
+    for (int r = 0; r < nref; r++) {
+      D.spmm(ka, kb, x, lx, nb, R1.p, 32);
+      D.axpby(1.0, rhs, lr, nb, -1.0, R1.p, 32);
+      M->solve(c, fac, R1.p, 32, R2.p, 32, nb);
+      D.axpby(1.0, R2.p, 32, nb, 1.0, x, lx);
+      spmv += nb;
+    }
+  };
+  // refinement steps needed by each factorization: measured once on a fixed random block, up to 3
+  // steps, while the relative residual max_j ||rhs_j - K x_j|| / ||rhs_j|| stays above 1e-12
+  auto calibrate = [&](const MFFactor& fac, double ka, double kb, double& rel_out) -> int {
+    const int nb = 4;
+    std::vector<double> R0;
+    random_block(n, nb, 777, R0);
+    DBuf<double> Rb, Xb, Tb;
+    Rb.alloc((size_t)n * nb);
+    Xb.alloc((size_t)n * nb);
+    Tb.alloc((size_t)n * nb);
+    FEM2D_CUDA(cudaMemcpyAsync(Rb.p, R0.data(), R0.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    std::vector<double> G;
+    D.gram(Rb.p, nb, nb, Rb.p, nb, nb, G);
+    std::vector<double> bn(nb);
+    for (int j = 0; j < nb; j++) bn[j] = std::sqrt(G[(size_t)j * nb + j]);
+    double prev = 1e300;
+    for (int nref = 0; nref <= 3; nref++) {
+      solve_ref(fac, ka, kb, Rb.p, nb, Xb.p, nb, nb, nref);
+      D.spmm(ka, kb, Xb.p, nb, nb, Tb.p, nb);
+      D.axpby(1.0, Rb.p, nb, nb, -1.0, Tb.p, nb);
+      D.gram(Tb.p, nb, nb, Tb.p, nb, nb, G);
+      double rel = 0;
+      for (int j = 0; j < nb; j++) rel = std::max(rel, std::sqrt(G[(size_t)j * nb + j]) / bn[j]);
+      rel_out = std::min(rel, prev);
+      if (rel < 1e-12) return nref;                      // accurate enough
+      if (rel > 0.5 * prev) return std::max(0, nref - 1);  // no longer improving
+      prev = rel;
+    }
+    return 3;
+  };
+  double rel_p = 0, rel_m = 0;
+  int nref_p = calibrate(fp, 1.0, cshift, rel_p);
+  int nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+  // small GEPs whose sparse factorization stays inaccurate after refinement (pivoting restricted to
+  // each front's fully-summed rows can grow badly on indefinite pencils of ill-conditioned bases)
+  // switch to one dense front with partial pivoting over all rows; the choice is kept in the plan
+  constexpr int64_t kDenseMax = 4096;
+  if ((rel_p > 1e-10 || rel_m > 1e-10) && !plan.dense && n <= kDenseMax) {
+    M = &mf_plan_dense(plan, c, h);
+    factor_both();
+    nref_p = calibrate(fp, 1.0, cshift, rel_p);
+    nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+  }
   // Out (ld lo) = T In (ld li), nb columns; In and Out may not alias W1..W3
   auto apply_T = [&](const double* In, int64_t li, double* Out, int64_t lo, int nb) {
     D.spmm(0.0, 1.0, In, li, nb, W1.p, 32);
-    mf.solve(c, fp, W1.p, 32, W2.p, 32, nb);
+    solve_ref(fp, 1.0, cshift, W1.p, 32, W2.p, 32, nb, nref_p);
     D.spmm(1.0, 0.0, W2.p, 32, nb, W3.p, 32);
-    mf.solve(c, fm, W3.p, 32, Out, lo, nb);
+    solve_ref(fm, 1.0, -sigma, W3.p, 32, Out, lo, nb, nref_m);
     spmv += 2 * nb;
     napply += nb;
   };
@@ -468,11 +588,17 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   std::vector<double> theta_sel, rel_sel;
   int cycles = 0, bx = b;
   bool converged = false;
+  // stagnation guard: when the worst wanted residual has not halved for two cycles, the next cycle
+  // rebuilds the whole block Krylov space from all selected Ritz vectors (every column expanded)
+  // instead of expanding the unconverged ones only
+  double best_worst = 1e300;
+  int stall = 0;
+  bool full = true;
   for (; cycles < max_cycles; cycles++) {
     int m, last0 = 0, lastn;
-    if (cycles == 0) {
-      D.copy(X.p, 32, b, V.p, mmax);
-      m = borth_new(0, b);
+    if (full) {
+      D.copy(X.p, 32, bx, V.p, mmax);
+      m = borth_new(0, bx);
       lastn = m;
     } else {
       // restart from the B-orthonormal Ritz vectors (and their exact products), expand the unconverged
@@ -499,7 +625,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       lastn = r;
       m += r;
     }
-    for (int st2 = (cycles == 0 ? 0 : 1); st2 < steps && lastn > 0 && m + lastn <= mmax; st2++) {
+    for (int st2 = (full ? 0 : 1); st2 < steps && lastn > 0 && m + lastn <= mmax; st2++) {
       apply_T(V.p + last0, mmax, V.p + m, mmax, lastn);
       int r = borth_new(m, lastn);
       if (r == 0) break;
@@ -609,6 +735,14 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       cycles++;
       break;
     }
+    if (worst < 0.5 * best_worst) {
+      best_worst = worst;
+      stall = 0;
+    } else {
+      stall++;
+    }
+    full = stall >= 2;
+    if (full) stall = 0;
   }
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t2 = std::chrono::steady_clock::now();
@@ -622,6 +756,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     for (int q = 0; q < k; q++) w = std::max(w, rel_sel[q]);
     st->max_rel_residual = w;
     st->spmv_count = spmv;
+    st->refine_spd = nref_p;
+    st->refine_indefinite = nref_m;
   }
   // back to the original pencil: x = D x~ (B-orthonormal), residuals in the original norms
   {
@@ -676,14 +812,11 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
 }
 
 // ================================================================ dense solve (nalgebra_solve_gep)
-void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double target, double* value,
-                 double* vector) {
+void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double target,
+                 double* value, double* vector) {
   const int64_t n = h.n;
   if (n > 1000) fail(FEM2D_E_TOO_LARGE, "Matrices Exceeded Maximum Size (1000x1000); Cannot Solve!");
-  MFSymbolic sym;
-  mf_symbolic(dom, h, sym);
-  MFDevice mf;
-  mf.setup(c, sym, 32);
+  MFDevice& mf = mf_plan(plan, c, dom, h);
   MFFactor fb;
   mf.factor(c, d.a.p, d.b.p, 0.0, 1.0, true, fb);
   if (fb.flags & 2) fail(FEM2D_E_B_NOT_SPD, "Failed to invert B-matrix (via cholesky); likely ill-conditioned!");
@@ -729,30 +862,67 @@ void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d
 
 namespace fem2d {
 
-void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double ca, double cb, bool spd,
-                   int nrhs, const double* rhs, double* x) {
+void gep_spmm(Ctx& c, const HostGEP& h, const DeviceGEP& d, double ca, double cb, const double* X, int64_t ldx, int nb,
+              double* Y, int64_t ldy) {
+  Dev D{c, h, d, d.a.p, d.b.p};
+  D.spmm(ca, cb, X, ldx, nb, Y, ldy);
+  FEM2D_CUDA(cudaGetLastError());
+}
+
+void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double ca,
+                   double cb, bool spd, int nrhs, const double* rhs, double* x) {
   const int64_t n = h.n;
-  MFSymbolic sym;
-  mf_symbolic(dom, h, sym);
-  MFDevice mf;
-  mf.setup(c, sym, 32);
-  MFFactor fac;
-  mf.factor(c, d.a.p, d.b.p, ca, cb, spd, fac);
-  if (spd && (fac.flags & 2)) fail(FEM2D_E_B_NOT_SPD, "the shifted matrix is not positive definite");
-  DBuf<double> R, X;
+  Dev D{c, h, d, d.a.p, d.b.p};
+  DBuf<double> R, X, T, U;
   R.alloc((size_t)n * 32);
   X.alloc((size_t)n * 32);
-  std::vector<double> hr((size_t)n * 32), hx((size_t)n * 32);
-  for (int c0 = 0; c0 < nrhs; c0 += 32) {
-    const int w = std::min(32, nrhs - c0);
-    for (int64_t i = 0; i < n; i++)
-      for (int k = 0; k < w; k++) hr[(size_t)i * 32 + k] = rhs[(size_t)i * nrhs + c0 + k];
-    FEM2D_CUDA(cudaMemcpyAsync(R.p, hr.data(), hr.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    mf.solve(c, fac, R.p, 32, X.p, 32, w);
-    FEM2D_CUDA(cudaMemcpyAsync(hx.data(), X.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-    for (int64_t i = 0; i < n; i++)
-      for (int k = 0; k < w; k++) x[(size_t)i * nrhs + c0 + k] = hx[(size_t)i * 32 + k];
+  T.alloc((size_t)n * 32);
+  U.alloc((size_t)n * 32);
+  std::vector<double> hr((size_t)n * 32), hx((size_t)n * 32), G;
+  // max over the columns of ||R - K X|| / ||R||, K = ca A + cb B
+  auto relres = [&](int w) {
+    D.spmm(ca, cb, X.p, 32, w, T.p, 32);
+    D.axpby(1.0, R.p, 32, w, -1.0, T.p, 32);
+    D.gram(T.p, 32, w, T.p, 32, w, G);
+    std::vector<double> tg = G;
+    D.gram(R.p, 32, w, R.p, 32, w, G);
+    double rel = 0;
+    for (int j = 0; j < w; j++)
+      rel = std::max(rel, std::sqrt(tg[(size_t)j * w + j] / std::max(G[(size_t)j * w + j], 1e-300)));
+    return rel;
+  };
+  for (int attempt = 0; attempt < 2; attempt++) {
+    MFDevice& mf = attempt == 0 ? mf_plan(plan, c, dom, h) : mf_plan_dense(plan, c, h);
+    MFFactor fac;
+    mf.factor(c, d.a.p, d.b.p, ca, cb, spd, fac);
+    if (spd && (fac.flags & 2)) fail(FEM2D_E_B_NOT_SPD, "the shifted matrix is not positive definite");
+    double worst = 0;
+    for (int c0 = 0; c0 < nrhs; c0 += 32) {
+      const int w = std::min(32, nrhs - c0);
+      for (int64_t i = 0; i < n; i++)
+        for (int k = 0; k < 32; k++) hr[(size_t)i * 32 + k] = k < w ? rhs[(size_t)i * nrhs + c0 + k] : 0.0;
+      FEM2D_CUDA(cudaMemcpyAsync(R.p, hr.data(), hr.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+      mf.solve(c, fac, R.p, 32, X.p, 32, w);
+      // iterative refinement in FP64 while it keeps improving (up to 3 steps)
+      double rel = relres(w);
+      for (int it = 0; it < 3 && rel > 1e-13; it++) {
+        mf.solve(c, fac, T.p, 32, U.p, 32, w);
+        D.axpby(1.0, U.p, 32, w, 1.0, X.p, 32);
+        const double r2 = relres(w);
+        if (r2 > 0.5 * rel) {   // no longer improving: undo the step
+          D.axpby(-1.0, U.p, 32, w, 1.0, X.p, 32);
+          break;
+        }
+        rel = r2;
+      }
+      worst = std::max(worst, rel);
+      FEM2D_CUDA(cudaMemcpyAsync(hx.data(), X.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+      for (int64_t i = 0; i < n; i++)
+        for (int k = 0; k < w; k++) x[(size_t)i * nrhs + c0 + k] = hx[(size_t)i * 32 + k];
+    }
+    // small systems the sparse plan cannot solve accurately are redone with one dense front
+    if (worst <= 1e-10 || plan.dense || n > 4096) break;
   }
 }
 

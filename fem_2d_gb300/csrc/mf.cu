@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <array>
 #include <cstring>
+#include <mutex>
 
 namespace cg = cooperative_groups;
 
@@ -397,6 +398,142 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
   }
 }
 
+
+// ------------------------------------------------------------------ small-front solves
+// Fronts with p <= kSmallP and f <= kSmallF (every front of an Elem-level elimination tree at the
+// orders this library meets in practice) are solved by one CTA each, with no sequential triangular
+// substitution: after the factorization, mf_invdiag_kernel overwrites each such front's p x p
+// diagonal LU square by (unit lower L11^-1, upper U11^-1), so both solve directions become dense,
+// fully parallel products:
+//   forward:  y = L11^-1 P b_p,  b_s -= L21 y          (b_s goes to the parent)
+//   backward: x_p = U11^-1 (y - U12 x_s)
+constexpr int kSmallP = 160;
+constexpr int kSmallF = 512;
+
+// column j of L11^-1 and of U11^-1 per thread, from a shared-memory copy of the LU square
+__global__ void __launch_bounds__(256) mf_invdiag_kernel(const int32_t* __restrict__ lf,
+                                                         const FrontDesc* __restrict__ fd, double* __restrict__ F) {
+  const FrontDesc d = fd[lf[blockIdx.x]];
+  const int f = d.f, p = d.p;
+  extern __shared__ double S[];   // S[k * p + i] = LU(i, k)
+  double* A = F + d.off;
+  for (int t = threadIdx.x; t < p * p; t += blockDim.x) {
+    const int i = t % p, k = t / p;
+    S[t] = A[(int64_t)k * f + i];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < p; j += blockDim.x) {
+    double* out = A + (int64_t)j * f;   // column j; only this thread writes it
+    // L11 x = e_j (unit diagonal): x_j = 1, x_i = -sum_{k=j}^{i-1} L(i,k) x_k
+    for (int i = j + 1; i < p; i++) {
+      double acc = -S[j * p + i];
+      for (int k = j + 1; k < i; k++) acc -= S[k * p + i] * out[k];
+      out[i] = acc;
+    }
+    // U11 y = e_j: y_j = 1 / U(j,j), y_i = -(sum_{k=i+1}^{j} U(i,k) y_k) / U(i,i)
+    out[j] = 1.0 / S[j * p + j];
+    for (int i = j - 1; i >= 0; i--) {
+      double acc = 0.0;
+      for (int k = i + 1; k <= j; k++) acc += S[k * p + i] * out[k];
+      out[i] = -acc / S[i * p + i];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) mf_forward_small_kernel(
+    const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd, const int32_t* __restrict__ dofs,
+    const int32_t* __restrict__ emap, const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
+    const int64_t* __restrict__ piv_off, const int64_t* __restrict__ woff, const double* __restrict__ F,
+    const double* __restrict__ B, int64_t ldb, int nb, double* __restrict__ W) {
+  const int fr = lf[blockIdx.x];
+  const FrontDesc d = fd[fr];
+  const int f = d.f, p = d.p;
+  extern __shared__ double sm[];
+  double* v = sm;            // v[c * f + i]
+  double* y = sm + f * nb;   // y[c * p + i]
+  const int32_t* D = dofs + d.dptr;
+  const int32_t* pm = perm + piv_off[fr];
+  const int32_t* ipm = iperm + piv_off[fr];
+  const double* A = F + d.off;
+  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) {
+    const int i = t % f, c = t / f;
+    v[t] = i < p ? B[(int64_t)D[pm[i]] * ldb + c] : 0.0;
+  }
+  __syncthreads();
+  for (int slot = 0; slot < MAXKIDS; slot++) {
+    const int ch = d.kid[slot];
+    if (ch < 0) continue;
+    const FrontDesc cd = fd[ch];
+    const int sz = cd.f - cd.p;
+    const double* cw = W + woff[ch];
+    const int32_t* m = emap + cd.eptr;
+    for (int t = threadIdx.x; t < sz * nb; t += blockDim.x) {
+      const int i = t % sz, c = t / sz;
+      const int row = m[i] < p ? ipm[m[i]] : m[i];   // pivot rows are stored permuted
+      v[c * f + row] += cw[(int64_t)c * cd.f + cd.p + i];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    const double* vc = v + c * f;
+    double acc = vc[i];
+    for (int k = 0; k < i; k++) acc += A[(int64_t)k * f + i] * vc[k];
+    y[c * p + i] = acc;
+  }
+  __syncthreads();
+  double* out = W + woff[fr];
+  const int s = f - p;
+  for (int t = threadIdx.x; t < s * nb; t += blockDim.x) {
+    const int i = p + t % s, c = t / s;
+    const double* yc = y + c * p;
+    double acc = v[c * f + i];
+    for (int k = 0; k < p; k++) acc -= A[(int64_t)k * f + i] * yc[k];
+    out[(int64_t)c * f + i] = acc;
+  }
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    out[(int64_t)c * f + i] = y[c * p + i];
+  }
+}
+
+__global__ void __launch_bounds__(256) mf_backward_small_kernel(
+    const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd, const int32_t* __restrict__ dofs,
+    const int64_t* __restrict__ woff, const double* __restrict__ F, const double* __restrict__ W, int nb,
+    double* __restrict__ X, int64_t ldx) {
+  const int fr = lf[blockIdx.x];
+  const FrontDesc d = fd[fr];
+  const int f = d.f, p = d.p;
+  if (p == 0) return;
+  const int s = f - p;
+  extern __shared__ double sm[];
+  double* xs = sm;            // xs[c * s + j]: solved struct unknowns
+  double* z = sm + s * nb;    // z[c * p + i]
+  const int32_t* D = dofs + d.dptr;
+  const double* A = F + d.off;
+  const double* v = W + woff[fr];
+  for (int t = threadIdx.x; t < s * nb; t += blockDim.x) {
+    const int j = t % s, c = t / s;
+    xs[t] = X[(int64_t)D[p + j] * ldx + c];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    const double* xc = xs + c * s;
+    double acc = v[(int64_t)c * f + i];
+    for (int j = 0; j < s; j++) acc -= A[(int64_t)(p + j) * f + i] * xc[j];
+    z[c * p + i] = acc;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    const double* zc = z + c * p;
+    double acc = 0.0;
+    for (int k = i; k < p; k++) acc += A[(int64_t)k * f + i] * zc[k];
+    X[(int64_t)D[i] * ldx + c] = acc;
+  }
+}
+
 }  // namespace
 
 void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
@@ -471,6 +608,45 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
       level_max_p[l] = std::max(level_max_p[l], s.p[s.level_fronts[k]]);
       level_factor_bytes[l] += 8.0 * (0.5 * P * P + P * (F - P));
     }
+  std::vector<int32_t> ls, ll;
+  small_ptr.assign(nlevels + 1, 0);
+  large_ptr.assign(nlevels + 1, 0);
+  level_small_f.assign(nlevels, 0);
+  level_small_p.assign(nlevels, 0);
+  max_small_p = 0;
+  for (int l = 0; l < nlevels; l++) {
+    small_ptr[l] = (int32_t)ls.size();
+    large_ptr[l] = (int32_t)ll.size();
+    for (int k = s.level_ptr[l]; k < s.level_ptr[l + 1]; k++) {
+      const int fr = s.level_fronts[k];
+      if (s.p[fr] <= kSmallP && s.f[fr] <= kSmallF) {
+        ls.push_back(fr);
+        level_small_f[l] = std::max(level_small_f[l], s.f[fr]);
+        level_small_p[l] = std::max(level_small_p[l], s.p[fr]);
+        max_small_p = std::max(max_small_p, s.p[fr]);
+      } else {
+        ll.push_back(fr);
+      }
+    }
+  }
+  small_ptr[nlevels] = (int32_t)ls.size();
+  large_ptr[nlevels] = (int32_t)ll.size();
+  nsmall = (int)ls.size();
+  lsmall.upload(ls, st);
+  llarge.upload(ll, st);
+  // dynamic shared memory limits are set once per device (a function attribute of the device's context)
+  static std::mutex attr_mu;
+  static bool attr_done[256] = {};
+  std::lock_guard<std::mutex> lk(attr_mu);
+  if (c.device >= 0 && c.device < 256 && !attr_done[c.device]) {
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_invdiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kSmallP * kSmallP * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kSmallF * 32 * (int)sizeof(double)));
+    attr_done[c.device] = true;
+  }
 }
 
 void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, double cb, bool cholesky,
@@ -512,6 +688,11 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
   if (out.iperm.n != out.piv.n) out.iperm.alloc(out.piv.n);
   mf_perm_kernel<<<(nf + 127) / 128, 128, 0, st>>>(nf, fd, out.piv.p, piv_off.p, out.perm.p, out.iperm.p);
   c.launches++;
+  if (nsmall > 0) {
+    mf_invdiag_kernel<<<nsmall, 256, (size_t)max_small_p * max_small_p * sizeof(double), st>>>(lsmall.p, fd,
+                                                                                              Fbuf.p);
+    c.launches++;
+  }
   FEM2D_CUDA(cudaGetLastError());
   out.flags = read_flags(c);
 }
@@ -522,19 +703,35 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
   if (nb > nb_cap) fail(FEM2D_E_INVALID_ARG, "solve block wider than the workspace");
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
   for (int l = 0; l < nlevels; l++) {
-    const int nfl = level_ptr[l + 1] - level_ptr[l];
     ProfScope ps(c, "mf_forward", level_factor_bytes[l]);
-    mf_forward_cluster_kernel<<<nfl * CL, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, ea_map.p, fac.perm.p,
-                                                        fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, nb,
-                                                        work.p);
-    c.launches++;
+    const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
+    if (ns > 0) {
+      const size_t smem = (size_t)(level_small_f[l] + level_small_p[l]) * nb * sizeof(double);
+      mf_forward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], fd, dofs.p, ea_map.p, fac.perm.p,
+                                                     fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, nb, work.p);
+      c.launches++;
+    }
+    if (nl > 0) {
+      mf_forward_cluster_kernel<<<nl * CL, 256, 0, st>>>(llarge.p + large_ptr[l], fd, dofs.p, ea_map.p, fac.perm.p,
+                                                         fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, nb,
+                                                         work.p);
+      c.launches++;
+    }
   }
   for (int l = nlevels - 1; l >= 0; l--) {
-    const int nfl = level_ptr[l + 1] - level_ptr[l];
     ProfScope ps(c, "mf_backward", level_factor_bytes[l]);
-    mf_backward_cluster_kernel<<<nfl * CL, 256, 0, st>>>(lfronts.p + level_ptr[l], fd, dofs.p, woff.p, Fbuf.p,
-                                                         work.p, nb, X, ldx);
-    c.launches++;
+    const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
+    if (ns > 0) {
+      const size_t smem = (size_t)level_small_f[l] * nb * sizeof(double);
+      mf_backward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], fd, dofs.p, woff.p, Fbuf.p,
+                                                      work.p, nb, X, ldx);
+      c.launches++;
+    }
+    if (nl > 0) {
+      mf_backward_cluster_kernel<<<nl * CL, 256, 0, st>>>(llarge.p + large_ptr[l], fd, dofs.p, woff.p, Fbuf.p,
+                                                          work.p, nb, X, ldx);
+      c.launches++;
+    }
   }
   FEM2D_CUDA(cudaGetLastError());
 }

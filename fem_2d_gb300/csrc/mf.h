@@ -43,5 +43,7 @@ struct MFSymbolic {
 };
 
 void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s);
+// one dense front with every DoF (full partial pivoting)
+void mf_symbolic_dense(const HostGEP& g, MFSymbolic& s);
 
 }  // namespace fem2d

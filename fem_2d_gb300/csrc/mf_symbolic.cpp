@@ -201,4 +201,38 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
   for (int f = 0; f < NF; f++) s.level_fronts[cur[s.level[f]]++] = f;
 }
 
+// One dense front holding every DoF: LU with partial pivoting over all rows (no restriction to a
+// front's fully-summed rows). Used for small GEPs whose sparse factorization loses too many digits.
+void mf_symbolic_dense(const HostGEP& g, MFSymbolic& s) {
+  const int64_t n = g.n;
+  s = MFSymbolic();
+  s.n = n;
+  if (n == 0) return;
+  if (n > 46340) fail(FEM2D_E_TOO_LARGE, "dense factorization plan above 46340 DoFs");
+  s.nfronts = 1;
+  s.parent = {-1};
+  s.level = {0};
+  s.f = {(int32_t)n};
+  s.p = {(int32_t)n};
+  s.dof_ptr = {0, n};
+  s.dofs.resize(n);
+  for (int64_t i = 0; i < n; i++) s.dofs[i] = (int32_t)i;
+  s.mat_off = {0, n * n};
+  s.mat_total = n * n;
+  s.asm_ptr = {0, (int64_t)g.col.size()};
+  s.asm_pos.resize(g.col.size());
+  s.asm_csr.resize(g.col.size());
+  for (int64_t x = 0; x < n; x++)
+    for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) {
+      s.asm_pos[k] = x * n + g.col[k];
+      s.asm_csr[k] = k;
+    }
+  s.ea_ptr = {0, 0};
+  s.nlevels = 1;
+  s.level_ptr = {0, 1};
+  s.level_fronts = {0};
+  s.max_f = s.max_p = (int)n;
+  s.flops = 2.0 * (double)n * n * n / 3.0;
+}
+
 }  // namespace fem2d

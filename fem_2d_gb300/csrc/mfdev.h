@@ -1,6 +1,8 @@
 // Device side of the multifrontal factorization (mf.cu).
 #pragma once
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 #include "device.h"
@@ -29,6 +31,11 @@ struct MFDevice {
   DBuf<int64_t> asm_pos, asm_csr, piv_off, woff;
   DBuf<double> work;
   DBuf<int> flags;
+  // per level, the fronts solved by one CTA each (inverted diagonal blocks) and the rest (clusters)
+  std::vector<int32_t> small_ptr, large_ptr;   // nlevels + 1 offsets into lsmall / llarge
+  std::vector<int32_t> level_small_f, level_small_p;
+  DBuf<int32_t> lsmall, llarge;
+  int nsmall = 0, max_small_p = 0;
 
   void setup(Ctx& c, const MFSymbolic& s, int nb_max);
   // factor c_a*A + c_b*B (values in full-CSR order); Cholesky mode skips pivoting (SPD shifts)
@@ -37,5 +44,23 @@ struct MFDevice {
   void solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, double* X, int64_t ldx, int nb);
   int read_flags(Ctx& c);
 };
+
+// The factorization plan of one GEP: the host symbolic phase and its device copy depend on the
+// sparsity pattern only, so they are built on the first solve of a GEP and reused by later solves of
+// the same GEP (numeric factorizations are always recomputed). mu serialises solves that share the
+// plan's solve workspace.
+struct MFPlan {
+  std::unique_ptr<MFSymbolic> sym;
+  std::unique_ptr<MFDevice> mf;
+  bool ready = false;
+  bool dense = false;   // a single dense front (chosen when the sparse plan's solves are inaccurate)
+  int device = -1;
+  std::mutex mu;
+};
+
+// the plan's MFDevice, building the plan on first use (or after a device change)
+MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h);
+// replace the plan by the dense single-front plan
+MFDevice& mf_plan_dense(MFPlan& p, Ctx& c, const HostGEP& h);
 
 }  // namespace fem2d

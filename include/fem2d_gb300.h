@@ -150,6 +150,28 @@ int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g);
  * on the context's stream; synchronise before reading d_a and d_b. No cudaMalloc, cudaFree or other
  * allocating call is made. */
 int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, double* d_b);
+/* galerkin_sample_gep_hcurl over many Domains at once (galerkin.rs:33-187 per Domain; the reference
+ * has no batched form: a caller loops over Domains). Each Domain gets its own host symbolic phase and
+ * its own GEP (out[i], freed with fem2d_gep_free); the device numeric phase of ALL of them is two
+ * launches: the 1-D contraction tables of every Domain in one, then one persistent launch over the
+ * concatenated CSR entries of every GEP (uneven expansion orders share the launch). autotune != 0
+ * picks the value kernel's launch shape by timing a fixed candidate list on the first batch of a
+ * size class and caches it per process (fem2d_autotune_export/import). Errors as
+ * fem2d_galerkin_sample_gep_hcurl, checked for every Domain before any work. report (optional,
+ * 6 doubles): device ms of the table launch, device ms of the value launch, threads per CTA, CTAs
+ * per SM, total CSR entries, total visit codes. */
+int fem2d_galerkin_sample_gep_hcurl_batch(fem2d_ctx* c, const fem2d_domain* const* domains, int64_t count, int basis,
+                                          int nq_u, int nq_v, int autotune, fem2d_gep** out, double* report);
+/* Numeric phase only, for GEPs already built (by either entry point) on this device: the same two
+ * batched launches over all of them. report as above. */
+int fem2d_gep_batch_recompute(fem2d_ctx* c, fem2d_gep* const* geps, int64_t count, int autotune, double* report);
+/* The autotuner's cache as text, one "key threads ctas_per_sm" line per entry (key = device name,
+ * table stride and size class). export: length (without the NUL) is returned in *length; buf may be
+ * NULL to query it. import: adds/overwrites entries; shapes outside the candidate list are
+ * FEM2D_E_INVALID_ARG. */
+int fem2d_autotune_export(char* buf, int64_t capacity, int64_t* length);
+int fem2d_autotune_import(const char* text, int64_t* entries);
+int fem2d_autotune_clear(void);
 void fem2d_gep_free(fem2d_gep* g);
 /* dims: ndofs, upper-triangle entry count (SparseMatrix::entries), full symmetric nnz
  * (SparseMatrix::num_entries, sparse_matrix.rs:32-35) */
@@ -177,6 +199,12 @@ int fem2d_dense_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, doubl
 int fem2d_gep_shifted_solve(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, int spd, int nrhs,
                             const double* rhs, double* x);
 
+/* Y = c_a A X + c_b B X with the GEP's device-resident A and B: the operator products an external
+ * eigensolver applies to the GEP (MatMult in the PETSc hand-off of slepc_solve.rs:14-68). d_x and
+ * d_y are device pointers to row-major n x nb blocks (leading dimensions ldx, ldy), 1 <= nb <= 32,
+ * d_x and d_y must not overlap. Queued on the context's stream; returns without synchronising. */
+int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, const double* d_x, int64_t ldx,
+                          int nb, double* d_y, int64_t ldy);
 typedef struct fem2d_solve_opts {
   int precond;          /* FEM2D_PRECOND_* */
   int max_outer;        /* outer (eigen) iterations, 0 = default */
@@ -194,6 +222,7 @@ typedef struct fem2d_solve_stats {
   double t_setup_ms, t_solve_ms;
   double max_rel_residual;
   int64_t spmv_count;
+  int refine_spd, refine_indefinite;   /* iterative-refinement steps per solve with A + cB and A - sigma B */
 } fem2d_solve_stats;
 
 /* gpu_solve_gep: the n_pairs eigenpairs of (A, B) nearest target, by a shift-invert block
