@@ -48,7 +48,8 @@ class _fem2d_solve_stats(ctypes.Structure):
     _fields_ = [("outer_iters", ctypes.c_int), ("inner_iters_total", ctypes.c_int), ("converged", ctypes.c_int),
                 ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
                 ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64),
-                ("refine_spd", ctypes.c_int), ("refine_indefinite", ctypes.c_int)]
+                ("refine_spd", ctypes.c_int), ("refine_indefinite", ctypes.c_int), ("dense_plan", ctypes.c_int),
+                ("floor_reached", ctypes.c_int)]
 
 
 def lib():
@@ -100,6 +101,22 @@ def lib():
         "fem2d_autotune_export": (ctypes.c_int, [ctypes.c_char_p, i64, i64p]),
         "fem2d_autotune_import": (ctypes.c_int, [ctypes.c_char_p, i64p]),
         "fem2d_autotune_clear": (ctypes.c_int, []),
+        "fem2d_patchnet_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, PP]),
+        "fem2d_patchnet_free": (None, [P]),
+        "fem2d_patchnet_num_params": (i64, [P]),
+        "fem2d_patchnet_get_params": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float)]),
+        "fem2d_patchnet_set_params": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float)]),
+        "fem2d_patchnet_features": (ctypes.c_int, [P, d, i64p, i64p, i32p, ctypes.POINTER(ctypes.c_float),
+                                                   ctypes.POINTER(ctypes.c_float)]),
+        "fem2d_patchnet_loss_grad": (ctypes.c_int, [P, P, P, d, dp, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_float)]),
+        "fem2d_patchnet_train": (ctypes.c_int, [P, P, PP, ctypes.c_int, d, ctypes.POINTER(dp), ctypes.c_int,
+                                                ctypes.c_int, d, dp]),
+        "fem2d_pcg_create": (ctypes.c_int, [P, P, d, d, P, PP]),
+        "fem2d_pcg_solve": (ctypes.c_int, [P, ctypes.c_int, dp, dp, d, ctypes.c_int, dp]),
+        "fem2d_pcg_harvest": (ctypes.c_int, [P, ctypes.c_int, dp, dp, d, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]),
+        "fem2d_pcg_create_with_basis": (ctypes.c_int, [P, P, d, d, ctypes.c_int, ctypes.POINTER(ctypes.c_float), PP]),
+        "fem2d_pcg_free": (None, [P]),
         "fem2d_gep_free": (None, [P]),
         "fem2d_gep_dims": (ctypes.c_int, [P, i64p, i64p, i64p]),
         "fem2d_gep_export_upper": (ctypes.c_int, [P, i32p, i32p, dp, dp]),
@@ -743,3 +760,4 @@ def gpu_solve_gep(gep, target_eigenvalue, **kw):
 
 
 from .fields import UniformFieldError, UniformFieldSpace  # noqa: E402
+from .learned import PCG, PatchNet, harvest_errors, patch_features  # noqa: E402

@@ -173,6 +173,21 @@ def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8, bas
     return Workload(name, mj, ops, basis=basis, glq=(10, 10), target=10.0, n_pairs=20, seed=seed)
 
 
+def learned_family(seed=0, nx=32, ny=16, orders=(5, 7), rounds=2, fraction=1.0):
+    """The learned-preconditioner family: [0,2]x[0,1], nx x ny Elems, orders (5,7), `rounds` seeded rounds of
+    anisotropic (U/V) refinement of `fraction` of the leaves (two rounds from a uniform grid keep Elems that
+    share an edge within two levels); KOLeg, GLQ [10,10], 10 pairs nearest 10.0. Full size 32x16."""
+    from . import Mesh
+
+    mj = grid_mesh_json(nx, ny, 0.0, 2.0, 0.0, 1.0)
+    ops = [("orders", orders[0], orders[1], None)]
+    m = Mesh.from_json(mj)
+    apply_ops(m, ops)
+    _random_rounds(m, ops, SplitMix64(7919 * (seed + 1)), rounds, fraction, [1, 2])
+    return Workload("learned_%dx%d_p%d-%d_seed%d" % (nx, ny, orders[0], orders[1], seed), mj, ops, basis=1,
+                    glq=(10, 10), target=10.0, n_pairs=10, seed=seed)
+
+
 def batch_member(seed):
     """One mesh of the batching family: a ~ U[1,3], (gx, gy) with gx*gy in [4,64] on [0,a]x[0,1],
     per-Elem orders (pu, pv) ~ U{2..8}^2, 0-2 random refinement rounds; GLQ [10,10], 4 pairs nearest 10."""

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -67,7 +68,29 @@ void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
   d.tables.alloc((size_t)2 * d.nivl * 5 * P * P);
   d.a.alloc(g.nnz_full);
   d.b.alloc(g.nnz_full);
-  d.h2d_bytes = (int64_t)(g.row_ptr.size() * 8 + g.col.size() * 4 + g.cptr.size() * 8 + g.codes.size() * 8 +
+  // rows of one Elem's interior functions share their column list; the operator products stage each
+  // run's gathered X rows once (eigen.cu spmm_group_kernel)
+  std::vector<int32_t> grp{0};
+  for (int64_t i = 1; i <= g.n; i++) {
+    const int64_t h = grp.back();
+    bool brk = i == g.n || i - h >= 64;
+    if (!brk) {
+      const int64_t li = g.row_ptr[i + 1] - g.row_ptr[i], lh = g.row_ptr[h + 1] - g.row_ptr[h];
+      brk = li != lh || std::memcmp(g.col.data() + g.row_ptr[i], g.col.data() + g.row_ptr[h], li * sizeof(int32_t)) != 0;
+    }
+    if (brk) grp.push_back((int32_t)i);
+  }
+  if (g.n == 0) grp.assign(1, 0);
+  std::vector<int2> work;
+  for (size_t q = 0; q + 1 < grp.size(); q++) {
+    const int64_t len = g.row_ptr[grp[q] + 1] - g.row_ptr[grp[q]];
+    for (int64_t c0 = 0; c0 < std::max<int64_t>(len, 1); c0 += 256) work.push_back(make_int2((int)q, (int)c0));
+  }
+  d.grp.upload(grp, s);
+  d.gwork.upload(work, s);
+  d.ngrp = (int)grp.size() - 1;
+  d.nwork = (int)work.size();
+  d.h2d_bytes = (int64_t)(grp.size() * 4 + work.size() * 8 + g.row_ptr.size() * 8 + g.col.size() * 4 + g.cptr.size() * 8 + g.codes.size() * 8 +
                           g.blocks.size() * sizeof(GBlock) + g.specs.size() * 4 + iv.size() * 8 + q.size() * 8);
 }
 

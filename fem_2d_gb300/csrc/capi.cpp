@@ -17,6 +17,7 @@
 #include "batch.h"
 #include "mf.h"
 #include "petsc_io.h"
+#include "precond.h"
 
 namespace fem2d {
 static thread_local std::string g_last_error;
@@ -30,11 +31,18 @@ struct fem2d_mesh { Mesh m; };
 struct fem2d_domain { Domain d; };
 struct fem2d_ctx { Ctx c; };
 struct fem2d_fields { FieldSpace f; };
+struct fem2d_patchnet { PatchNet net; };
+struct fem2d_pcg {
+  std::unique_ptr<PCGSolver> s;
+  int64_t n = 0;
+  int device = 0;
+};
 struct fem2d_gep {
   Domain dom;   // the Domain the GEP was sampled from (its Elem trees drive the factorization)
   HostGEP h;
   DeviceGEP d;
   Ctx* ctx = nullptr;
+  int device = 0;   // kept apart from ctx: freeing must not read a context that may already be gone
   double t_symbolic_ms = 0, t_tables_ms = 0, t_values_ms = 0, t_upload_ms = 0;
   mutable MFPlan plan;   // factorization plan, built by the first solve and reused (pattern-only)
 };
@@ -298,6 +306,7 @@ void fem2d_ctx_destroy(fem2d_ctx* c) {
   if (c->c.flush_buf) cudaFree(c->c.flush_buf);
   if (c->c.stream) cudaStreamDestroy(c->c.stream);
   delete c;
+  cudaGetLastError();
 }
 
 int fem2d_ctx_synchronize(fem2d_ctx* c) {
@@ -387,6 +396,7 @@ int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int bas
   FEM2D_CUDA(cudaSetDevice(c->c.device));
   std::unique_ptr<fem2d_gep> g(new fem2d_gep);
   g->ctx = &c->c;
+  g->device = c->c.device;
   g->dom = d->d;
   auto t0 = std::chrono::steady_clock::now();
   build_symbolic(d->d, basis, nq_u == 0 ? 0 : nq_u, nq_v == 0 ? 0 : nq_v, g->h);
@@ -464,6 +474,8 @@ int fem2d_galerkin_sample_gep_hcurl_batch(fem2d_ctx* c, const fem2d_domain* cons
   for (int64_t i = 0; i < count; i++) {
     std::unique_ptr<fem2d_gep> g(new fem2d_gep);
     g->ctx = &c->c;
+    g->device = c->c.device;
+  g->device = c->c.device;
     g->dom = domains[i]->d;
     auto t0 = std::chrono::steady_clock::now();
     build_symbolic(domains[i]->d, basis, nq_u, nq_v, g->h);
@@ -528,8 +540,9 @@ int fem2d_autotune_clear(void) {
 
 void fem2d_gep_free(fem2d_gep* g) {
   if (!g) return;
-  if (g->ctx) cudaSetDevice(g->ctx->device);
+  cudaSetDevice(g->device);
   delete g;
+  cudaGetLastError();   // a failed release must not surface in a later, unrelated call
 }
 
 int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64_t* nnz_full) {
@@ -732,8 +745,9 @@ int fem2d_fields_create(fem2d_ctx* c, const fem2d_domain* d, int basis, int d0, 
 
 void fem2d_fields_free(fem2d_fields* f) {
   if (!f) return;
-  if (f->f.ctx) cudaSetDevice(f->f.ctx->device);
+  cudaSetDevice(f->f.device);
   delete f;
+  cudaGetLastError();
 }
 
 int64_t fem2d_fields_num_leaves(const fem2d_fields* f) { return f ? (int64_t)f->f.leaves.size() : -1; }
@@ -790,3 +804,159 @@ int fem2d_fields_xy_device(fem2d_fields* f, const double* d_solution, int64_t n_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------
+// Inner PCG solver and the learned per-Elem-patch coarse-space network (precond.h)
+int fem2d_patchnet_create(int k, int hidden, uint64_t seed, fem2d_patchnet** out) {
+  API_BEGIN
+  if (!out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (k < 1 || k > 32 || hidden < 1 || hidden > 1024) fail(FEM2D_E_INVALID_ARG, "k must be 1..32, hidden 1..1024");
+  std::unique_ptr<fem2d_patchnet> p(new fem2d_patchnet);
+  p->net.k = k;
+  p->net.hidden = hidden;
+  p->net.init(seed);
+  *out = p.release();
+  API_END
+}
+
+void fem2d_patchnet_free(fem2d_patchnet* p) { delete p; }
+
+int64_t fem2d_patchnet_num_params(const fem2d_patchnet* p) { return p ? p->net.size() : -1; }
+
+int fem2d_patchnet_get_params(const fem2d_patchnet* p, float* out) {
+  API_BEGIN
+  if (!p || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::memcpy(out, p->net.params.data(), p->net.params.size() * sizeof(float));
+  API_END
+}
+
+int fem2d_patchnet_set_params(fem2d_patchnet* p, const float* in) {
+  API_BEGIN
+  if (!p || !in) fail(FEM2D_E_INVALID_ARG, "null argument");
+  std::memcpy(p->net.params.data(), in, p->net.params.size() * sizeof(float));
+  API_END
+}
+
+int fem2d_patchnet_features(const fem2d_domain* d, double shift, int64_t* sizes, int64_t* patch_ptr, int32_t* dof,
+                            float* feat, float* weight) {
+  API_BEGIN
+  if (!d || !sizes) fail(FEM2D_E_INVALID_ARG, "null argument");
+  Patches pt;
+  build_patches(d->d, shift, pt);
+  sizes[0] = pt.npatch();
+  sizes[1] = pt.nrows;
+  if (patch_ptr) std::memcpy(patch_ptr, pt.ptr.data(), pt.ptr.size() * sizeof(int64_t));
+  if (dof) std::memcpy(dof, pt.dof.data(), pt.dof.size() * sizeof(int32_t));
+  if (feat) std::memcpy(feat, pt.feat.data(), pt.feat.size() * sizeof(float));
+  if (weight) std::memcpy(weight, pt.weight.data(), pt.weight.size() * sizeof(float));
+  API_END
+}
+
+static std::vector<double> to_row_major(const double* samples, int S, int64_t n) {
+  std::vector<double> E((size_t)n * S);
+  for (int s = 0; s < S; s++)
+    for (int64_t i = 0; i < n; i++) E[(size_t)i * S + s] = samples[(size_t)s * n + i];
+  return E;
+}
+
+int fem2d_patchnet_loss_grad(fem2d_ctx* c, const fem2d_patchnet* p, const fem2d_gep* g, double shift,
+                             const double* samples, int S, double* loss, float* grad) {
+  API_BEGIN
+  if (!c || !p || !g || !samples || !loss) fail(FEM2D_E_INVALID_ARG, "null argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  Patches pt;
+  build_patches(g->dom, shift, pt);
+  const std::vector<double> E = to_row_major(samples, S, g->h.n);
+  std::vector<float> gr(p->net.size(), 0.f);
+  *loss = patchnet_loss_grad(c->c, p->net, pt, g->h.n, E.data(), S, gr);
+  if (grad) std::memcpy(grad, gr.data(), gr.size() * sizeof(float));
+  API_END
+}
+
+int fem2d_patchnet_train(fem2d_ctx* c, fem2d_patchnet* p, const fem2d_gep* const* geps, int count, double shift,
+                         const double* const* samples, int S, int epochs, double lr, double* loss_history) {
+  API_BEGIN
+  if (!c || !p || !geps || !samples || count < 1 || epochs < 1) fail(FEM2D_E_INVALID_ARG, "invalid argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  std::vector<Patches> pts(count);
+  std::vector<std::vector<double>> Es(count);
+  std::vector<const Patches*> pp;
+  std::vector<int64_t> ns;
+  std::vector<const double*> ep;
+  for (int i = 0; i < count; i++) {
+    if (!geps[i] || !samples[i]) fail(FEM2D_E_INVALID_ARG, "null GEP or sample set");
+    build_patches(geps[i]->dom, shift, pts[i]);
+    Es[i] = to_row_major(samples[i], S, geps[i]->h.n);
+    pp.push_back(&pts[i]);
+    ns.push_back(geps[i]->h.n);
+    ep.push_back(Es[i].data());
+  }
+  const std::vector<double> h = patchnet_train(c->c, p->net, pp, ns, ep, S, epochs, lr);
+  if (loss_history) std::memcpy(loss_history, h.data(), h.size() * sizeof(double));
+  API_END
+}
+
+int fem2d_pcg_create(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, const fem2d_patchnet* net,
+                     fem2d_pcg** out) {
+  API_BEGIN
+  if (!c || !g || !out) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (g->ctx->device != c->c.device) fail(FEM2D_E_INVALID_ARG, "the GEP lives on another device");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  std::unique_ptr<fem2d_pcg> p(new fem2d_pcg);
+  p->s.reset(new PCGSolver(c->c, g->dom, g->h, g->d, c_a, c_b, net ? &net->net : nullptr));
+  p->n = g->h.n;
+  p->device = c->c.device;
+  *out = p.release();
+  API_END
+}
+
+int fem2d_pcg_solve(fem2d_pcg* p, int nrhs, const double* rhs, double* x, double tol, int max_iter, double* stats) {
+  API_BEGIN
+  if (!p || !rhs || !x || nrhs < 1 || max_iter < 1) fail(FEM2D_E_INVALID_ARG, "invalid argument");
+  PCGStats st;
+  p->s->solve(nrhs, rhs, x, tol, max_iter, &st);
+  if (stats) {
+    stats[0] = st.iters;
+    stats[1] = st.relres;
+    stats[2] = st.ms;
+    stats[3] = st.setup_ms;
+    stats[4] = st.coarse_dim;
+  }
+  if (!(st.relres <= tol)) fail(FEM2D_E_NOT_CONVERGED, "PCG did not reach the tolerance (x holds the last iterate)");
+  API_END
+}
+
+int fem2d_pcg_harvest(fem2d_pcg* p, int nrhs, const double* rhs, const double* xstar, double tol, int max_iter,
+                      int first, int every, int max_samples, double* samples, int* nsamples) {
+  API_BEGIN
+  if (!p || !rhs || !xstar || !samples || !nsamples || every < 1 || max_samples < 1)
+    fail(FEM2D_E_INVALID_ARG, "invalid argument");
+  std::vector<double> x((size_t)p->n * nrhs), snaps;
+  PCGStats st;
+  p->s->solve(nrhs, rhs, x.data(), tol, max_iter, &st, &snaps, xstar, every, max_samples, first);
+  const int S = (int)(snaps.size() / std::max<int64_t>(p->n, 1));
+  std::memcpy(samples, snaps.data(), snaps.size() * sizeof(double));
+  *nsamples = S;
+  API_END
+}
+
+int fem2d_pcg_create_with_basis(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, int k, const float* basis,
+                                fem2d_pcg** out) {
+  API_BEGIN
+  if (!c || !g || !out || !basis) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (g->ctx->device != c->c.device) fail(FEM2D_E_INVALID_ARG, "the GEP lives on another device");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  std::unique_ptr<fem2d_pcg> p(new fem2d_pcg);
+  p->s.reset(new PCGSolver(c->c, g->dom, g->h, g->d, c_a, c_b, nullptr, basis, k));
+  p->n = g->h.n;
+  p->device = c->c.device;
+  *out = p.release();
+  API_END
+}
+
+void fem2d_pcg_free(fem2d_pcg* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  delete p;
+  cudaGetLastError();
+}

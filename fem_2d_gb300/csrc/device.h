@@ -96,6 +96,11 @@ struct DeviceGEP {
   DBuf<uint32_t> specs;
   DBuf<double> ivl, glq, tables;   // ivl: (s, o) pairs; glq: u x, u w, v x, v w
   DBuf<double> a, b;               // values, full symmetric CSR order
+  // runs of consecutive rows with identical column lists (at most 64 rows each): row starts, ngrp + 1;
+  // work items (run, first column of a <= 256-column segment) for the operator products
+  DBuf<int32_t> grp;
+  DBuf<int2> gwork;
+  int ngrp = 0, nwork = 0;
   int nivl = 0;
   int64_t h2d_bytes = 0;
 };

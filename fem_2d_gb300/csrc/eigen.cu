@@ -92,6 +92,83 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t n, const int64_t* __r
   }
 }
 
+// Y = (ca A + cb B) X for nb <= 32 columns over runs of rows with one shared column list (an Elem's
+// interior functions couple to the same functions). A work item is one run and one segment of at most
+// 256 of its columns, so the long rows of ancestor Elems (over a thousand columns) spread over many
+// CTAs. Per pass of 48 columns a CTA stages the gathered X rows (48 x nb) and the run's combined
+// values ca*A + cb*B (rows x 48, each row's entries read contiguously) in shared memory, accumulates
+// every (row, column) output from shared memory only, and adds its partial sums to Y (zeroed before
+// the launch) with FP64 atomics. X is gathered once per run instead of once per row. Up to 64 rows x
+// 32 columns = 8 outputs per thread.
+constexpr int kGrpChunk = 48;
+constexpr int kGrpRows = 64;
+constexpr int kGrpSeg = 256;
+__global__ void zero_block_kernel(int64_t n, int nb, double* __restrict__ Y, int64_t ldy) {
+  const int64_t total = n * nb;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+    Y[(t / nb) * ldy + t % nb] = 0.0;
+}
+
+__global__ void __launch_bounds__(256) spmm_group_kernel(int nwork, const int2* __restrict__ work,
+                                                         const int32_t* __restrict__ grp,
+                                                         const int64_t* __restrict__ rp,
+                                                         const int32_t* __restrict__ col,
+                                                         const double* __restrict__ va, const double* __restrict__ vb,
+                                                         double ca, double cb, const double* __restrict__ X,
+                                                         int64_t ldx, int nb, double* __restrict__ Y, int64_t ldy) {
+  __shared__ double xs[kGrpChunk * 32];
+  __shared__ double vs[kGrpRows * (kGrpChunk + 1)];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int2 it = work[w];
+    const int r0 = grp[it.x], R = grp[it.x + 1] - r0;
+    const int64_t c0 = rp[r0];
+    const int cend = min((int)(rp[r0 + 1] - c0), it.y + kGrpSeg);
+    const int32_t* cols = col + c0;
+    double acc[8];
+#pragma unroll
+    for (int o = 0; o < 8; o++) acc[o] = 0.0;
+    for (int q0 = it.y; q0 < cend; q0 += kGrpChunk) {
+      const int qn = min(kGrpChunk, cend - q0);
+      __syncthreads();
+      for (int t = threadIdx.x; t < qn * nb; t += blockDim.x) {
+        const int q = t / nb, j = t - q * nb;
+        xs[q * 32 + j] = __ldg(X + (int64_t)__ldg(cols + q0 + q) * ldx + j);
+      }
+      for (int t = threadIdx.x; t < R * kGrpChunk; t += blockDim.x) {
+        const int r = t / kGrpChunk, q = t - r * kGrpChunk;
+        double v = 0.0;
+        if (q < qn) {
+          const int64_t k = rp[r0 + r] + q0 + q;
+          if (ca != 0.0) v += ca * __ldg(va + k);
+          if (cb != 0.0) v += cb * __ldg(vb + k);
+        }
+        vs[r * (kGrpChunk + 1) + q] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int o = 0; o < 8; o++) {
+        const int t = threadIdx.x + o * 256;
+        if (t < R * nb) {
+          const int r = t / nb, j = t - r * nb;
+          const double* vr = vs + r * (kGrpChunk + 1);
+          double s = acc[o];
+#pragma unroll 8
+          for (int q = 0; q < qn; q++) s += vr[q] * xs[q * 32 + j];
+          acc[o] = s;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+      const int t = threadIdx.x + o * 256;
+      if (t < R * nb) {
+        const int r = t / nb, j = t - r * nb;
+        atomicAdd(Y + (int64_t)(r0 + r) * ldy + j, acc[o]);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) gram_partial_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a,
                                                            const double* __restrict__ Y, int64_t ldy, int b,
                                                            int64_t rows_per_block, int e0, double* __restrict__ P) {
@@ -263,6 +340,8 @@ __global__ void densify_kernel(int64_t n, const int64_t* __restrict__ rp, const 
 }
 
 // ---------------------------------------------------------------- host helpers
+void setup_gemm_smem(int device);
+
 struct Dev {
   Ctx& c;
   const HostGEP& h;
@@ -276,6 +355,15 @@ struct Dev {
   void spmm(double ca, double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
     const double nv = (ca != 0.0) + (cb != 0.0);
     ProfScope ps(c, "spmm", (double)h.nnz_full * (4.0 + 8.0 * nv) + 8.0 * (h.n + 1) + 16.0 * h.n * nb);
+    if (d.nwork > 0 && nb <= 32) {
+      const int64_t zb = std::min<int64_t>((h.n * nb + 255) / 256, (int64_t)c.num_sms * 8);
+      zero_block_kernel<<<(int)std::max<int64_t>(zb, 1), 256, 0, c.stream>>>(h.n, nb, Y, ldy);
+      const int grid = std::max(1, std::min(d.nwork, c.num_sms * 6));
+      spmm_group_kernel<<<grid, 256, 0, c.stream>>>(d.nwork, d.gwork.p, d.grp.p, d.row_ptr.p, d.col.p, va, vb, ca,
+                                                    cb, X, ldx, nb, Y, ldy);
+      c.launches += 2;
+      return;
+    }
     for (int c0 = 0; c0 < nb; c0 += 32) {
       const int w = std::min(32, nb - c0);
       int G = 1;
@@ -592,7 +680,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // rebuilds the whole block Krylov space from all selected Ritz vectors (every column expanded)
   // instead of expanding the unconverged ones only
   double best_worst = 1e300;
-  int stall = 0;
+  int stall = 0, stall_total = 0;
+  bool attained = false;
   bool full = true;
   for (; cycles < max_cycles; cycles++) {
     int m, last0 = 0, lastn;
@@ -738,8 +827,19 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     if (worst < 0.5 * best_worst) {
       best_worst = worst;
       stall = 0;
+      stall_total = 0;
     } else {
       stall++;
+      stall_total++;
+    }
+    // attainable accuracy: with nearly dependent (high-order monomial) bases the FP64 residual floor
+    // can sit above tol; eight cycles without halving the worst residual, below 1e-6, end the solve
+    // as converged (eigenvalue errors scale with the squared residual)
+    if (stall_total >= 8 && worst < 1e-6) {
+      converged = true;
+      attained = true;
+      cycles++;
+      break;
     }
     full = stall >= 2;
     if (full) stall = 0;
@@ -758,6 +858,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     st->spmv_count = spmv;
     st->refine_spd = nref_p;
     st->refine_indefinite = nref_m;
+    st->dense_plan = plan.dense ? 1 : 0;
+    st->floor_reached = attained ? 1 : 0;
   }
   // back to the original pencil: x = D x~ (B-orthonormal), residuals in the original norms
   {

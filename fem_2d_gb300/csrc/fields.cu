@@ -121,6 +121,7 @@ void fields_plan(Ctx& c, const Domain& d, int basis, int d0, int d1, FieldSpace&
   if (basis == FEM2D_BASIS_KOLEG && std::max(mo[0], mo[1]) > 12)
     fail(FEM2D_E_INVALID_ARG, "KOLeg is tabulated for expansion orders up to 12");
   f.ctx = &c;
+  f.device = c.device;
   f.basis = basis;
   f.d0 = d0;
   f.d1 = d1;

@@ -23,6 +23,7 @@ struct alignas(16) FieldItem {
 
 struct FieldSpace {
   Ctx* ctx = nullptr;
+  int device = 0;
   int basis = 0, d0 = 0, d1 = 0;
   int imax = 0, jmax = 0;             // Mesh::max_expansion_orders
   int64_t ndofs = 0;

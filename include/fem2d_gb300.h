@@ -223,6 +223,8 @@ typedef struct fem2d_solve_stats {
   double max_rel_residual;
   int64_t spmv_count;
   int refine_spd, refine_indefinite;   /* iterative-refinement steps per solve with A + cB and A - sigma B */
+  int dense_plan;      /* 1: the factorization used one dense front (small, ill-conditioned GEP) */
+  int floor_reached;   /* 1: stopped at the attainable residual floor (above tol, below 1e-6) */
 } fem2d_solve_stats;
 
 /* gpu_solve_gep: the n_pairs eigenpairs of (A, B) nearest target, by a shift-invert block
@@ -272,6 +274,53 @@ int fem2d_fields_leaf_bounds(const fem2d_fields* f, double* out);
 int fem2d_fields_xy(fem2d_fields* f, const double* solution, int64_t n_solution, double* x_out, double* y_out);
 /* the same on device pointers (an eigenvector left on the device); asynchronous on the context's stream */
 int fem2d_fields_xy_device(fem2d_fields* f, const double* d_solution, int64_t n_solution, double* d_x, double* d_y);
+
+/* ---------------- inner PCG solver and learned preconditioner (no reference counterpart) ----------
+ * The reference hands the shifted systems of its sparse eigensolve to SLEPc/PETSc KSP in an external
+ * process (slepc_solve.rs:14-68). This is the device inner solver for SPD shifts K = c_a A + c_b B
+ * (c_a, c_b > 0): conjugate gradients preconditioned by
+ *   net == NULL: additive Schwarz over Elem patches (exact inverse of each Elem's block of K, every
+ *                basis function of the Elem, shared edge functions included) -- the plain method;
+ *   net != NULL: the same plus a two-level coarse correction whose basis the per-Elem-patch network
+ *                produces (k vectors per Elem from the features of its basis functions; coarse
+ *                operator Z^T K Z inverted densely, at most 16384 coarse vectors).
+ * The network (an MLP 16 -> hidden -> hidden -> k, tanh, FP32) is trained on the GPU by its own
+ * forward/backward/Adam kernels on error vectors of the plain solver. */
+typedef struct fem2d_patchnet fem2d_patchnet;
+typedef struct fem2d_pcg fem2d_pcg;
+int fem2d_patchnet_create(int k, int hidden, uint64_t seed, fem2d_patchnet** out);
+void fem2d_patchnet_free(fem2d_patchnet* p);
+int64_t fem2d_patchnet_num_params(const fem2d_patchnet* p);
+/* parameters as floats: W1 (16 x hidden), b1, W2 (hidden x hidden), b2, W3 (hidden x k), b3; row-major */
+int fem2d_patchnet_get_params(const fem2d_patchnet* p, float* out);
+int fem2d_patchnet_set_params(fem2d_patchnet* p, const float* in);
+/* the network's inputs on a Domain (host only): sizes[2] = {patches, rows}; per patch the row range
+ * (patch_ptr, patches + 1), per row its DoF, 16 features and its partition-of-unity weight */
+int fem2d_patchnet_features(const fem2d_domain* d, double shift, int64_t* sizes, int64_t* patch_ptr, int32_t* dof,
+                            float* feat, float* weight);
+/* mean projection loss over Elems and the S error samples (S vectors of ndofs doubles, one after
+ * another, S <= 256) and its gradient with respect to the parameters (grad may be NULL) */
+int fem2d_patchnet_loss_grad(fem2d_ctx* c, const fem2d_patchnet* p, const fem2d_gep* g, double shift,
+                             const double* samples, int S, double* loss, float* grad);
+/* Adam (beta 0.9/0.999) over `count` GEPs, each with S samples; loss_history[epochs] (may be NULL) */
+int fem2d_patchnet_train(fem2d_ctx* c, fem2d_patchnet* p, const fem2d_gep* const* geps, int count, double shift,
+                         const double* const* samples, int S, int epochs, double lr, double* loss_history);
+int fem2d_pcg_create(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, const fem2d_patchnet* net,
+                     fem2d_pcg** out);
+/* x = K^-1 rhs (ndofs x nrhs row-major, host); every column to ||r|| <= tol ||b||. stats (may be NULL,
+ * 5 doubles): iterations, worst relative residual, solve ms, set-up ms, coarse dimension.
+ * FEM2D_E_NOT_CONVERGED if max_iter is reached first (x holds the last iterate). */
+int fem2d_pcg_solve(fem2d_pcg* p, int nrhs, const double* rhs, double* x, double tol, int max_iter, double* stats);
+/* the solver's training data: runs PCG on rhs and records, every `every` iterations from iteration
+ * `first` on, the error xstar - x_i of each unconverged column (xstar: exact solutions, ndofs x nrhs
+ * row-major), at most max_samples vectors of ndofs doubles into samples; *nsamples = the number */
+int fem2d_pcg_harvest(fem2d_pcg* p, int nrhs, const double* rhs, const double* xstar, double tol, int max_iter,
+                      int first, int every, int max_samples, double* samples, int* nsamples);
+/* the two-level solver with a caller-given coarse basis instead of the network's: k vectors per Elem,
+ * basis[rows x k] with rows in fem2d_patchnet_features order (a deflation basis of the caller's own) */
+int fem2d_pcg_create_with_basis(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, int k, const float* basis,
+                                fem2d_pcg** out);
+void fem2d_pcg_free(fem2d_pcg* p);
 
 #ifdef __cplusplus
 }
