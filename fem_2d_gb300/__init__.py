@@ -41,7 +41,7 @@ E_B_NOT_SPD, E_SPURIOUS, E_TOO_LARGE, E_NOT_CONVERGED, E_CUDA, E_TIMEOUT, E_NO_D
 class _fem2d_solve_opts(ctypes.Structure):
     _fields_ = [("precond", ctypes.c_int), ("max_outer", ctypes.c_int), ("max_inner", ctypes.c_int),
                 ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("block", ctypes.c_int),
-                ("verbose", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("krylov_steps", ctypes.c_int)]
 
 
 class _fem2d_solve_stats(ctypes.Structure):
@@ -129,6 +129,8 @@ def lib():
         "fem2d_ctx_set_profiling": (ctypes.c_int, [P, ctypes.c_int]),
         "fem2d_ctx_profile_reset": (ctypes.c_int, [P]),
         "fem2d_ctx_profile_query": (ctypes.c_int, [P, ctypes.c_char_p, dp, i64p, dp]),
+        "fem2d_ctx_profile_flops": (ctypes.c_int, [P, ctypes.c_char_p, dp]),
+        "fem2d_ctx_fp64_peak": (ctypes.c_int, [P, dp]),
         "fem2d_dense_solve_gep": (ctypes.c_int, [P, P, d, dp, dp]),
         "fem2d_gep_shifted_solve": (ctypes.c_int, [P, P, d, d, ctypes.c_int, ctypes.c_int, dp, dp]),
         "fem2d_gpu_solve_gep": (ctypes.c_int, [P, P, d, ctypes.c_int, ctypes.POINTER(_fem2d_solve_opts), dp, dp, dp,
@@ -454,10 +456,17 @@ class Context:
         _check(lib().fem2d_ctx_profile_reset(self._h))
 
     def profile(self, region):
-        ms, cnt, by = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+        ms, cnt, by, fl = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
         _check(lib().fem2d_ctx_profile_query(self._h, region.encode(), ctypes.byref(ms), ctypes.byref(cnt),
                                              ctypes.byref(by)))
-        return {"ms": ms.value, "count": cnt.value, "bytes": by.value}
+        _check(lib().fem2d_ctx_profile_flops(self._h, region.encode(), ctypes.byref(fl)))
+        return {"ms": ms.value, "count": cnt.value, "bytes": by.value, "flops": fl.value}
+
+    def fp64_peak(self):
+        """Measured FP64 FMA throughput of the device in TFLOP/s (library microbenchmark)."""
+        t = ctypes.c_double()
+        _check(lib().fem2d_ctx_fp64_peak(self._h, ctypes.byref(t)))
+        return t.value
 
 
 class GEP:
@@ -737,7 +746,7 @@ PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
 
 
 def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOBI, tol=0.0, max_outer=0,
-                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None):
+                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0):
     """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
     the context the GEP was built on)."""
     ctx = ctx or gep.ctx
@@ -745,7 +754,7 @@ def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOB
     vals = np.zeros(n_pairs)
     vecs = np.zeros((n_pairs, n))
     res = np.zeros(n_pairs)
-    o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose)
+    o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose, krylov_steps)
     st = _fem2d_solve_stats()
     _check(lib().fem2d_gpu_solve_gep(ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
                                      _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),

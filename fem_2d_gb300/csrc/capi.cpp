@@ -376,6 +376,22 @@ int fem2d_ctx_profile_query(const fem2d_ctx* c, const char* region, double* ms, 
   API_END
 }
 
+int fem2d_ctx_profile_flops(const fem2d_ctx* c, const char* region, double* flops) {
+  API_BEGIN
+  if (!c || !region || !flops) fail(FEM2D_E_INVALID_ARG, "null argument");
+  auto it = c->c.prof.find(region);
+  *flops = it == c->c.prof.end() ? 0.0 : it->second.flops;
+  API_END
+}
+
+int fem2d_ctx_fp64_peak(fem2d_ctx* c, double* tflops) {
+  API_BEGIN
+  if (!c || !tflops) fail(FEM2D_E_INVALID_ARG, "null argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  *tflops = measure_fp64_peak(c->c);
+  API_END
+}
+
 // ------------------------------------------------------------------ galerkin
 int fem2d_galerkin_sample_gep_hcurl(fem2d_ctx* c, const fem2d_domain* d, int basis, int nq_u, int nq_v,
                                     fem2d_gep** out) {

@@ -20,7 +20,7 @@ namespace fem2d {
   } while (0)
 
 struct ProfRec {
-  double ms = 0, bytes = 0;
+  double ms = 0, bytes = 0, flops = 0;
   int64_t count = 0;
 };
 
@@ -39,9 +39,9 @@ struct Ctx {
 struct ProfScope {
   Ctx& c;
   const char* name;
-  double bytes;
+  double bytes, flops;
   cudaEvent_t a = nullptr, b = nullptr;
-  ProfScope(Ctx& ctx, const char* n, double by) : c(ctx), name(n), bytes(by) {
+  ProfScope(Ctx& ctx, const char* n, double by, double fl = 0.0) : c(ctx), name(n), bytes(by), flops(fl) {
     if (!c.profile) return;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
@@ -56,6 +56,7 @@ struct ProfScope {
     ProfRec& r = c.prof[name];
     r.ms += ms;
     r.bytes += bytes;
+    r.flops += flops;
     r.count++;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
@@ -112,5 +113,7 @@ void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, f
 // the same two kernels with the tables in a file-scope device array; writes caller-owned A and B
 void device_values_noalloc(Ctx& c, const HostGEP& g, const DeviceGEP& d, double* out_a, double* out_b);
 size_t noalloc_table_capacity();
+// peaks.cu: measured FP64 FMA throughput (TFLOP/s) on the context's device
+double measure_fp64_peak(Ctx& c);
 
 }  // namespace fem2d

@@ -8,7 +8,7 @@
 // with c = 0.05 |sigma|: eigenvalue lambda / ((lambda - sigma)(lambda + c)), close to the plain
 // shift-invert 1 / (lambda - sigma) for every physical mode, zero on the null space (A kills it
 // whatever the accuracy of the SPD solve) and small for high-frequency modes; exact multifrontal
-// solves (mf.cu). Each cycle builds a block Krylov basis [X, TX_u, T^2 X_u, T^3 X_u] (X_u the
+// solves (mf.cu). Each cycle builds a block Krylov basis [X, TX_u, ..., T^s X_u] (s = 4 by default; X_u the
 // unconverged Ritz vectors; converged pairs are kept but not expanded), B-orthonormalised by CGS2
 // in FP64, then a Rayleigh-Ritz step on the pencil (A, B) itself (FP64); Ritz pairs with a relative
 // residual above 1 (mixtures of null-space and high-frequency directions that land near sigma) are
@@ -217,7 +217,7 @@ __global__ void reduce_partials_kernel(const double* __restrict__ P, int nblk, i
 
 // Z = beta*Z + X * C; X n x a (ldx), C a x b row-major (device), Z n x b (ldz)
 __global__ void __launch_bounds__(256) gemm_nn_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a,
-                                                      const double* __restrict__ C, int b, double beta,
+                                                      const double* __restrict__ C, int b, double alpha, double beta,
                                                       double* __restrict__ Z, int64_t ldz) {
   extern __shared__ double cs[];
   for (int t = threadIdx.x; t < a * b; t += blockDim.x) cs[t] = C[t];
@@ -226,9 +226,20 @@ __global__ void __launch_bounds__(256) gemm_nn_kernel(int64_t n, const double* _
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t / b;
     const int j = (int)(t % b);
-    double s = 0.0;
     const double* xr = X + r * ldx;
-    for (int i = 0; i < a; i++) s += xr[i] * cs[i * b + j];
+    // four independent accumulators keep several row loads in flight
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = 0;
+#pragma unroll 2
+    for (; i + 4 <= a; i += 4) {
+      s0 += xr[i] * cs[i * b + j];
+      s1 += xr[i + 1] * cs[(i + 1) * b + j];
+      s2 += xr[i + 2] * cs[(i + 2) * b + j];
+      s3 += xr[i + 3] * cs[(i + 3) * b + j];
+    }
+    for (; i < a; i++) s0 += xr[i] * cs[i * b + j];
+    double s = (s0 + s1) + (s2 + s3);
+    if (alpha != 1.0) s *= alpha;
     Z[r * ldz + j] = beta == 0.0 ? s : beta * Z[r * ldz + j] + s;
   }
 }
@@ -354,7 +365,8 @@ struct Dev {
 
   void spmm(double ca, double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
     const double nv = (ca != 0.0) + (cb != 0.0);
-    ProfScope ps(c, "spmm", (double)h.nnz_full * (4.0 + 8.0 * nv) + 8.0 * (h.n + 1) + 16.0 * h.n * nb);
+    ProfScope ps(c, "spmm", (double)h.nnz_full * (4.0 + 8.0 * nv) + 8.0 * (h.n + 1) + 16.0 * h.n * nb,
+                 2.0 * (double)h.nnz_full * nb);
     if (d.nwork > 0 && nb <= 32) {
       const int64_t zb = std::min<int64_t>((h.n * nb + 255) / 256, (int64_t)c.num_sms * 8);
       zero_block_kernel<<<(int)std::max<int64_t>(zb, 1), 256, 0, c.stream>>>(h.n, nb, Y, ldy);
@@ -408,7 +420,7 @@ struct Dev {
       FEM2D_CUDA(cudaMemcpyAsync(small.p, Ct.data(), Ct.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
       const size_t smem = Ct.size() * sizeof(double);
       const int64_t blocks = std::min<int64_t>((h.n * w + 255) / 256, (int64_t)c.num_sms * 8);
-      gemm_nn_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, smem, c.stream>>>(h.n, X, ldx, a, small.p, w, beta,
+      gemm_nn_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, smem, c.stream>>>(h.n, X, ldx, a, small.p, w, 1.0, beta,
                                                                                 Z + j0, ldz);
       c.launches++;   // (pageable copies are staged before cudaMemcpyAsync returns: Ct may be reused)
     }
@@ -416,6 +428,31 @@ struct Dev {
   void axpby(double alpha, const double* X, int64_t ldx, int b, double beta, double* Y, int64_t ldy) {
     const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
     axpby_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, b, alpha, X, ldx, beta, Y, ldy);
+    c.launches++;
+  }
+  // C (a x b, device, row-major) = X^T Y without leaving the device
+  void gram_dev(const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b, double* Cd) {
+    const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
+    const int64_t rpb = (h.n + nblk - 1) / nblk;
+    const int ab = a * b;
+    if (part.n < (size_t)nblk * ab) part.alloc((size_t)nblk * ab);
+    const size_t smem = (size_t)32 * (a + b) * sizeof(double);
+    for (int e0 = 0; e0 < ab; e0 += 8 * 256) {
+      gram_partial_kernel<<<nblk, 256, smem, c.stream>>>(h.n, X, ldx, a, Y, ldy, b, rpb, e0, part.p);
+      c.launches++;
+    }
+    reduce_partials_kernel<<<(ab + 255) / 256, 256, 0, c.stream>>>(part.p, nblk, ab, Cd);
+    c.launches++;
+  }
+  // Z = beta Z + alpha X C with C (a x b) already on the device (a * b * 8 bytes fit the kernel's smem)
+  void gemm_dev(const double* X, int64_t ldx, int a, const double* Cd, int b, double alpha, double beta, double* Z,
+                int64_t ldz) {
+    if (a <= 0 || b <= 0) return;
+    const size_t smem = (size_t)a * b * sizeof(double);
+    if (smem > 96 * 1024) fail(FEM2D_E_INVALID_ARG, "device-resident projection block too large");
+    const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
+    gemm_nn_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, smem, c.stream>>>(h.n, X, ldx, a, Cd, b, alpha, beta, Z,
+                                                                              ldz);
     c.launches++;
   }
   void copy(const double* X, int64_t ldx, int b, double* Y, int64_t ldy) {
@@ -496,7 +533,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   int b = o.block > 0 ? o.block : std::min<int64_t>(k + guard, n);
   if (b < k) b = k;
   if (b > 32) fail(FEM2D_E_INVALID_ARG, "block size above 32 (n_pairs too large for one block)");
-  const int steps = 3;
+  const int steps = o.krylov_steps > 0 ? std::min(o.krylov_steps, 8) : 4;
   const int mmax = b * (steps + 1);
   const double tol = o.tol > 0 ? o.tol : 1e-10;
   const int max_cycles = o.max_outer > 0 ? o.max_outer : 40;
@@ -618,18 +655,20 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // W = V[:, m0:m0+r]: B-orthogonalise against V[:, :m0] (CGS2, B*W tracked linearly), orthonormalise
   // within the block (eigen-decomposition of its Gram matrix, rank-revealing), then store the exact
   // products A*W and B*W in AV and BV. Returns the number of columns kept.
+  DBuf<double> Cproj;
+  Cproj.alloc((size_t)mmax * 32);
   auto borth_new = [&](int m0, int r) -> int {
     if (r <= 0) return 0;
     double* Wb = V.p + m0;
     double* BWb = BV.p + m0;
     D.spmm(0.0, 1.0, Wb, mmax, r, BWb, mmax);
     spmv += r;
-    std::vector<double> C, G, w, z;
+    std::vector<double> G, w, z;
+    // W -= V (V^T B W), B W -= (B V)(V^T B W): coefficients stay on the device (no host round trip)
     auto project = [&](int cols) {
-      D.gram(V.p, mmax, m0, BWb, mmax, cols, C);
-      for (auto& x : C) x = -x;
-      D.gemm(V.p, mmax, m0, C, cols, 1.0, Wb, mmax);
-      D.gemm(BV.p, mmax, m0, C, cols, 1.0, BWb, mmax);
+      D.gram_dev(V.p, mmax, m0, BWb, mmax, cols, Cproj.p);
+      D.gemm_dev(V.p, mmax, m0, Cproj.p, cols, -1.0, 1.0, Wb, mmax);
+      D.gemm_dev(BV.p, mmax, m0, Cproj.p, cols, -1.0, 1.0, BWb, mmax);
     };
     if (m0 > 0) {
       project(r);

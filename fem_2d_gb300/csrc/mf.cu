@@ -440,26 +440,66 @@ __global__ void __launch_bounds__(256) mf_invdiag_kernel(const int32_t* __restri
   }
 }
 
-__global__ void __launch_bounds__(256) mf_forward_small_kernel(
-    const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd, const int32_t* __restrict__ dofs,
-    const int32_t* __restrict__ emap, const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
-    const int64_t* __restrict__ piv_off, const int64_t* __restrict__ woff, const double* __restrict__ F,
-    const double* __restrict__ B, int64_t ldb, int nb, double* __restrict__ W) {
-  const int fr = lf[blockIdx.x];
+// sum_{k = k0}^{k1 - 1} A[k * f] * v[k] with four independent accumulators (eight loads in flight per
+// thread): the solve loops are latency-bound on the factor reads, not FP64-bound
+__device__ __forceinline__ double col_dot(const double* __restrict__ A, int f, const double* __restrict__ v, int k0,
+                                          int k1) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int k = k0;
+#pragma unroll 2
+  for (; k + 4 <= k1; k += 4) {
+    a0 += A[(int64_t)k * f] * v[k];
+    a1 += A[(int64_t)(k + 1) * f] * v[k + 1];
+    a2 += A[(int64_t)(k + 2) * f] * v[k + 2];
+    a3 += A[(int64_t)(k + 3) * f] * v[k + 3];
+  }
+  for (; k < k1; k++) a0 += A[(int64_t)k * f] * v[k];
+  return (a0 + a1) + (a2 + a3);
+}
+
+struct SolveArgs {
+  const FrontDesc* fd;
+  const int32_t *dofs, *emap, *perm, *iperm;
+  const int64_t *piv_off, *woff;
+  const double* F;
+  const double* B;
+  int64_t ldb;
+  double* W;
+  double* X;
+  int64_t ldx;
+  int nb;
+};
+
+// forward solve of one small front by the calling CTA (sm: (f + p) * nb doubles)
+__device__ __forceinline__ void forward_small_front(int fr, const SolveArgs& a, double* sm) {
+  const FrontDesc* __restrict__ fd = a.fd;
+  const int32_t* __restrict__ dofs = a.dofs;
+  const int32_t* __restrict__ emap = a.emap;
+  const int32_t* __restrict__ perm = a.perm;
+  const int32_t* __restrict__ iperm = a.iperm;
+  const int64_t* __restrict__ piv_off = a.piv_off;
+  const int64_t* __restrict__ woff = a.woff;
+  const double* __restrict__ F = a.F;
+  const double* __restrict__ B = a.B;
+  const int64_t ldb = a.ldb;
+  const int nb = a.nb;
+  double* __restrict__ W = a.W;
   const FrontDesc d = fd[fr];
   const int f = d.f, p = d.p;
-  extern __shared__ double sm[];
   double* v = sm;            // v[c * f + i]
   double* y = sm + f * nb;   // y[c * p + i]
   const int32_t* D = dofs + d.dptr;
   const int32_t* pm = perm + piv_off[fr];
   const int32_t* ipm = iperm + piv_off[fr];
   const double* A = F + d.off;
-  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) {
-    const int i = t % f, c = t / f;
-    v[t] = i < p ? B[(int64_t)D[pm[i]] * ldb + c] : 0.0;
-  }
+  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) v[t] = 0.0;
   __syncthreads();
+  // the pivot rows' right-hand side and every child's update vector in one pass (shared-memory
+  // atomics: two children can feed the same parent row), so their dependent index loads overlap
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    atomicAdd(v + c * f + i, B[(int64_t)D[pm[i]] * ldb + c]);
+  }
   for (int slot = 0; slot < MAXKIDS; slot++) {
     const int ch = d.kid[slot];
     if (ch < 0) continue;
@@ -469,17 +509,16 @@ __global__ void __launch_bounds__(256) mf_forward_small_kernel(
     const int32_t* m = emap + cd.eptr;
     for (int t = threadIdx.x; t < sz * nb; t += blockDim.x) {
       const int i = t % sz, c = t / sz;
-      const int row = m[i] < p ? ipm[m[i]] : m[i];   // pivot rows are stored permuted
-      v[c * f + row] += cw[(int64_t)c * cd.f + cd.p + i];
+      const int mi = m[i];
+      const int row = mi < p ? ipm[mi] : mi;   // pivot rows are stored permuted
+      atomicAdd(v + c * f + row, cw[(int64_t)c * cd.f + cd.p + i]);
     }
-    __syncthreads();
   }
+  __syncthreads();
   for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
     const int i = t % p, c = t / p;
     const double* vc = v + c * f;
-    double acc = vc[i];
-    for (int k = 0; k < i; k++) acc += A[(int64_t)k * f + i] * vc[k];
-    y[c * p + i] = acc;
+    y[c * p + i] = vc[i] + col_dot(A + i, f, vc, 0, i);
   }
   __syncthreads();
   double* out = W + woff[fr];
@@ -487,9 +526,7 @@ __global__ void __launch_bounds__(256) mf_forward_small_kernel(
   for (int t = threadIdx.x; t < s * nb; t += blockDim.x) {
     const int i = p + t % s, c = t / s;
     const double* yc = y + c * p;
-    double acc = v[c * f + i];
-    for (int k = 0; k < p; k++) acc -= A[(int64_t)k * f + i] * yc[k];
-    out[(int64_t)c * f + i] = acc;
+    out[(int64_t)c * f + i] = v[c * f + i] - col_dot(A + i, f, yc, 0, p);
   }
   for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
     const int i = t % p, c = t / p;
@@ -497,16 +534,25 @@ __global__ void __launch_bounds__(256) mf_forward_small_kernel(
   }
 }
 
-__global__ void __launch_bounds__(256) mf_backward_small_kernel(
-    const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd, const int32_t* __restrict__ dofs,
-    const int64_t* __restrict__ woff, const double* __restrict__ F, const double* __restrict__ W, int nb,
-    double* __restrict__ X, int64_t ldx) {
-  const int fr = lf[blockIdx.x];
+__global__ void __launch_bounds__(256) mf_forward_small_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
+  extern __shared__ double sm[];
+  forward_small_front(lf[blockIdx.x], a, sm);
+}
+
+// backward solve of one small front by the calling CTA (sm: f * nb doubles)
+__device__ __forceinline__ void backward_small_front(int fr, const SolveArgs& a, double* sm) {
+  const FrontDesc* __restrict__ fd = a.fd;
+  const int32_t* __restrict__ dofs = a.dofs;
+  const int64_t* __restrict__ woff = a.woff;
+  const double* __restrict__ F = a.F;
+  const double* __restrict__ W = a.W;
+  const int nb = a.nb;
+  double* __restrict__ X = a.X;
+  const int64_t ldx = a.ldx;
   const FrontDesc d = fd[fr];
   const int f = d.f, p = d.p;
   if (p == 0) return;
   const int s = f - p;
-  extern __shared__ double sm[];
   double* xs = sm;            // xs[c * s + j]: solved struct unknowns
   double* z = sm + s * nb;    // z[c * p + i]
   const int32_t* D = dofs + d.dptr;
@@ -520,18 +566,19 @@ __global__ void __launch_bounds__(256) mf_backward_small_kernel(
   for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
     const int i = t % p, c = t / p;
     const double* xc = xs + c * s;
-    double acc = v[(int64_t)c * f + i];
-    for (int j = 0; j < s; j++) acc -= A[(int64_t)(p + j) * f + i] * xc[j];
-    z[c * p + i] = acc;
+    z[c * p + i] = v[(int64_t)c * f + i] - col_dot(A + (int64_t)p * f + i, f, xc, 0, s);
   }
   __syncthreads();
   for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
     const int i = t % p, c = t / p;
     const double* zc = z + c * p;
-    double acc = 0.0;
-    for (int k = i; k < p; k++) acc += A[(int64_t)k * f + i] * zc[k];
-    X[(int64_t)D[i] * ldx + c] = acc;
+    X[(int64_t)D[i] * ldx + c] = col_dot(A + i, f, zc, i, p);
   }
+}
+
+__global__ void __launch_bounds__(256) mf_backward_small_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
+  extern __shared__ double sm[];
+  backward_small_front(lf[blockIdx.x], a, sm);
 }
 
 }  // namespace
@@ -702,13 +749,16 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
   cudaStream_t st = c.stream;
   if (nb > nb_cap) fail(FEM2D_E_INVALID_ARG, "solve block wider than the workspace");
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
+  double fbytes = 0.0;
+  for (double b : level_factor_bytes) fbytes += b;
+  // the whole solve is one profiled region: per-level events would dominate the short level launches
+  ProfScope ps(c, "mf_solve", 2.0 * fbytes, 2.0 * 2.0 * (fbytes / 8.0) * nb);
+  SolveArgs a{fd, dofs.p, ea_map.p, fac.perm.p, fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, work.p, X, ldx, nb};
   for (int l = 0; l < nlevels; l++) {
-    ProfScope ps(c, "mf_forward", level_factor_bytes[l]);
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)(level_small_f[l] + level_small_p[l]) * nb * sizeof(double);
-      mf_forward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], fd, dofs.p, ea_map.p, fac.perm.p,
-                                                     fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, nb, work.p);
+      mf_forward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
       c.launches++;
     }
     if (nl > 0) {
@@ -719,12 +769,10 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     }
   }
   for (int l = nlevels - 1; l >= 0; l--) {
-    ProfScope ps(c, "mf_backward", level_factor_bytes[l]);
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)level_small_f[l] * nb * sizeof(double);
-      mf_backward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], fd, dofs.p, woff.p, Fbuf.p,
-                                                      work.p, nb, X, ldx);
+      mf_backward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
       c.launches++;
     }
     if (nl > 0) {

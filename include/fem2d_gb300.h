@@ -125,6 +125,12 @@ int fem2d_ctx_timer_stop(fem2d_ctx* c, double* ms);
 int fem2d_ctx_set_profiling(fem2d_ctx* c, int on);
 int fem2d_ctx_profile_reset(fem2d_ctx* c);
 int fem2d_ctx_profile_query(const fem2d_ctx* c, const char* region, double* ms, int64_t* count, double* bytes);
+/* algorithmic FP64 flops of a profiled region ("spmm": 2 nnz nb per call; "mf_solve": 2 per factor
+ * entry read, per right-hand side, both directions) */
+int fem2d_ctx_profile_flops(const fem2d_ctx* c, const char* region, double* flops);
+/* measured FP64 FMA throughput of this device (TFLOP/s): independent fused multiply-add chains on every
+ * SM for about 20 ms; the denominator of the FP64-bound kernels' roofline (no reference counterpart) */
+int fem2d_ctx_fp64_peak(fem2d_ctx* c, double* tflops);
 
 /* ---------------- Galerkin sampling (src/fem_problem/galerkin.rs:33-187) ---------------- */
 /* galerkin_sample_gep_hcurl::<BSpace, CurlCurl, L2Inner>(&domain, Some([nq_u, nq_v])).
@@ -206,13 +212,15 @@ int fem2d_gep_shifted_solve(fem2d_ctx* c, const fem2d_gep* g, double c_a, double
 int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, const double* d_x, int64_t ldx,
                           int nb, double* d_y, int64_t ldy);
 typedef struct fem2d_solve_opts {
-  int precond;          /* FEM2D_PRECOND_* */
-  int max_outer;        /* outer (eigen) iterations, 0 = default */
-  int max_inner;        /* inner solver iterations per application, 0 = default */
+  int precond;          /* reserved: the eigensolve's shifted systems are solved exactly (multifrontal LU);
+                           the iterative inner solver with its preconditioners is fem2d_pcg_* */
+  int max_outer;        /* outer (restart) cycles, 0 = default 40 */
+  int max_inner;        /* reserved */
   double tol;           /* relative residual ||Ax - lambda Bx|| / (|lambda| ||Bx||), 0 = default 1e-10 */
-  double inner_tol;     /* inner relative tolerance, 0 = default */
+  double inner_tol;     /* reserved */
   int block;            /* block size, 0 = default (n_pairs + guard) */
   int verbose;
+  int krylov_steps;     /* block Krylov steps per restart cycle (at most 8), 0 = default 4 */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {
