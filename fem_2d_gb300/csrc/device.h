@@ -64,24 +64,45 @@ struct ProfScope {
 };
 
 // A device buffer owned by this library.
+// Buffers that live for one call on one stream (solver temporaries, numeric factors) use the
+// stream-ordered allocator (alloc_on): their release does not synchronise the device, so concurrent
+// solves on other streams keep running. Buffers that outlive the call use alloc.
+void enable_stream_pool(int device);   // once per device: freed stream-ordered memory stays cached
+
 template <class T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t st = nullptr;   // set when the buffer came from the stream-ordered allocator
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (st) cudaFreeAsync(p, st);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    st = nullptr;
   }
   void alloc(size_t count) {
     release();
     if (count == 0) return;
     FEM2D_CUDA(cudaMalloc(&p, count * sizeof(T)));
     n = count;
+  }
+  void alloc_on(size_t count, cudaStream_t s) {
+    release();
+    if (count == 0) return;
+    FEM2D_CUDA(cudaMallocAsync(&p, count * sizeof(T), s));
+    n = count;
+    st = s;
+  }
+  void upload_on(const std::vector<T>& v, cudaStream_t s) {
+    alloc_on(v.size(), s);
+    if (!v.empty()) FEM2D_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
   }
   void upload(const std::vector<T>& v, cudaStream_t s) {
     alloc(v.size());

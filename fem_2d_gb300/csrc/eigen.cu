@@ -26,6 +26,7 @@
 #include <mutex>
 #include <numeric>
 
+#include "blockscale.h"
 #include "eigen.h"
 #include "mf.h"
 #include "mfdev.h"
@@ -392,8 +393,8 @@ struct Dev {
     const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
     const int64_t rpb = (h.n + nblk - 1) / nblk;
     const int ab = a * b;
-    if (part.n < (size_t)nblk * ab) part.alloc((size_t)nblk * ab);
-    if (small.n < (size_t)ab) small.alloc(std::max<size_t>(ab, 16384));
+    if (part.n < (size_t)nblk * ab) part.alloc_on((size_t)nblk * ab, c.stream);
+    if (small.n < (size_t)ab) small.alloc_on(std::max<size_t>(ab, 16384), c.stream);
     const size_t smem = (size_t)32 * (a + b) * sizeof(double);
     for (int e0 = 0; e0 < ab; e0 += 8 * 256) {
       gram_partial_kernel<<<nblk, 256, smem, c.stream>>>(h.n, X, ldx, a, Y, ldy, b, rpb, e0, part.p);
@@ -416,7 +417,7 @@ struct Dev {
       Ct.resize((size_t)a * w);
       for (int i = 0; i < a; i++)
         for (int j = 0; j < w; j++) Ct[(size_t)i * w + j] = C[(size_t)i * b + j0 + j];
-      if (small.n < Ct.size()) small.alloc(std::max<size_t>(Ct.size(), 16384));
+      if (small.n < Ct.size()) small.alloc_on(std::max<size_t>(Ct.size(), 16384), c.stream);
       FEM2D_CUDA(cudaMemcpyAsync(small.p, Ct.data(), Ct.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
       const size_t smem = Ct.size() * sizeof(double);
       const int64_t blocks = std::min<int64_t>((h.n * w + 255) / 256, (int64_t)c.num_sms * 8);
@@ -435,7 +436,7 @@ struct Dev {
     const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
     const int64_t rpb = (h.n + nblk - 1) / nblk;
     const int ab = a * b;
-    if (part.n < (size_t)nblk * ab) part.alloc((size_t)nblk * ab);
+    if (part.n < (size_t)nblk * ab) part.alloc_on((size_t)nblk * ab, c.stream);
     const size_t smem = (size_t)32 * (a + b) * sizeof(double);
     for (int e0 = 0; e0 < ab; e0 += 8 * 256) {
       gram_partial_kernel<<<nblk, 256, smem, c.stream>>>(h.n, X, ldx, a, Y, ldy, b, rpb, e0, part.p);
@@ -528,6 +529,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
                   fem2d_solve_stats* st) {
   auto t0 = std::chrono::steady_clock::now();
   setup_gemm_smem(c.device);
+  enable_stream_pool(c.device);
   const int64_t n = h.n;
   const int guard = std::max(4, k / 2);
   int b = o.block > 0 ? o.block : std::min<int64_t>(k + guard, n);
@@ -544,10 +546,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // eigenvalues, eigenvectors x = D x~); it keeps the unnormalised high-order bases well scaled
   DBuf<double> sc, sa, sb;
   DBuf<int> bad;
-  sc.alloc(n);
-  sa.alloc(h.nnz_full);
-  sb.alloc(h.nnz_full);
-  bad.alloc(1);
+  sc.alloc_on(n, c.stream);
+  sa.alloc_on(h.nnz_full, c.stream);
+  sb.alloc_on(h.nnz_full, c.stream);
+  bad.alloc_on(1, c.stream);
   FEM2D_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), c.stream));
   {
     const int64_t blocks = std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 16);
@@ -576,9 +578,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
 
   Dev D{c, h, d, sa.p, sb.p};
   DBuf<double> V, AV, BV, X, AX, BX, G0, W1, W2, W3;
-  V.alloc((size_t)n * mmax);
-  AV.alloc((size_t)n * mmax);
-  BV.alloc((size_t)n * mmax);
+  V.alloc_on((size_t)n * mmax, c.stream);
+  AV.alloc_on((size_t)n * mmax, c.stream);
+  BV.alloc_on((size_t)n * mmax, c.stream);
   for (DBuf<double>* buf : {&X, &AX, &BX, &G0, &W1, &W2, &W3}) buf->alloc((size_t)n * 32);
   int64_t spmv = 0, napply = 0;
 
@@ -587,8 +589,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // loses digits on indefinite pencils with ill-conditioned (monomial) bases; refinement restores
   // them. R1, R2 are scratch blocks.
   DBuf<double> R1, R2;
-  R1.alloc((size_t)n * 32);
-  R2.alloc((size_t)n * 32);
+  R1.alloc_on((size_t)n * 32, c.stream);
+  R2.alloc_on((size_t)n * 32, c.stream);
   auto solve_ref = [&](const MFFactor& fac, double ka, double kb, const double* rhs, int64_t lr, double* x, int64_t lx,
                        int nb, int nref) {
     M->solve(c, fac, rhs, lr, x, lx, nb);
@@ -607,9 +609,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     std::vector<double> R0;
     random_block(n, nb, 777, R0);
     DBuf<double> Rb, Xb, Tb;
-    Rb.alloc((size_t)n * nb);
-    Xb.alloc((size_t)n * nb);
-    Tb.alloc((size_t)n * nb);
+    Rb.alloc_on((size_t)n * nb, c.stream);
+    Xb.alloc_on((size_t)n * nb, c.stream);
+    Tb.alloc_on((size_t)n * nb, c.stream);
     FEM2D_CUDA(cudaMemcpyAsync(Rb.p, R0.data(), R0.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     std::vector<double> G;
     D.gram(Rb.p, nb, nb, Rb.p, nb, nb, G);
@@ -631,8 +633,24 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     return 3;
   };
   double rel_p = 0, rel_m = 0;
+  BlockScale bsc;
+  bool blocked = false;
+  if (plan.block) {   // an earlier solve of this GEP needed the block scaling
+    bsc.build(c, h, d, sa.p, sb.p);
+    blocked = true;
+    factor_both();
+  }
   int nref_p = calibrate(fp, 1.0, cshift, rel_p);
   int nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+  if ((rel_p > 1e-10 || rel_m > 1e-10) && !blocked && !plan.dense) {
+    // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
+    bsc.build(c, h, d, sa.p, sb.p);
+    blocked = true;
+    plan.block = true;
+    factor_both();
+    nref_p = calibrate(fp, 1.0, cshift, rel_p);
+    nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+  }
   // small GEPs whose sparse factorization stays inaccurate after refinement (pivoting restricted to
   // each front's fully-summed rows can grow badly on indefinite pencils of ill-conditioned bases)
   // switch to one dense front with partial pivoting over all rows; the choice is kept in the plan
@@ -656,7 +674,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // within the block (eigen-decomposition of its Gram matrix, rank-revealing), then store the exact
   // products A*W and B*W in AV and BV. Returns the number of columns kept.
   DBuf<double> Cproj;
-  Cproj.alloc((size_t)mmax * 32);
+  Cproj.alloc_on((size_t)mmax * 32, c.stream);
   auto borth_new = [&](int m0, int r) -> int {
     if (r <= 0) return 0;
     double* Wb = V.p + m0;
@@ -708,7 +726,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     std::vector<double> R0;
     random_block(n, b, 12345, R0);
     DBuf<double> R;
-    R.alloc((size_t)n * b);
+    R.alloc_on((size_t)n * b, c.stream);
     FEM2D_CUDA(cudaMemcpyAsync(R.p, R0.data(), R0.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     apply_T(R.p, b, X.p, 32, b);
   }
@@ -801,45 +819,50 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
         for (int k2 = 0; k2 < m2; k2++) acc += Wh[(size_t)i * m2 + k2] * Z[(size_t)k2 * m2 + q];
         Y[(size_t)i * m2 + q] = acc;
       }
-    // Ritz residuals of all m2 pairs: AV*Y - BV*Y*theta
+    // Ritz residuals AV*y - BV*y*theta of the non-spurious pairs nearest sigma only (twice the block):
+    // the selection never reaches further, and the products scale with the number of columns
+    std::vector<int> order;
+    for (int j = 0; j < m2; j++)
+      if (std::fabs(th[j]) > spur) order.push_back(j);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return std::fabs(th[x] - sigma) < std::fabs(th[y] - sigma); });
+    if ((int)order.size() < k) fail(FEM2D_E_SPURIOUS, "only spurious (null-space) Ritz values were found");
+    const int nc = std::min<int>((int)order.size(), 2 * b);
+    std::vector<double> Ysub((size_t)m * nc), thc(nc);
+    for (int i = 0; i < m; i++)
+      for (int q = 0; q < nc; q++) Ysub[(size_t)i * nc + q] = Y[(size_t)i * m2 + order[q]];
+    for (int q = 0; q < nc; q++) thc[q] = th[order[q]];
     DBuf<double> AY, BY, th_d, P;
-    AY.alloc((size_t)n * m2);
-    BY.alloc((size_t)n * m2);
-    D.gemm(AV.p, mmax, m, Y, m2, 0.0, AY.p, m2);
-    D.gemm(BV.p, mmax, m, Y, m2, 0.0, BY.p, m2);
-    th_d.upload(th, c.stream);
+    AY.alloc_on((size_t)n * nc, c.stream);
+    BY.alloc_on((size_t)n * nc, c.stream);
+    D.gemm(AV.p, mmax, m, Ysub, nc, 0.0, AY.p, nc);
+    D.gemm(BV.p, mmax, m, Ysub, nc, 0.0, BY.p, nc);
+    th_d.upload_on(thc, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
-    P.alloc((size_t)nblk * 2 * m2);
-    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AY.p, BY.p, m2, m2, th_d.p, rpb, P.p);
+    P.alloc_on((size_t)nblk * 2 * nc, c.stream);
+    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AY.p, BY.p, nc, nc, th_d.p, rpb, P.p);
     c.launches++;
-    std::vector<double> Ph((size_t)nblk * 2 * m2);
+    std::vector<double> Ph((size_t)nblk * 2 * nc);
     FEM2D_CUDA(cudaMemcpyAsync(Ph.data(), P.p, Ph.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-    std::vector<double> rel(m2);
-    for (int j = 0; j < m2; j++) {
+    std::vector<double> rel(m2, 1e300);
+    for (int q = 0; q < nc; q++) {
       double sr = 0, sb = 0;
-      for (int q = 0; q < nblk; q++) {
-        sr += Ph[(size_t)q * 2 * m2 + j];
-        sb += Ph[(size_t)q * 2 * m2 + m2 + j];
+      for (int t = 0; t < nblk; t++) {
+        sr += Ph[(size_t)t * 2 * nc + q];
+        sb += Ph[(size_t)t * 2 * nc + nc + q];
       }
-      rel[j] = std::sqrt(sr) / (std::fabs(th[j]) * std::sqrt(sb) + 1e-300);
+      rel[order[q]] = std::sqrt(sr) / (std::fabs(thc[q]) * std::sqrt(sb) + 1e-300);
     }
     std::vector<int> cand;
-    for (int j = 0; j < m2; j++)
-      if (std::fabs(th[j]) > spur && rel[j] < 1.0) cand.push_back(j);
-    std::stable_sort(cand.begin(), cand.end(),
-                     [&](int x, int y) { return std::fabs(th[x] - sigma) < std::fabs(th[y] - sigma); });
+    for (int q = 0; q < nc; q++)
+      if (rel[order[q]] < 1.0) cand.push_back(order[q]);
     if ((int)cand.size() < k) {
       // not enough credible Ritz pairs yet: keep the nearest non-spurious ones regardless of residual
-      cand.clear();
-      for (int j = 0; j < m2; j++)
-        if (std::fabs(th[j]) > spur) cand.push_back(j);
-      std::stable_sort(cand.begin(), cand.end(),
-                       [&](int x, int y) { return std::fabs(th[x] - sigma) < std::fabs(th[y] - sigma); });
+      cand.assign(order.begin(), order.begin() + nc);
     }
     std::vector<int> sel(cand.begin(), cand.begin() + std::min<size_t>(cand.size(), (size_t)b));
-    if ((int)sel.size() < k) fail(FEM2D_E_SPURIOUS, "only spurious (null-space) Ritz values were found");
     bx = (int)sel.size();
     std::vector<double> Ysel((size_t)m * bx);
     for (int i = 0; i < m; i++)
@@ -898,22 +921,27 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     st->refine_spd = nref_p;
     st->refine_indefinite = nref_m;
     st->dense_plan = plan.dense ? 1 : 0;
+    st->block_scaled = blocked ? 1 : 0;
     st->floor_reached = attained ? 1 : 0;
   }
   // back to the original pencil: x = D x~ (B-orthonormal), residuals in the original norms
   {
-    const int64_t blocks = std::min<int64_t>((n * bx + 255) / 256, (int64_t)c.num_sms * 8);
-    scale_rows_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, bx, sc.p, X.p, 32);
-    c.launches++;
+    if (blocked) {
+      bsc.unscale(c, X.p, 32, bx);
+    } else {
+      const int64_t blocks = std::min<int64_t>((n * bx + 255) / 256, (int64_t)c.num_sms * 8);
+      scale_rows_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, bx, sc.p, X.p, 32);
+      c.launches++;
+    }
     D.va = d.a.p;
     D.vb = d.b.p;
     D.spmm(1.0, 0.0, X.p, 32, bx, AX.p, 32);
     D.spmm(0.0, 1.0, X.p, 32, bx, BX.p, 32);
     DBuf<double> th_d, P;
-    th_d.upload(theta_sel, c.stream);
+    th_d.upload_on(theta_sel, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
-    P.alloc((size_t)nblk * 2 * bx);
+    P.alloc_on((size_t)nblk * 2 * bx, c.stream);
     resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AX.p, BX.p, 32, bx, th_d.p, rpb, P.p);
     c.launches++;
     std::vector<double> Ph((size_t)nblk * 2 * bx);
@@ -962,8 +990,8 @@ void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d
   mf.factor(c, d.a.p, d.b.p, 0.0, 1.0, true, fb);
   if (fb.flags & 2) fail(FEM2D_E_B_NOT_SPD, "Failed to invert B-matrix (via cholesky); likely ill-conditioned!");
   DBuf<double> Ad, Z;
-  Ad.alloc((size_t)n * n);
-  Z.alloc((size_t)n * n);
+  Ad.alloc_on((size_t)n * n, c.stream);
+  Z.alloc_on((size_t)n * n, c.stream);
   FEM2D_CUDA(cudaMemsetAsync(Ad.p, 0, (size_t)n * n * sizeof(double), c.stream));
   densify_kernel<<<(int)std::min<int64_t>(n, 4096), 128, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.a.p, d.b.p, 1.0,
                                                                         0.0, Ad.p);
@@ -1015,10 +1043,10 @@ void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP&
   const int64_t n = h.n;
   Dev D{c, h, d, d.a.p, d.b.p};
   DBuf<double> R, X, T, U;
-  R.alloc((size_t)n * 32);
-  X.alloc((size_t)n * 32);
-  T.alloc((size_t)n * 32);
-  U.alloc((size_t)n * 32);
+  R.alloc_on((size_t)n * 32, c.stream);
+  X.alloc_on((size_t)n * 32, c.stream);
+  T.alloc_on((size_t)n * 32, c.stream);
+  U.alloc_on((size_t)n * 32, c.stream);
   std::vector<double> hr((size_t)n * 32), hx((size_t)n * 32), G;
   // max over the columns of ||R - K X|| / ||R||, K = ca A + cb B
   auto relres = [&](int w) {

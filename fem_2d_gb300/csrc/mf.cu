@@ -581,6 +581,41 @@ __global__ void __launch_bounds__(256) mf_backward_small_kernel(const int32_t* _
   backward_small_front(lf[blockIdx.x], a, sm);
 }
 
+// X = Kinv B for a dense inverse (n x n, row-major): one warp per row, lane c owns right-hand side c;
+// four accumulators keep the inverse-row and B-row loads in flight
+__global__ void __launch_bounds__(256) dense_inverse_apply_kernel(int64_t n, const double* __restrict__ Kinv,
+                                                                  const double* __restrict__ B, int64_t ldb, int nb,
+                                                                  double* __restrict__ X, int64_t ldx) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < n;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const double* row = Kinv + i * n;
+    const bool live = lane < nb;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int64_t j = 0;
+    for (; j + 4 <= n; j += 4) {
+      if (live) {
+        s0 += row[j] * B[j * ldb + lane];
+        s1 += row[j + 1] * B[(j + 1) * ldb + lane];
+        s2 += row[j + 2] * B[(j + 2) * ldb + lane];
+        s3 += row[j + 3] * B[(j + 3) * ldb + lane];
+      }
+    }
+    for (; j < n; j++)
+      if (live) s0 += row[j] * B[j * ldb + lane];
+    if (live) X[i * ldx + lane] = (s0 + s1) + (s2 + s3);
+  }
+}
+
+__global__ void identity_block_kernel(int64_t n, int64_t j0, int w, double* __restrict__ E) {
+  const int64_t total = n * 32;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / 32;
+    const int c = (int)(t % 32);
+    E[t] = (c < w && i == j0 + c) ? 1.0 : 0.0;
+  }
+}
+
 }  // namespace
 
 void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
@@ -700,8 +735,9 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
                       MFFactor& out) {
   cudaStream_t st = c.stream;
   DBuf<double>& Fbuf = out.F;
-  if (Fbuf.n != (size_t)std::max<int64_t>(mat_total, 1)) Fbuf.alloc(std::max<int64_t>(mat_total, 1));
-  if (out.piv.n != (size_t)std::max<int64_t>(piv_total, 1)) out.piv.alloc(std::max<int64_t>(piv_total, 1));
+  enable_stream_pool(c.device);
+  if (Fbuf.n != (size_t)std::max<int64_t>(mat_total, 1)) Fbuf.alloc_on(std::max<int64_t>(mat_total, 1), st);
+  if (out.piv.n != (size_t)std::max<int64_t>(piv_total, 1)) out.piv.alloc_on(std::max<int64_t>(piv_total, 1), st);
   FEM2D_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), st));
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
   ProfScope ps(c, "mf_factor", 8.0 * (double)mat_total);
@@ -731,14 +767,33 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
       c.launches++;
     }
   }
-  if (out.perm.n != out.piv.n) out.perm.alloc(out.piv.n);
-  if (out.iperm.n != out.piv.n) out.iperm.alloc(out.piv.n);
+  if (out.perm.n != out.piv.n) out.perm.alloc_on(out.piv.n, st);
+  if (out.iperm.n != out.piv.n) out.iperm.alloc_on(out.piv.n, st);
   mf_perm_kernel<<<(nf + 127) / 128, 128, 0, st>>>(nf, fd, out.piv.p, piv_off.p, out.perm.p, out.iperm.p);
   c.launches++;
   if (nsmall > 0) {
     mf_invdiag_kernel<<<nsmall, 256, (size_t)max_small_p * max_small_p * sizeof(double), st>>>(lsmall.p, fd,
                                                                                               Fbuf.p);
     c.launches++;
+  }
+  out.inv_n = 0;
+  if (nf == 1 && max_p == max_f && max_f <= 4096) {
+    // one dense front: K^-1 column block by column block (solves against identity columns)
+    const int64_t n = max_f;
+    out.inv.alloc_on((size_t)n * n, st);
+    DBuf<double> E, Xt;
+    E.alloc_on((size_t)n * 32, st);
+    Xt.alloc_on((size_t)n * 32, st);
+    for (int64_t j0 = 0; j0 < n; j0 += 32) {
+      const int w = (int)std::min<int64_t>(32, n - j0);
+      identity_block_kernel<<<(int)std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 8), 256, 0, st>>>(
+          n, j0, w, E.p);
+      c.launches++;
+      solve(c, out, E.p, 32, Xt.p, 32, w);
+      FEM2D_CUDA(cudaMemcpy2DAsync(out.inv.p + j0, n * sizeof(double), Xt.p, 32 * sizeof(double),
+                                   w * sizeof(double), n, cudaMemcpyDeviceToDevice, st));
+    }
+    out.inv_n = n;
   }
   FEM2D_CUDA(cudaGetLastError());
   out.flags = read_flags(c);
@@ -748,6 +803,15 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
   const DBuf<double>& Fbuf = fac.F;
   cudaStream_t st = c.stream;
   if (nb > nb_cap) fail(FEM2D_E_INVALID_ARG, "solve block wider than the workspace");
+  if (fac.inv_n > 0) {
+    ProfScope ps(c, "mf_solve", 8.0 * fac.inv_n * fac.inv_n, 2.0 * fac.inv_n * fac.inv_n * nb);
+    const int64_t blocks = std::min<int64_t>((fac.inv_n * 32 + 255) / 256, (int64_t)c.num_sms * 8);
+    dense_inverse_apply_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, st>>>(fac.inv_n, fac.inv.p, B, ldb, nb, X,
+                                                                                 ldx);
+    c.launches++;
+    FEM2D_CUDA(cudaGetLastError());
+    return;
+  }
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
   double fbytes = 0.0;
   for (double b : level_factor_bytes) fbytes += b;

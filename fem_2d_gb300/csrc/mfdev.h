@@ -17,6 +17,10 @@ struct MFFactor {
   DBuf<int32_t> perm;    // gather permutation equivalent to the row swaps
   DBuf<int32_t> iperm;   // its inverse
   int flags = 0;   // 1: a zero pivot was perturbed, 2: a non-positive pivot in Cholesky mode
+  // dense single-front plans (small GEPs): the explicit inverse K^-1 (n x n, row-major), formed once
+  // after the factorization; solves are then one dense product instead of a sequential block walk
+  DBuf<double> inv;
+  int64_t inv_n = 0;
 };
 
 struct MFDevice {
@@ -54,6 +58,7 @@ struct MFPlan {
   std::unique_ptr<MFDevice> mf;
   bool ready = false;
   bool dense = false;   // a single dense front (chosen when the sparse plan's solves are inaccurate)
+  bool block = false;   // the eigensolve scales the pencil by row-run blocks (see blockscale.h)
   int device = -1;
   std::mutex mu;
 };

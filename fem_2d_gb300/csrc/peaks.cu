@@ -3,6 +3,9 @@
 // than FP32 operations per clock, so these kernels are bounded by it rather than by HBM.
 #include <cuda_runtime.h>
 
+#include <cstdint>
+#include <mutex>
+
 #include "device.h"
 
 namespace fem2d {
@@ -47,6 +50,20 @@ double measure_fp64_peak(Ctx& c) {
   cudaEventDestroy(e1);
   const double flops = 2.0 * 8.0 * iters * (double)blocks * threads * reps;
   return flops / (ms * 1e-3) / 1e12;
+}
+
+void enable_stream_pool(int device) {
+  static std::mutex mu;
+  static bool done[256] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  if (device < 0 || device >= 256 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
+  done[device] = true;
 }
 
 }  // namespace fem2d
