@@ -607,12 +607,91 @@ __global__ void __launch_bounds__(256) dense_inverse_apply_kernel(int64_t n, con
   }
 }
 
-__global__ void identity_block_kernel(int64_t n, int64_t j0, int w, double* __restrict__ E) {
-  const int64_t total = n * 32;
+// Gauss-Jordan inversion of a dense n x n matrix in place (n <= 4096), one pivot per step:
+//   gjp_pivot_kernel   (1 CTA)  partial pivoting: the largest |M[i][q]|, i >= q, row q <-> row p, recorded
+//   gjp_update_kernel           M[i][j] -= M[i][q] M[q][j] / M[q][q] for i, j != q
+//   gjp_finish_kernel           column q and row q scaled, then (one thread, next launch) the pivot inverted
+// and after the last step the row interchanges are undone as column interchanges in reverse order.
+// Without pivoting (SPD shifts) a non-positive pivot sets flag 2; a zero pivot sets flag 1 and is
+// perturbed.
+__global__ void __launch_bounds__(1024) gjp_pivot_kernel(int n, int q, int pivoting, double* __restrict__ M,
+                                                         int32_t* __restrict__ piv, int* __restrict__ flags) {
+  __shared__ double bv[1024];
+  __shared__ int bi[1024];
+  double best = -1.0;
+  int bidx = q;
+  if (pivoting)
+    for (int i = q + threadIdx.x; i < n; i += blockDim.x) {
+      const double a = fabs(M[(int64_t)i * n + q]);
+      if (a > best) { best = a; bidx = i; }
+    }
+  bv[threadIdx.x] = best;
+  bi[threadIdx.x] = bidx;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      const double o = bv[threadIdx.x + st];
+      const int oi = bi[threadIdx.x + st];
+      if (o > bv[threadIdx.x] || (o == bv[threadIdx.x] && oi < bi[threadIdx.x])) {
+        bv[threadIdx.x] = o;
+        bi[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const int p = pivoting ? bi[0] : q;
+  if (threadIdx.x == 0) piv[q] = p;
+  if (p != q)
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      const double t = M[(int64_t)q * n + j];
+      M[(int64_t)q * n + j] = M[(int64_t)p * n + j];
+      M[(int64_t)p * n + j] = t;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double d = M[(int64_t)q * n + q];
+    if (!(fabs(d) > 0.0) || (!pivoting && !(d > 0.0))) {
+      atomicOr(flags, pivoting ? 1 : 2);
+      if (d == 0.0) M[(int64_t)q * n + q] = 1e-300;
+    }
+  }
+}
+
+__global__ void gjp_update_kernel(int n, int q, double* __restrict__ M) {
+  const double inv = 1.0 / M[(int64_t)q * n + q];
+  const int64_t total = (int64_t)n * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / 32;
-    const int c = (int)(t % 32);
-    E[t] = (c < w && i == j0 + c) ? 1.0 : 0.0;
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (i == q || j == q) continue;
+    M[t] -= M[(int64_t)i * n + q] * inv * M[(int64_t)q * n + j];
+  }
+}
+
+__global__ void gjp_finish_kernel(int n, int q, double* __restrict__ M) {
+  const double inv = 1.0 / M[(int64_t)q * n + q];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (i != q) {
+      M[(int64_t)i * n + q] = -M[(int64_t)i * n + q] * inv;
+      M[(int64_t)q * n + i] = M[(int64_t)q * n + i] * inv;
+    }
+}
+
+__global__ void gjp_recip_kernel(int n, int q, double* __restrict__ M) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) M[(int64_t)q * n + q] = 1.0 / M[(int64_t)q * n + q];
+}
+
+// undo the row interchanges as column interchanges, last pivot first; one thread per row
+__global__ void gjp_unscramble_kernel(int n, const int32_t* __restrict__ piv, double* __restrict__ M) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double* row = M + (int64_t)i * n;
+    for (int k = n - 1; k >= 0; k--) {
+      const int p = piv[k];
+      if (p != k) {
+        const double t = row[k];
+        row[k] = row[p];
+        row[p] = t;
+      }
+    }
   }
 }
 
@@ -741,6 +820,32 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
   FEM2D_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), st));
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
   ProfScope ps(c, "mf_factor", 8.0 * (double)mat_total);
+  out.inv_n = 0;
+  if (nf == 1 && max_p == max_f && max_f <= 4096) {
+    // one dense front (a small GEP): its explicit inverse by Gauss-Jordan, kept in F; solves are then
+    // one dense product
+    const int n = max_f;
+    FEM2D_CUDA(cudaMemsetAsync(Fbuf.p, 0, (size_t)n * n * sizeof(double), st));
+    mf_assemble_kernel<<<dim3(8, 1), 256, 0, st>>>(lfronts.p, fd, asm_pos.p, asm_csr.p, va, vb, ca, cb, Fbuf.p);
+    c.launches++;
+    const int gu = (int)std::min<int64_t>(((int64_t)n * n + 255) / 256, (int64_t)c.num_sms * 8);
+    const int pivoting = cholesky ? 0 : 1;
+    for (int q = 0; q < n; q++) {
+      gjp_pivot_kernel<<<1, 1024, 0, st>>>(n, q, pivoting, Fbuf.p, out.piv.p, flags.p);
+      gjp_update_kernel<<<gu, 256, 0, st>>>(n, q, Fbuf.p);
+      gjp_finish_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, q, Fbuf.p);
+      gjp_recip_kernel<<<1, 32, 0, st>>>(n, q, Fbuf.p);
+      c.launches += 4;
+    }
+    if (pivoting) {
+      gjp_unscramble_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, out.piv.p, Fbuf.p);
+      c.launches++;
+    }
+    FEM2D_CUDA(cudaGetLastError());
+    out.inv_n = n;
+    out.flags = read_flags(c);
+    return;
+  }
   for (int l = 0; l < nlevels; l++) {
     const int nfl = level_ptr[l + 1] - level_ptr[l];
     const int32_t* lf = lfronts.p + level_ptr[l];
@@ -776,25 +881,7 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
                                                                                               Fbuf.p);
     c.launches++;
   }
-  out.inv_n = 0;
-  if (nf == 1 && max_p == max_f && max_f <= 4096) {
-    // one dense front: K^-1 column block by column block (solves against identity columns)
-    const int64_t n = max_f;
-    out.inv.alloc_on((size_t)n * n, st);
-    DBuf<double> E, Xt;
-    E.alloc_on((size_t)n * 32, st);
-    Xt.alloc_on((size_t)n * 32, st);
-    for (int64_t j0 = 0; j0 < n; j0 += 32) {
-      const int w = (int)std::min<int64_t>(32, n - j0);
-      identity_block_kernel<<<(int)std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 8), 256, 0, st>>>(
-          n, j0, w, E.p);
-      c.launches++;
-      solve(c, out, E.p, 32, Xt.p, 32, w);
-      FEM2D_CUDA(cudaMemcpy2DAsync(out.inv.p + j0, n * sizeof(double), Xt.p, 32 * sizeof(double),
-                                   w * sizeof(double), n, cudaMemcpyDeviceToDevice, st));
-    }
-    out.inv_n = n;
-  }
+
   FEM2D_CUDA(cudaGetLastError());
   out.flags = read_flags(c);
 }
@@ -806,7 +893,7 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
   if (fac.inv_n > 0) {
     ProfScope ps(c, "mf_solve", 8.0 * fac.inv_n * fac.inv_n, 2.0 * fac.inv_n * fac.inv_n * nb);
     const int64_t blocks = std::min<int64_t>((fac.inv_n * 32 + 255) / 256, (int64_t)c.num_sms * 8);
-    dense_inverse_apply_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, st>>>(fac.inv_n, fac.inv.p, B, ldb, nb, X,
+    dense_inverse_apply_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, st>>>(fac.inv_n, Fbuf.p, B, ldb, nb, X,
                                                                                  ldx);
     c.launches++;
     FEM2D_CUDA(cudaGetLastError());

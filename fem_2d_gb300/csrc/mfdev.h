@@ -17,9 +17,8 @@ struct MFFactor {
   DBuf<int32_t> perm;    // gather permutation equivalent to the row swaps
   DBuf<int32_t> iperm;   // its inverse
   int flags = 0;   // 1: a zero pivot was perturbed, 2: a non-positive pivot in Cholesky mode
-  // dense single-front plans (small GEPs): the explicit inverse K^-1 (n x n, row-major), formed once
-  // after the factorization; solves are then one dense product instead of a sequential block walk
-  DBuf<double> inv;
+  // dense single-front plans (small GEPs): F holds the explicit inverse K^-1 (n x n) instead of LU
+  // factors (Gauss-Jordan, partial pivoting); solves are then one dense product
   int64_t inv_n = 0;
 };
 
