@@ -49,7 +49,7 @@ class _fem2d_solve_stats(ctypes.Structure):
                 ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
                 ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64),
                 ("refine_spd", ctypes.c_int), ("refine_indefinite", ctypes.c_int), ("dense_plan", ctypes.c_int),
-                ("floor_reached", ctypes.c_int), ("block_scaled", ctypes.c_int)]
+                ("floor_reached", ctypes.c_int), ("block_scaled", ctypes.c_int), ("delayed_pivots", ctypes.c_int)]
 
 
 def lib():

@@ -34,7 +34,6 @@
 
 namespace fem2d {
 
-void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s);
 
 namespace {
 
@@ -256,6 +255,26 @@ __global__ void copy_block_kernel(int64_t n, int b, const double* __restrict__ X
 }
 
 // R = AX - BX * diag(theta) column by column, accumulating column sums of squares of R and of BX
+// per CTA the largest absolute row sum of ka A + kb B over its rows (an upper bound of the 2-norm)
+__global__ void __launch_bounds__(256) rowsum_max_kernel(int64_t n, const int64_t* __restrict__ rp,
+                                                         const double* __restrict__ va, const double* __restrict__ vb,
+                                                         double ka, double kb, double* __restrict__ part) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t k = rp[r]; k < rp[r + 1]; k++) s += fabs(ka * va[k] + kb * vb[k]);
+    m = fmax(m, s);
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
 // Y = alpha X + beta Y on an n x b row-major block
 __global__ void axpby_kernel(int64_t n, int b, double alpha, const double* __restrict__ X, int64_t ldx, double beta,
                              double* __restrict__ Y, int64_t ldy) {
@@ -501,7 +520,7 @@ MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h) {
     p.mf.reset();
     p.sym.reset(new MFSymbolic);
     if (p.dense) mf_symbolic_dense(h, *p.sym);
-    else mf_symbolic(dom, h, *p.sym);
+    else mf_symbolic(dom, h, *p.sym, p.lift.empty() ? nullptr : &p.lift);
     p.mf.reset(new MFDevice);
     p.mf->setup(c, *p.sym, 32);
     p.device = c.device;
@@ -567,8 +586,20 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   MFFactor fm, fp;
   // A + c B (c > 0) is SPD: factored without pivoting
   const double cshift = 0.05 * std::fabs(sigma);
+  int delayed = 0;
   auto factor_both = [&]() {
     M->factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
+    // delayed pivoting: columns of A - sigma B without a stable pivot among their front's fully-summed
+    // rows move (their DoFs' elimination) to the parent front; re-plan and refactor, at most 3 rounds
+    for (int round = 0; round < 3 && !fm.weak.empty() && !plan.dense; round++) {
+      if (plan.lift.empty()) plan.lift.assign(n, 0);
+      for (int32_t x : fm.weak)
+        if (plan.lift[x] < 255) plan.lift[x]++;
+      delayed += (int)fm.weak.size();
+      plan.ready = false;
+      M = &mf_plan(plan, c, dom, h);
+      M->factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
+    }
     M->factor(c, sa.p, sb.p, 1.0, cshift, true, fp);
     if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + c B is not positive definite; B is likely ill-conditioned");
   };
@@ -604,8 +635,24 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   };
   // refinement steps needed by each factorization: measured once on a fixed random block, up to 3
   // steps, while the relative residual max_j ||rhs_j - K x_j|| / ||rhs_j|| stays above 1e-12
+  // The accuracy measure is the normwise backward error ||b - K x|| / (||K|| ||x|| + ||b||) of the
+  // solves (||K|| bounded by the largest absolute row sum): a backward-stable factorization keeps it
+  // near the unit roundoff whatever cond(K) is, whereas the plain residual ||b - K x|| / ||b|| cannot
+  // fall below about eps * cond(K) even for an exact-in-FP64 solve.
   auto calibrate = [&](const MFFactor& fac, double ka, double kb, double& rel_out) -> int {
     const int nb = 4;
+    double knorm = 0.0;
+    {
+      const int nblk = std::max(1, std::min<int>(c.num_sms * 2, (int)((n + 255) / 256)));
+      DBuf<double> part;
+      part.alloc_on(nblk, c.stream);
+      rowsum_max_kernel<<<nblk, 256, 0, c.stream>>>(n, d.row_ptr.p, D.va, D.vb, ka, kb, part.p);
+      c.launches++;
+      std::vector<double> hp(nblk);
+      FEM2D_CUDA(cudaMemcpyAsync(hp.data(), part.p, nblk * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+      for (double v : hp) knorm = std::max(knorm, v);
+    }
     std::vector<double> R0;
     random_block(n, nb, 777, R0);
     DBuf<double> Rb, Xb, Tb;
@@ -623,11 +670,17 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       D.spmm(ka, kb, Xb.p, nb, nb, Tb.p, nb);
       D.axpby(1.0, Rb.p, nb, nb, -1.0, Tb.p, nb);
       D.gram(Tb.p, nb, nb, Tb.p, nb, nb, G);
-      double rel = 0;
-      for (int j = 0; j < nb; j++) rel = std::max(rel, std::sqrt(G[(size_t)j * nb + j]) / bn[j]);
-      rel_out = std::min(rel, prev);
-      if (rel < 1e-12) return nref;                      // accurate enough
-      if (rel > 0.5 * prev) return std::max(0, nref - 1);  // no longer improving
+      std::vector<double> GX;
+      D.gram(Xb.p, nb, nb, Xb.p, nb, nb, GX);
+      double rel = 0, bwd = 0;
+      for (int j = 0; j < nb; j++) {
+        const double rn = std::sqrt(G[(size_t)j * nb + j]), xn = std::sqrt(GX[(size_t)j * nb + j]);
+        rel = std::max(rel, rn / bn[j]);
+        bwd = std::max(bwd, rn / (knorm * xn + bn[j]));
+      }
+      if (nref == 0 || rel <= prev) rel_out = bwd;
+      if (rel < 1e-12 || bwd < 1e-15) return nref;        // as accurate as FP64 allows
+      if (rel > 0.5 * prev) return std::max(0, nref - 1);  // refinement no longer improves
       prev = rel;
     }
     return 3;
@@ -642,7 +695,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   }
   int nref_p = calibrate(fp, 1.0, cshift, rel_p);
   int nref_m = calibrate(fm, 1.0, -sigma, rel_m);
-  if ((rel_p > 1e-10 || rel_m > 1e-10) && !blocked && !plan.dense) {
+  if ((rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense) {
     // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
     bsc.build(c, h, d, sa.p, sb.p);
     blocked = true;
@@ -655,7 +708,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // each front's fully-summed rows can grow badly on indefinite pencils of ill-conditioned bases)
   // switch to one dense front with partial pivoting over all rows; the choice is kept in the plan
   constexpr int64_t kDenseMax = 4096;
-  if ((rel_p > 1e-10 || rel_m > 1e-10) && !plan.dense && n <= kDenseMax) {
+  if ((rel_p > 1e-11 || rel_m > 1e-11) && !plan.dense && n <= kDenseMax) {
     M = &mf_plan_dense(plan, c, h);
     factor_both();
     nref_p = calibrate(fp, 1.0, cshift, rel_p);
@@ -922,6 +975,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     st->refine_indefinite = nref_m;
     st->dense_plan = plan.dense ? 1 : 0;
     st->block_scaled = blocked ? 1 : 0;
+    st->delayed_pivots = delayed;
     st->floor_reached = attained ? 1 : 0;
   }
   // back to the original pencil: x = D x~ (B-orthonormal), residuals in the original norms

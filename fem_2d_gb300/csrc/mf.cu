@@ -63,10 +63,18 @@ __global__ void mf_extend_add_kernel(const int32_t* __restrict__ lf, const Front
 }
 
 // columns k0 .. k0+w-1 of every front with p > k0: pivot, swap full rows, scale, update the panel
+// A column whose largest fully-summed entry is below kWeakPivot times its largest entry in the rows of
+// the front's other (not yet summed) DoFs has no stable pivot here: its DoF is recorded, and the solver
+// moves its elimination to the parent front and refactors (delayed pivoting).
+constexpr double kWeakPivot = 1e-3;
+
 __global__ void __launch_bounds__(256) mf_panel_kernel(const int32_t* __restrict__ lf,
                                                        const FrontDesc* __restrict__ fd, int k0, int pivoting,
                                                        double* __restrict__ F, int32_t* __restrict__ piv,
-                                                       const int64_t* __restrict__ piv_off, int* __restrict__ flags) {
+                                                       const int64_t* __restrict__ piv_off, int* __restrict__ flags,
+                                                       const int32_t* __restrict__ dofs,
+                                                       int32_t* __restrict__ weak, int* __restrict__ nweak,
+                                                       int weak_cap) {
   const int fr = lf[blockIdx.x];
   const FrontDesc d = fd[fr];
   if (d.p <= k0) return;
@@ -102,6 +110,21 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int32_t* __restrict
         __syncthreads();
       }
       best = sidx[0];
+      const double fully = sval[0];
+      __syncthreads();
+      // largest entry of column k in the rows of the not-yet-summed DoFs
+      double sm = 0.0;
+      for (int i = d.p + threadIdx.x; i < f; i += blockDim.x) sm = fmax(sm, fabs(colk[i]));
+      sval[threadIdx.x] = sm;
+      __syncthreads();
+      for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) sval[threadIdx.x] = fmax(sval[threadIdx.x], sval[threadIdx.x + st]);
+        __syncthreads();
+      }
+      if (threadIdx.x == 0 && fully < kWeakPivot * sval[0] && d.parent >= 0) {
+        const int slot = atomicAdd(nweak, 1);
+        if (slot < weak_cap) weak[slot] = dofs[d.dptr + k];
+      }
     }
     if (threadIdx.x == 0) {
       s_piv = best;
@@ -759,6 +782,8 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
   piv_total = po;
   work.alloc(std::max<int64_t>(wo, 1));
   flags.alloc(1);
+  weak_list.alloc(std::max<int64_t>(s.n, 1));
+  weak_count.alloc(1);
   level_max_f.assign(nlevels, 0);
   level_max_p.assign(nlevels, 0);
   level_factor_bytes.assign(nlevels, 0.0);
@@ -818,6 +843,8 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
   if (Fbuf.n != (size_t)std::max<int64_t>(mat_total, 1)) Fbuf.alloc_on(std::max<int64_t>(mat_total, 1), st);
   if (out.piv.n != (size_t)std::max<int64_t>(piv_total, 1)) out.piv.alloc_on(std::max<int64_t>(piv_total, 1), st);
   FEM2D_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), st));
+  FEM2D_CUDA(cudaMemsetAsync(weak_count.p, 0, sizeof(int), st));
+  out.weak.clear();
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
   ProfScope ps(c, "mf_factor", 8.0 * (double)mat_total);
   out.inv_n = 0;
@@ -860,7 +887,8 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
     }
     const int mf = level_max_f[l], mp = level_max_p[l];
     for (int k0 = 0; k0 < mp; k0 += PANEL) {
-      mf_panel_kernel<<<nfl, 256, 0, st>>>(lf, fd, k0, cholesky ? 0 : 1, Fbuf.p, out.piv.p, piv_off.p, flags.p);
+      mf_panel_kernel<<<nfl, 256, 0, st>>>(lf, fd, k0, cholesky ? 0 : 1, Fbuf.p, out.piv.p, piv_off.p, flags.p,
+                                           dofs.p, weak_list.p, weak_count.p, (int)weak_list.n);
       const int rest = mf - k0;   // upper bound of remaining columns
       if (rest > 0) {
         dim3 gt((rest + 127) / 128, nfl);
@@ -884,6 +912,17 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
 
   FEM2D_CUDA(cudaGetLastError());
   out.flags = read_flags(c);
+  if (!cholesky) {
+    int nw = 0;
+    FEM2D_CUDA(cudaMemcpyAsync(&nw, weak_count.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FEM2D_CUDA(cudaStreamSynchronize(st));
+    nw = std::min<int>(nw, (int)weak_list.n);
+    if (nw > 0) {
+      out.weak.resize(nw);
+      FEM2D_CUDA(cudaMemcpyAsync(out.weak.data(), weak_list.p, nw * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+      FEM2D_CUDA(cudaStreamSynchronize(st));
+    }
+  }
 }
 
 void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, double* X, int64_t ldx, int nb) {

@@ -42,7 +42,8 @@ struct MFSymbolic {
   double flops = 0;                        // factorization flop estimate
 };
 
-void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s);
+// lift (optional, one entry per DoF): eliminate that DoF so many tree levels above its natural front
+void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s, const std::vector<uint8_t>* lift = nullptr);
 // one dense front with every DoF (full partial pivoting)
 void mf_symbolic_dense(const HostGEP& g, MFSymbolic& s);
 

@@ -18,7 +18,7 @@
 
 namespace fem2d {
 
-void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
+void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s, const std::vector<uint8_t>* lift) {
   const Mesh& m = d.mesh;
   const int64_t n = g.n;
   const int R = (int)m.roots.size();
@@ -99,6 +99,11 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s) {
       node[dof] = node[dof] < 0 ? en : lca(node[dof], en);
     }
   }
+  // delayed pivots: a DoF whose column could not be pivoted stably in its front is eliminated that many
+  // levels higher (every coupling of the DoF stays on one root path, so the tree remains valid)
+  if (lift && (int64_t)lift->size() == n)
+    for (int64_t x = 0; x < n; x++)
+      for (int l = 0; l < (*lift)[x] && node[x] >= 0 && parent[node[x]] >= 0; l++) node[x] = parent[node[x]];
   std::vector<std::vector<int32_t>> piv(NF);
   for (int64_t x = 0; x < n; x++) {
     if (node[x] < 0) fail(FEM2D_E_INVALID_ARG, "a DoF has no basis spec");

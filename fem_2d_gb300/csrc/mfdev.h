@@ -17,6 +17,7 @@ struct MFFactor {
   DBuf<int32_t> perm;    // gather permutation equivalent to the row swaps
   DBuf<int32_t> iperm;   // its inverse
   int flags = 0;   // 1: a zero pivot was perturbed, 2: a non-positive pivot in Cholesky mode
+  std::vector<int32_t> weak;   // DoFs whose columns had no stable pivot among their front's fully-summed rows
   // dense single-front plans (small GEPs): F holds the explicit inverse K^-1 (n x n) instead of LU
   // factors (Gauss-Jordan, partial pivoting); solves are then one dense product
   int64_t inv_n = 0;
@@ -34,6 +35,8 @@ struct MFDevice {
   DBuf<int64_t> asm_pos, asm_csr, piv_off, woff;
   DBuf<double> work;
   DBuf<int> flags;
+  DBuf<int32_t> weak_list;   // capacity n: weak-pivot DoFs recorded by the panel kernel
+  DBuf<int> weak_count;
   // per level, the fronts solved by one CTA each (inverted diagonal blocks) and the rest (clusters)
   std::vector<int32_t> small_ptr, large_ptr;   // nlevels + 1 offsets into lsmall / llarge
   std::vector<int32_t> level_small_f, level_small_p;
@@ -58,6 +61,7 @@ struct MFPlan {
   bool ready = false;
   bool dense = false;   // a single dense front (chosen when the sparse plan's solves are inaccurate)
   bool block = false;   // the eigensolve scales the pencil by row-run blocks (see blockscale.h)
+  std::vector<uint8_t> lift;   // per DoF: levels its elimination was moved up (delayed pivots)
   int device = -1;
   std::mutex mu;
 };

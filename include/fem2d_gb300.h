@@ -234,6 +234,7 @@ typedef struct fem2d_solve_stats {
   int dense_plan;      /* 1: the factorization used one dense front (small, ill-conditioned GEP) */
   int floor_reached;   /* 1: stopped at the attainable residual floor (above tol, below 1e-6) */
   int block_scaled;    /* 1: the pencil was scaled by Cholesky factors of B's row-run diagonal blocks */
+  int delayed_pivots;  /* DoFs whose elimination moved to a parent front (no stable pivot in their own) */
 } fem2d_solve_stats;
 
 /* gpu_solve_gep: the n_pairs eigenpairs of (A, B) nearest target, by a shift-invert block
