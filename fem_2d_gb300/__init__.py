@@ -41,7 +41,8 @@ E_B_NOT_SPD, E_SPURIOUS, E_TOO_LARGE, E_NOT_CONVERGED, E_CUDA, E_TIMEOUT, E_NO_D
 class _fem2d_solve_opts(ctypes.Structure):
     _fields_ = [("precond", ctypes.c_int), ("max_outer", ctypes.c_int), ("max_inner", ctypes.c_int),
                 ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("block", ctypes.c_int),
-                ("verbose", ctypes.c_int), ("krylov_steps", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("krylov_steps", ctypes.c_int),
+                ("damping", ctypes.c_double), ("scaling", ctypes.c_int)]
 
 
 class _fem2d_solve_stats(ctypes.Structure):
@@ -49,7 +50,8 @@ class _fem2d_solve_stats(ctypes.Structure):
                 ("t_setup_ms", ctypes.c_double), ("t_solve_ms", ctypes.c_double),
                 ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64),
                 ("refine_spd", ctypes.c_int), ("refine_indefinite", ctypes.c_int), ("dense_plan", ctypes.c_int),
-                ("floor_reached", ctypes.c_int), ("block_scaled", ctypes.c_int), ("delayed_pivots", ctypes.c_int)]
+                ("floor_reached", ctypes.c_int), ("block_scaled", ctypes.c_int), ("delayed_pivots", ctypes.c_int),
+                ("max_backward_error", ctypes.c_double)]
 
 
 def lib():
@@ -746,7 +748,7 @@ PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
 
 
 def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOBI, tol=0.0, max_outer=0,
-                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0):
+                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0, damping=0.0, scaling=0):
     """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
     the context the GEP was built on)."""
     ctx = ctx or gep.ctx
@@ -754,7 +756,8 @@ def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOB
     vals = np.zeros(n_pairs)
     vecs = np.zeros((n_pairs, n))
     res = np.zeros(n_pairs)
-    o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose, krylov_steps)
+    o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose, krylov_steps, damping,
+                          scaling)
     st = _fem2d_solve_stats()
     _check(lib().fem2d_gpu_solve_gep(ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
                                      _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),

@@ -254,16 +254,20 @@ __global__ void copy_block_kernel(int64_t n, int b, const double* __restrict__ X
   }
 }
 
-// R = AX - BX * diag(theta) column by column, accumulating column sums of squares of R and of BX
-// per CTA the largest absolute row sum of ka A + kb B over its rows (an upper bound of the 2-norm)
+// per CTA the largest absolute row sum of ka A + kb B over its rows (an upper bound of the 2-norm);
+// one warp per row (coalesced reads of the row's values)
 __global__ void __launch_bounds__(256) rowsum_max_kernel(int64_t n, const int64_t* __restrict__ rp,
                                                          const double* __restrict__ va, const double* __restrict__ vb,
                                                          double ka, double kb, double* __restrict__ part) {
   __shared__ double red[256];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double m = 0.0;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t r = warp0; r < n; r += nwarps) {
     double s = 0.0;
-    for (int64_t k = rp[r]; k < rp[r + 1]; k++) s += fabs(ka * va[k] + kb * vb[k]);
+    for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += 32) s += fabs(ka * va[k] + kb * vb[k]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     m = fmax(m, s);
   }
   red[threadIdx.x] = m;
@@ -286,34 +290,42 @@ __global__ void axpby_kernel(int64_t n, int b, double alpha, const double* __res
   }
 }
 
+// R = AX - BX * diag(theta) column by column, accumulating per CTA the column sums of squares of R, of
+// BX and of X: P[cta][0, b) = |R|^2, [b, 2b) = |BX|^2, [2b, 3b) = |X|^2
 __global__ void __launch_bounds__(256) resid_partial_kernel(int64_t n, const double* __restrict__ AX,
-                                                            const double* __restrict__ BX, int64_t ld, int b,
+                                                            const double* __restrict__ BX,
+                                                            const double* __restrict__ X, int64_t ld, int b,
                                                             const double* __restrict__ theta, int64_t rows_per_block,
                                                             double* __restrict__ P) {
-  __shared__ double sr[256], sb[256];
+  __shared__ double sr[256], sb[256], sx[256];
   const int64_t r0 = blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
   for (int j = 0; j < b; j++) {
-    double a1 = 0.0, a2 = 0.0;
+    double a1 = 0.0, a2 = 0.0, a3 = 0.0;
     const double th = theta[j];
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
       const double bx = BX[r * ld + j];
       const double res = AX[r * ld + j] - th * bx;
+      const double x = X[r * ld + j];
       a1 += res * res;
       a2 += bx * bx;
+      a3 += x * x;
     }
     sr[threadIdx.x] = a1;
     sb[threadIdx.x] = a2;
+    sx[threadIdx.x] = a3;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
       if (threadIdx.x < s) {
         sr[threadIdx.x] += sr[threadIdx.x + s];
         sb[threadIdx.x] += sb[threadIdx.x + s];
+        sx[threadIdx.x] += sx[threadIdx.x + s];
       }
       __syncthreads();
     }
     if (threadIdx.x == 0) {
-      P[(int64_t)blockIdx.x * 2 * b + j] = sr[0];
-      P[(int64_t)blockIdx.x * 2 * b + b + j] = sb[0];
+      P[(int64_t)blockIdx.x * 3 * b + j] = sr[0];
+      P[(int64_t)blockIdx.x * 3 * b + b + j] = sb[0];
+      P[(int64_t)blockIdx.x * 3 * b + 2 * b + j] = sx[0];
     }
     __syncthreads();
   }
@@ -570,22 +582,40 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   sb.alloc_on(h.nnz_full, c.stream);
   bad.alloc_on(1, c.stream);
   FEM2D_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), c.stream));
+  const int64_t jblocks = std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 16));
   {
-    const int64_t blocks = std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 16);
-    jacobi_scale_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.b.p,
-                                                                                 sc.p, bad.p);
-    scale_csr_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.a.p, d.b.p,
-                                                                              sc.p, sa.p, sb.p);
+    jacobi_scale_kernel<<<(int)jblocks, 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.b.p, sc.p, bad.p);
+    scale_csr_kernel<<<(int)jblocks, 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.a.p, d.b.p, sc.p, sa.p, sb.p);
     c.launches += 2;
     int hb = 0;
     FEM2D_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
     if (hb) fail(FEM2D_E_B_NOT_SPD, "B has a non-positive diagonal entry");
   }
+  // Row-run block scaling (default): S = blockdiag(L_g^-1) over runs of rows with one column list, L_g the
+  // Cholesky factor of B's diagonal block of run g; S A S^T and S B S^T keep the pattern, their diagonal
+  // blocks of B become identities, and cond(B) drops by orders of magnitude for monomial bases, which
+  // lowers the forward error of every shifted solve. A run block that is not numerically positive
+  // definite falls back to the Jacobi scaling (unless the block scaling was asked for).
+  BlockScale bsc;
+  bool blocked = false;
+  if (o.scaling != 1) {
+    try {
+      bsc.build(c, h, d, sa.p, sb.p);
+      blocked = true;
+    } catch (const Error&) {
+      if (o.scaling == 2) throw;
+      scale_csr_kernel<<<(int)jblocks, 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.a.p, d.b.p, sc.p, sa.p, sb.p);
+      c.launches++;
+    }
+  }
   MFDevice* M = &mf_plan(plan, c, dom, h);
   MFFactor fm, fp;
-  // A + c B (c > 0) is SPD: factored without pivoting
-  const double cshift = 0.05 * std::fabs(sigma);
+  // A + c B (c > 0) is SPD: factored without pivoting. c = |sigma| by default: the null space of the
+  // curl-curl operator, smeared by rounding to |lambda| <~ eps ||A|| / lambda_min(B), is damped by
+  // lambda / (lambda + c) in every application of T, and the physical modes below sigma keep
+  // |mu| = lambda / ((lambda + c)(sigma - lambda)) above the far end of a 20-pair window.
+  const double cshift = (o.damping > 0 ? o.damping : 1.0) * std::fabs(sigma);
   int delayed = 0;
   auto factor_both = [&]() {
     M->factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
@@ -639,20 +669,23 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // solves (||K|| bounded by the largest absolute row sum): a backward-stable factorization keeps it
   // near the unit roundoff whatever cond(K) is, whereas the plain residual ||b - K x|| / ||b|| cannot
   // fall below about eps * cond(K) even for an exact-in-FP64 solve.
+  // ||ka A + kb B||_inf of the pencil in use (largest absolute row sum)
+  auto pencil_norm = [&](double ka, double kb) -> double {
+    const int nblk = std::max(1, std::min<int>(c.num_sms * 4, (int)((n + 7) / 8)));
+    DBuf<double> part;
+    part.alloc_on(nblk, c.stream);
+    rowsum_max_kernel<<<nblk, 256, 0, c.stream>>>(n, d.row_ptr.p, D.va, D.vb, ka, kb, part.p);
+    c.launches++;
+    std::vector<double> hp(nblk);
+    FEM2D_CUDA(cudaMemcpyAsync(hp.data(), part.p, nblk * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+    double m = 0.0;
+    for (double v : hp) m = std::max(m, v);
+    return m;
+  };
   auto calibrate = [&](const MFFactor& fac, double ka, double kb, double& rel_out) -> int {
     const int nb = 4;
-    double knorm = 0.0;
-    {
-      const int nblk = std::max(1, std::min<int>(c.num_sms * 2, (int)((n + 255) / 256)));
-      DBuf<double> part;
-      part.alloc_on(nblk, c.stream);
-      rowsum_max_kernel<<<nblk, 256, 0, c.stream>>>(n, d.row_ptr.p, D.va, D.vb, ka, kb, part.p);
-      c.launches++;
-      std::vector<double> hp(nblk);
-      FEM2D_CUDA(cudaMemcpyAsync(hp.data(), part.p, nblk * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-      FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-      for (double v : hp) knorm = std::max(knorm, v);
-    }
+    const double knorm = pencil_norm(ka, kb);
     std::vector<double> R0;
     random_block(n, nb, 777, R0);
     DBuf<double> Rb, Xb, Tb;
@@ -686,24 +719,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     return 3;
   };
   double rel_p = 0, rel_m = 0;
-  BlockScale bsc;
-  bool blocked = false;
-  if (plan.block) {   // an earlier solve of this GEP needed the block scaling
-    bsc.build(c, h, d, sa.p, sb.p);
-    blocked = true;
-    factor_both();
-  }
   int nref_p = calibrate(fp, 1.0, cshift, rel_p);
   int nref_m = calibrate(fm, 1.0, -sigma, rel_m);
-  if ((rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense) {
-    // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
-    bsc.build(c, h, d, sa.p, sb.p);
-    blocked = true;
-    plan.block = true;
-    factor_both();
-    nref_p = calibrate(fp, 1.0, cshift, rel_p);
-    nref_m = calibrate(fm, 1.0, -sigma, rel_m);
-  }
   // small GEPs whose sparse factorization stays inaccurate after refinement (pivoting restricted to
   // each front's fully-summed rows can grow badly on indefinite pencils of ill-conditioned bases)
   // switch to one dense front with partial pivoting over all rows; the choice is kept in the plan
@@ -774,6 +791,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     return keep;
   };
 
+  const double norm_a = pencil_norm(1.0, 0.0), norm_b = pencil_norm(0.0, 1.0);
   // start block: T applied to a fixed pseudo-random block
   {
     std::vector<double> R0;
@@ -783,14 +801,24 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     FEM2D_CUDA(cudaMemcpyAsync(R.p, R0.data(), R0.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     apply_T(R.p, b, X.p, 32, b);
   }
-  std::vector<double> theta_sel, rel_sel;
+  // A pair is converged when its relative residual is below tol or its normwise backward error
+  // ||A x - theta B x|| / ((||A|| + |theta| ||B||) ||x||) is below kBackward: the pair is then exact for
+  // a pencil within 1e-14 of (A, B). With high-order monomial bases ||A|| grows as p^4 / h^2 and the
+  // relative residual attainable in FP64 rises with it; converged pairs are not expanded again (the
+  // expansion of a pair at its attainable accuracy adds only rounding noise to the basis, and noise
+  // mixing null-space and high-frequency directions yields spurious Ritz values near sigma).
+  constexpr double kBackward = 1e-14;
+  // The attainable backward error is set by the forward accuracy of the T applications, which falls
+  // with cond(A - sigma B): a pair whose residual stopped falling for two cycles while its backward
+  // error is below kStuck is converged too (its Ritz value, second order in the residual, is settled).
+  constexpr double kSame = 1e-8, kStuck = 1e-11;
+  std::vector<double> theta_sel, rel_sel, bwd_sel, theta_prev, rel_prev;
+  std::vector<int> stuck_sel, stuck_prev;
+  std::vector<uint8_t> conv_sel;
   int cycles = 0, bx = b;
   bool converged = false;
-  // stagnation guard: when the worst wanted residual has not halved for two cycles, the next cycle
-  // rebuilds the whole block Krylov space from all selected Ritz vectors (every column expanded)
-  // instead of expanding the unconverged ones only
   double best_worst = 1e300;
-  int stall = 0, stall_total = 0;
+  int stall_total = 0;
   bool attained = false;
   bool full = true;
   for (; cycles < max_cycles; cycles++) {
@@ -805,13 +833,12 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       D.copy(AX.p, 32, bx, AV.p, mmax);
       D.copy(BX.p, 32, bx, BV.p, mmax);
       m = bx;
-      std::vector<double> sel_cols;
       int u = 0;
       for (int q = 0; q < bx; q++)
-        if (rel_sel[q] >= tol) u++;
+        if (!conv_sel[q]) u++;
       std::vector<double> Gsel((size_t)bx * u, 0.0);
       for (int q = 0, k2 = 0; q < bx; q++)
-        if (rel_sel[q] >= tol) Gsel[(size_t)q * u + k2++] = 1.0;
+        if (!conv_sel[q]) Gsel[(size_t)q * u + k2++] = 1.0;
       int r = 0;
       if (u > 0) {
         // expand with T applied to the unconverged Ritz vectors: T kills their null-space part and
@@ -885,28 +912,32 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     for (int i = 0; i < m; i++)
       for (int q = 0; q < nc; q++) Ysub[(size_t)i * nc + q] = Y[(size_t)i * m2 + order[q]];
     for (int q = 0; q < nc; q++) thc[q] = th[order[q]];
-    DBuf<double> AY, BY, th_d, P;
+    DBuf<double> AY, BY, XY, th_d, P;
     AY.alloc_on((size_t)n * nc, c.stream);
     BY.alloc_on((size_t)n * nc, c.stream);
+    XY.alloc_on((size_t)n * nc, c.stream);
     D.gemm(AV.p, mmax, m, Ysub, nc, 0.0, AY.p, nc);
     D.gemm(BV.p, mmax, m, Ysub, nc, 0.0, BY.p, nc);
+    D.gemm(V.p, mmax, m, Ysub, nc, 0.0, XY.p, nc);
     th_d.upload_on(thc, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
-    P.alloc_on((size_t)nblk * 2 * nc, c.stream);
-    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AY.p, BY.p, nc, nc, th_d.p, rpb, P.p);
+    P.alloc_on((size_t)nblk * 3 * nc, c.stream);
+    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AY.p, BY.p, XY.p, nc, nc, th_d.p, rpb, P.p);
     c.launches++;
-    std::vector<double> Ph((size_t)nblk * 2 * nc);
+    std::vector<double> Ph((size_t)nblk * 3 * nc);
     FEM2D_CUDA(cudaMemcpyAsync(Ph.data(), P.p, Ph.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-    std::vector<double> rel(m2, 1e300);
+    std::vector<double> rel(m2, 1e300), bwd(m2, 1e300);
     for (int q = 0; q < nc; q++) {
-      double sr = 0, sb = 0;
+      double sr = 0, sb = 0, sx = 0;
       for (int t = 0; t < nblk; t++) {
-        sr += Ph[(size_t)t * 2 * nc + q];
-        sb += Ph[(size_t)t * 2 * nc + nc + q];
+        sr += Ph[(size_t)t * 3 * nc + q];
+        sb += Ph[(size_t)t * 3 * nc + nc + q];
+        sx += Ph[(size_t)t * 3 * nc + 2 * nc + q];
       }
       rel[order[q]] = std::sqrt(sr) / (std::fabs(thc[q]) * std::sqrt(sb) + 1e-300);
+      bwd[order[q]] = std::sqrt(sr) / ((norm_a + std::fabs(thc[q]) * norm_b) * std::sqrt(sx) + 1e-300);
     }
     std::vector<int> cand;
     for (int q = 0; q < nc; q++)
@@ -925,39 +956,64 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     D.gemm(BV.p, mmax, m, Ysel, bx, 0.0, BX.p, 32);
     theta_sel.resize(bx);
     rel_sel.resize(bx);
+    bwd_sel.resize(bx);
+    conv_sel.assign(bx, 0);
+    stuck_sel.assign(bx, 0);
     for (int q = 0; q < bx; q++) {
       theta_sel[q] = th[sel[q]];
       rel_sel[q] = rel[sel[q]];
+      bwd_sel[q] = bwd[sel[q]];
+      // the same pair (its Ritz value within kSame of one of the previous cycle) whose residual has not
+      // halved for two cycles, with a backward error below kStuck, has reached the accuracy the T
+      // applications allow
+      stuck_sel[q] = 0;
+      for (size_t p = 0; p < theta_prev.size(); p++)
+        if (std::fabs(theta_sel[q] - theta_prev[p]) <= kSame * std::fabs(theta_sel[q])) {
+          stuck_sel[q] = rel_sel[q] > 0.5 * rel_prev[p] ? stuck_prev[p] + 1 : 0;
+          break;
+        }
+      conv_sel[q] =
+          (rel_sel[q] < tol || bwd_sel[q] < kBackward || (stuck_sel[q] >= 2 && bwd_sel[q] < kStuck)) ? 1 : 0;
     }
-    double worst = 0;
-    for (int q = 0; q < k; q++) worst = std::max(worst, rel_sel[q]);
+    theta_prev = theta_sel;
+    rel_prev = rel_sel;
+    stuck_prev = stuck_sel;
+    double worst = 0, worst_bwd = 0;
+    bool all_conv = true, by_bwd = false;
+    for (int q = 0; q < k; q++) {
+      worst = std::max(worst, rel_sel[q]);
+      worst_bwd = std::max(worst_bwd, bwd_sel[q]);
+      all_conv = all_conv && conv_sel[q];
+      by_bwd = by_bwd || rel_sel[q] >= tol;
+    }
     if (o.verbose)
-      fprintf(stderr, "[gpu_solve_gep] cycle %d basis %d worst residual %.3e  theta0 %.12f\n", cycles, m, worst,
-              theta_sel[0]);
-    if (worst < tol) {
+      fprintf(stderr, "[gpu_solve_gep] cycle %d basis %d worst residual %.3e backward error %.3e theta0 %.12f\n",
+              cycles, m, worst, worst_bwd, theta_sel[0]);
+    if (o.verbose > 1)
+      for (int q = 0; q < k; q++)
+        fprintf(stderr, "    pair %2d theta %.12f residual %.3e backward error %.3e%s\n", q, theta_sel[q], rel_sel[q],
+                bwd_sel[q], conv_sel[q] ? " converged" : "");
+    if (all_conv) {
       converged = true;
+      attained = by_bwd;
       cycles++;
       break;
     }
     if (worst < 0.5 * best_worst) {
       best_worst = worst;
-      stall = 0;
       stall_total = 0;
     } else {
-      stall++;
       stall_total++;
     }
-    // attainable accuracy: with nearly dependent (high-order monomial) bases the FP64 residual floor
-    // can sit above tol; eight cycles without halving the worst residual, below 1e-6, end the solve
-    // as converged (eigenvalue errors scale with the squared residual)
+    // last resort: eight cycles without halving the worst residual, below 1e-6, end the solve as
+    // converged (eigenvalue errors scale with the squared residual)
     if (stall_total >= 8 && worst < 1e-6) {
       converged = true;
       attained = true;
       cycles++;
       break;
     }
-    full = stall >= 2;
-    if (full) stall = 0;
+    full = false;
   }
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t2 = std::chrono::steady_clock::now();
@@ -995,24 +1051,31 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     th_d.upload_on(theta_sel, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
-    P.alloc_on((size_t)nblk * 2 * bx, c.stream);
-    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AX.p, BX.p, 32, bx, th_d.p, rpb, P.p);
+    P.alloc_on((size_t)nblk * 3 * bx, c.stream);
+    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AX.p, BX.p, X.p, 32, bx, th_d.p, rpb, P.p);
     c.launches++;
-    std::vector<double> Ph((size_t)nblk * 2 * bx);
+    const double na0 = pencil_norm(1.0, 0.0), nb0 = pencil_norm(0.0, 1.0);
+    std::vector<double> Ph((size_t)nblk * 3 * bx);
     FEM2D_CUDA(cudaMemcpyAsync(Ph.data(), P.p, Ph.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
     for (int j = 0; j < bx; j++) {
-      double sr = 0, sbb = 0;
+      double sr = 0, sbb = 0, sx = 0;
       for (int q = 0; q < nblk; q++) {
-        sr += Ph[(size_t)q * 2 * bx + j];
-        sbb += Ph[(size_t)q * 2 * bx + bx + j];
+        sr += Ph[(size_t)q * 3 * bx + j];
+        sbb += Ph[(size_t)q * 3 * bx + bx + j];
+        sx += Ph[(size_t)q * 3 * bx + 2 * bx + j];
       }
       rel_sel[j] = std::sqrt(sr) / (std::fabs(theta_sel[j]) * std::sqrt(sbb) + 1e-300);
+      bwd_sel[j] = std::sqrt(sr) / ((na0 + std::fabs(theta_sel[j]) * nb0) * std::sqrt(sx) + 1e-300);
     }
     if (st) {
-      double w = 0;
-      for (int q = 0; q < k; q++) w = std::max(w, rel_sel[q]);
+      double w = 0, wb = 0;
+      for (int q = 0; q < k; q++) {
+        w = std::max(w, rel_sel[q]);
+        wb = std::max(wb, bwd_sel[q]);
+      }
       st->max_rel_residual = w;
+      st->max_backward_error = wb;
     }
   }
   // outputs: B-normalised (the Ritz vectors are B-orthonormal), sign fixed by the largest entry

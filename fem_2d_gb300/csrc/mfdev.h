@@ -60,7 +60,6 @@ struct MFPlan {
   std::unique_ptr<MFDevice> mf;
   bool ready = false;
   bool dense = false;   // a single dense front (chosen when the sparse plan's solves are inaccurate)
-  bool block = false;   // the eigensolve scales the pencil by row-run blocks (see blockscale.h)
   std::vector<uint8_t> lift;   // per DoF: levels its elimination was moved up (delayed pivots)
   int device = -1;
   std::mutex mu;

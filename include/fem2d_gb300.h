@@ -221,6 +221,11 @@ typedef struct fem2d_solve_opts {
   int block;            /* block size, 0 = default (n_pairs + guard) */
   int verbose;
   int krylov_steps;     /* block Krylov steps per restart cycle (at most 8), 0 = default 4 */
+  double damping;       /* null-space damping c / |sigma| of T = (A - sigma B)^-1 A (A + c B)^-1 B,
+                           0 = default */
+  int scaling;          /* 0 = automatic (Jacobi; row-run blocks when the Jacobi-scaled factorizations are
+                           inaccurate), 1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's
+                           diagonal blocks over runs of rows with one column list) */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {
@@ -232,9 +237,11 @@ typedef struct fem2d_solve_stats {
   int64_t spmv_count;
   int refine_spd, refine_indefinite;   /* iterative-refinement steps per solve with A + cB and A - sigma B */
   int dense_plan;      /* 1: the factorization used one dense front (small, ill-conditioned GEP) */
-  int floor_reached;   /* 1: stopped at the attainable residual floor (above tol, below 1e-6) */
+  int floor_reached;   /* 1: some pair was accepted by its backward error (below 1e-14) or at the residual
+                          floor (eight cycles without progress, below 1e-6) rather than by tol */
   int block_scaled;    /* 1: the pencil was scaled by Cholesky factors of B's row-run diagonal blocks */
   int delayed_pivots;  /* DoFs whose elimination moved to a parent front (no stable pivot in their own) */
+  double max_backward_error;  /* max over the pairs of ||Ax - lambda Bx|| / ((||A|| + |lambda| ||B||) ||x||) */
 } fem2d_solve_stats;
 
 /* gpu_solve_gep: the n_pairs eigenpairs of (A, B) nearest target, by a shift-invert block
