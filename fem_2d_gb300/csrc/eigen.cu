@@ -3,16 +3,19 @@
 // gpu_solve_gep (stands beside slepc_solve_gep, slepc_solve.rs:14-68): the n_pairs eigenpairs of
 // (A, B) nearest the target sigma among the non-spurious spectrum. The curl-curl operator has a large
 // null space (gradients, lambda = 0) which sits at distance |sigma| from the target; the reference
-// treats such modes as spurious (nalgebra_solve.rs:24-26). The search space is generated with
+// treats such modes as spurious (nalgebra_solve.rs:24-26). The pencil is first scaled by the Cholesky
+// factors of B's row-run diagonal blocks (blockscale.cu; Jacobi scaling as the fallback). The search
+// space is generated with
 //     T = (A - sigma B)^-1 A (A + c B)^-1 B
-// with c = 0.05 |sigma|: eigenvalue lambda / ((lambda - sigma)(lambda + c)), close to the plain
-// shift-invert 1 / (lambda - sigma) for every physical mode, zero on the null space (A kills it
-// whatever the accuracy of the SPD solve) and small for high-frequency modes; exact multifrontal
-// solves (mf.cu). Each cycle builds a block Krylov basis [X, TX_u, ..., T^s X_u] (s = 4 by default; X_u the
-// unconverged Ritz vectors; converged pairs are kept but not expanded), B-orthonormalised by CGS2
-// in FP64, then a Rayleigh-Ritz step on the pencil (A, B) itself (FP64); Ritz pairs with a relative
-// residual above 1 (mixtures of null-space and high-frequency directions that land near sigma) are
-// not selected. Residuals ||A x - lambda B x|| / (|lambda| ||B x||) are computed in FP64.
+// with c = |sigma|: eigenvalue lambda / ((lambda - sigma)(lambda + c)), close to the plain
+// shift-invert 1 / (lambda - sigma) for the physical modes, zero on the null space (A kills it
+// whatever the accuracy of the SPD solve; rounding smears it to small lambda, damped by
+// lambda / (lambda + c)) and small for high-frequency modes; exact multifrontal solves (mf.cu). Each
+// cycle builds a block Krylov basis [XL, X, TX, ..., T^s X] (s = 4 by default; XL the locked converged
+// pairs, X the active Ritz vectors), B-orthonormalised by CGS2 in FP64, then a Rayleigh-Ritz step on
+// the pencil (A, B) itself (FP64) over the active columns; Ritz pairs with a relative residual above 1
+// (mixtures of null-space and high-frequency directions that land near sigma) are not selected.
+// Residuals ||A x - lambda B x|| / (|lambda| ||B x||) and backward errors are computed in FP64.
 //
 // nalgebra_solve_gep (nalgebra_solve.rs:14-50) on the device: B is factored (Cholesky mode; a
 // non-positive pivot is FailedToInvertB), Z = B^-1 A is formed column block by column block, and
@@ -804,54 +807,68 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // A pair is converged when its relative residual is below tol or its normwise backward error
   // ||A x - theta B x|| / ((||A|| + |theta| ||B||) ||x||) is below kBackward: the pair is then exact for
   // a pencil within 1e-14 of (A, B). With high-order monomial bases ||A|| grows as p^4 / h^2 and the
-  // relative residual attainable in FP64 rises with it; converged pairs are not expanded again (the
-  // expansion of a pair at its attainable accuracy adds only rounding noise to the basis, and noise
-  // mixing null-space and high-frequency directions yields spurious Ritz values near sigma).
+  // relative residual attainable in FP64 rises with it.
   constexpr double kBackward = 1e-14;
   // The attainable backward error is set by the forward accuracy of the T applications, which falls
   // with cond(A - sigma B): a pair whose residual stopped falling for two cycles while its backward
   // error is below kStuck is converged too (its Ritz value, second order in the residual, is settled).
   constexpr double kSame = 1e-8, kStuck = 1e-11;
+  // Converged pairs are locked: their vectors and exact products are kept as they are, every new
+  // direction is B-orthogonalised against them, and the Rayleigh-Ritz step runs on the active part of
+  // the basis only. Locked pairs are not expanded again (the expansion of a pair at its attainable
+  // accuracy adds only rounding noise, and noise that mixes null-space and high-frequency directions
+  // yields spurious Ritz values near sigma) and do not drift through later Rayleigh-Ritz steps.
+  DBuf<double> XL, AXL, BXL;
+  for (DBuf<double>* buf : {&XL, &AXL, &BXL}) buf->alloc_on((size_t)n * 32, c.stream);
+  int nl = 0;
+  std::vector<double> theta_l, rel_l, bwd_l;
   std::vector<double> theta_sel, rel_sel, bwd_sel, theta_prev, rel_prev;
   std::vector<int> stuck_sel, stuck_prev;
-  std::vector<uint8_t> conv_sel;
   int cycles = 0, bx = b;
   bool converged = false;
   double best_worst = 1e300;
   int stall_total = 0;
   bool attained = false;
-  bool full = true;
+  // the k pairs nearest sigma among the locked and the selected active ones: (locked?, index)
+  std::vector<std::pair<int, int>> nearest;
+  auto merge_nearest = [&]() {
+    std::vector<std::pair<int, int>> all;
+    for (int j = 0; j < nl; j++) all.push_back({1, j});
+    for (int j = 0; j < bx; j++) all.push_back({0, j});
+    auto th_of = [&](const std::pair<int, int>& e) { return e.first ? theta_l[e.second] : theta_sel[e.second]; };
+    std::stable_sort(all.begin(), all.end(), [&](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+      return std::fabs(th_of(x) - sigma) < std::fabs(th_of(y) - sigma);
+    });
+    all.resize(std::min<size_t>(all.size(), (size_t)k));
+    nearest = all;
+  };
   for (; cycles < max_cycles; cycles++) {
-    int m, last0 = 0, lastn;
-    if (full) {
+    int m, last0, lastn;
+    if (cycles == 0) {
       D.copy(X.p, 32, bx, V.p, mmax);
       m = borth_new(0, bx);
+      last0 = 0;
       lastn = m;
     } else {
-      // restart from the B-orthonormal Ritz vectors (and their exact products), expand the unconverged
-      D.copy(X.p, 32, bx, V.p, mmax);
-      D.copy(AX.p, 32, bx, AV.p, mmax);
-      D.copy(BX.p, 32, bx, BV.p, mmax);
-      m = bx;
-      int u = 0;
-      for (int q = 0; q < bx; q++)
-        if (!conv_sel[q]) u++;
-      std::vector<double> Gsel((size_t)bx * u, 0.0);
-      for (int q = 0, k2 = 0; q < bx; q++)
-        if (!conv_sel[q]) Gsel[(size_t)q * u + k2++] = 1.0;
-      int r = 0;
-      if (u > 0) {
-        // expand with T applied to the unconverged Ritz vectors: T kills their null-space part and
-        // damps high-frequency content, which also pushes spurious Ritz vectors out of the basis
-        D.gemm(X.p, 32, bx, Gsel, u, 0.0, G0.p, 32);
-        apply_T(G0.p, 32, V.p + m, mmax, u);
-        r = borth_new(m, u);
+      // V = [locked | active Ritz vectors | T^j (active)]; every active vector is unconverged
+      if (nl > 0) {
+        D.copy(XL.p, 32, nl, V.p, mmax);
+        D.copy(AXL.p, 32, nl, AV.p, mmax);
+        D.copy(BXL.p, 32, nl, BV.p, mmax);
       }
+      D.copy(X.p, 32, bx, V.p + nl, mmax);
+      D.copy(AX.p, 32, bx, AV.p + nl, mmax);
+      D.copy(BX.p, 32, bx, BV.p + nl, mmax);
+      m = nl + bx;
+      // expand with T applied to the active Ritz vectors: T kills their null-space part and damps
+      // high-frequency content, which also pushes spurious Ritz vectors out of the basis
+      apply_T(X.p, 32, V.p + m, mmax, bx);
+      const int r = borth_new(m, bx);
       last0 = m;
       lastn = r;
       m += r;
     }
-    for (int st2 = (full ? 0 : 1); st2 < steps && lastn > 0 && m + lastn <= mmax; st2++) {
+    for (int st2 = (cycles == 0 ? 0 : 1); st2 < steps && lastn > 0 && m + lastn <= mmax; st2++) {
       apply_T(V.p + last0, mmax, V.p + m, mmax, lastn);
       int r = borth_new(m, lastn);
       if (r == 0) break;
@@ -859,41 +876,45 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       lastn = r;
       m += r;
     }
-    // Rayleigh-Ritz on (V^T A V, V^T B V)
+    // Rayleigh-Ritz on the active columns [nl, m): (V^T A V, V^T B V)
+    const int ma = m - nl;
+    const double* Va = V.p + nl;
+    const double* AVa = AV.p + nl;
+    const double* BVa = BV.p + nl;
     std::vector<double> GA, GB, wb, zb;
-    D.gram(V.p, mmax, m, AV.p, mmax, m, GA);
-    D.gram(V.p, mmax, m, BV.p, mmax, m, GB);
-    for (int i = 0; i < m; i++)
+    D.gram(Va, mmax, ma, AVa, mmax, ma, GA);
+    D.gram(Va, mmax, ma, BVa, mmax, ma, GB);
+    for (int i = 0; i < ma; i++)
       for (int j = 0; j < i; j++) {
-        GA[(size_t)i * m + j] = GA[(size_t)j * m + i] = 0.5 * (GA[(size_t)i * m + j] + GA[(size_t)j * m + i]);
-        GB[(size_t)i * m + j] = GB[(size_t)j * m + i] = 0.5 * (GB[(size_t)i * m + j] + GB[(size_t)j * m + i]);
+        GA[(size_t)i * ma + j] = GA[(size_t)j * ma + i] = 0.5 * (GA[(size_t)i * ma + j] + GA[(size_t)j * ma + i]);
+        GB[(size_t)i * ma + j] = GB[(size_t)j * ma + i] = 0.5 * (GB[(size_t)i * ma + j] + GB[(size_t)j * ma + i]);
       }
-    if (!symeig(m, GB, wb, zb)) fail(FEM2D_E_NOT_CONVERGED, "Gram eigen-decomposition failed");
+    if (!symeig(ma, GB, wb, zb)) fail(FEM2D_E_NOT_CONVERGED, "Gram eigen-decomposition failed");
     const double wbmax = *std::max_element(wb.begin(), wb.end());
     std::vector<int> kb;
-    for (int q = 0; q < m; q++)
+    for (int q = 0; q < ma; q++)
       if (wb[q] > 1e-12 * wbmax) kb.push_back(q);
     const int m2 = (int)kb.size();
-    std::vector<double> Wh((size_t)m * m2);   // GB^-1/2 restricted to its numerical range
-    for (int i = 0; i < m; i++)
-      for (int q = 0; q < m2; q++) Wh[(size_t)i * m2 + q] = zb[(size_t)i * m + kb[q]] / std::sqrt(wb[kb[q]]);
-    std::vector<double> S((size_t)m2 * m2, 0.0), tmp((size_t)m * m2, 0.0);
-    for (int i = 0; i < m; i++)
+    std::vector<double> Wh((size_t)ma * m2);   // GB^-1/2 restricted to its numerical range
+    for (int i = 0; i < ma; i++)
+      for (int q = 0; q < m2; q++) Wh[(size_t)i * m2 + q] = zb[(size_t)i * ma + kb[q]] / std::sqrt(wb[kb[q]]);
+    std::vector<double> S((size_t)m2 * m2, 0.0), tmp((size_t)ma * m2, 0.0);
+    for (int i = 0; i < ma; i++)
       for (int q = 0; q < m2; q++) {
         double acc = 0.0;
-        for (int k2 = 0; k2 < m; k2++) acc += GA[(size_t)i * m + k2] * Wh[(size_t)k2 * m2 + q];
+        for (int k2 = 0; k2 < ma; k2++) acc += GA[(size_t)i * ma + k2] * Wh[(size_t)k2 * m2 + q];
         tmp[(size_t)i * m2 + q] = acc;
       }
     for (int p2 = 0; p2 < m2; p2++)
       for (int q = 0; q < m2; q++) {
         double acc = 0.0;
-        for (int i = 0; i < m; i++) acc += Wh[(size_t)i * m2 + p2] * tmp[(size_t)i * m2 + q];
+        for (int i = 0; i < ma; i++) acc += Wh[(size_t)i * m2 + p2] * tmp[(size_t)i * m2 + q];
         S[(size_t)p2 * m2 + q] = acc;
       }
     std::vector<double> th, Z;
     if (!symeig(m2, S, th, Z)) fail(FEM2D_E_NOT_CONVERGED, "Rayleigh-Ritz eigen-decomposition failed");
-    std::vector<double> Y((size_t)m * m2, 0.0);
-    for (int i = 0; i < m; i++)
+    std::vector<double> Y((size_t)ma * m2, 0.0);
+    for (int i = 0; i < ma; i++)
       for (int q = 0; q < m2; q++) {
         double acc = 0.0;
         for (int k2 = 0; k2 < m2; k2++) acc += Wh[(size_t)i * m2 + k2] * Z[(size_t)k2 * m2 + q];
@@ -906,19 +927,19 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       if (std::fabs(th[j]) > spur) order.push_back(j);
     std::stable_sort(order.begin(), order.end(),
                      [&](int x, int y) { return std::fabs(th[x] - sigma) < std::fabs(th[y] - sigma); });
-    if ((int)order.size() < k) fail(FEM2D_E_SPURIOUS, "only spurious (null-space) Ritz values were found");
+    if (nl + (int)order.size() < k) fail(FEM2D_E_SPURIOUS, "only spurious (null-space) Ritz values were found");
     const int nc = std::min<int>((int)order.size(), 2 * b);
-    std::vector<double> Ysub((size_t)m * nc), thc(nc);
-    for (int i = 0; i < m; i++)
+    std::vector<double> Ysub((size_t)ma * nc), thc(nc);
+    for (int i = 0; i < ma; i++)
       for (int q = 0; q < nc; q++) Ysub[(size_t)i * nc + q] = Y[(size_t)i * m2 + order[q]];
     for (int q = 0; q < nc; q++) thc[q] = th[order[q]];
     DBuf<double> AY, BY, XY, th_d, P;
     AY.alloc_on((size_t)n * nc, c.stream);
     BY.alloc_on((size_t)n * nc, c.stream);
     XY.alloc_on((size_t)n * nc, c.stream);
-    D.gemm(AV.p, mmax, m, Ysub, nc, 0.0, AY.p, nc);
-    D.gemm(BV.p, mmax, m, Ysub, nc, 0.0, BY.p, nc);
-    D.gemm(V.p, mmax, m, Ysub, nc, 0.0, XY.p, nc);
+    D.gemm(AVa, mmax, ma, Ysub, nc, 0.0, AY.p, nc);
+    D.gemm(BVa, mmax, ma, Ysub, nc, 0.0, BY.p, nc);
+    D.gemm(Va, mmax, ma, Ysub, nc, 0.0, XY.p, nc);
     th_d.upload_on(thc, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
@@ -939,61 +960,100 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       rel[order[q]] = std::sqrt(sr) / (std::fabs(thc[q]) * std::sqrt(sb) + 1e-300);
       bwd[order[q]] = std::sqrt(sr) / ((norm_a + std::fabs(thc[q]) * norm_b) * std::sqrt(sx) + 1e-300);
     }
+    // the active block keeps b - nl vectors (at least 4): the nearest credible Ritz pairs
+    const int ba = std::max(4, b - nl);
     std::vector<int> cand;
     for (int q = 0; q < nc; q++)
       if (rel[order[q]] < 1.0) cand.push_back(order[q]);
-    if ((int)cand.size() < k) {
+    if ((int)cand.size() < std::max(1, k - nl)) {
       // not enough credible Ritz pairs yet: keep the nearest non-spurious ones regardless of residual
       cand.assign(order.begin(), order.begin() + nc);
     }
-    std::vector<int> sel(cand.begin(), cand.begin() + std::min<size_t>(cand.size(), (size_t)b));
-    bx = (int)sel.size();
-    std::vector<double> Ysel((size_t)m * bx);
-    for (int i = 0; i < m; i++)
-      for (int q = 0; q < bx; q++) Ysel[(size_t)i * bx + q] = Y[(size_t)i * m2 + sel[q]];
-    D.gemm(V.p, mmax, m, Ysel, bx, 0.0, X.p, 32);
-    D.gemm(AV.p, mmax, m, Ysel, bx, 0.0, AX.p, 32);
-    D.gemm(BV.p, mmax, m, Ysel, bx, 0.0, BX.p, 32);
-    theta_sel.resize(bx);
-    rel_sel.resize(bx);
-    bwd_sel.resize(bx);
-    conv_sel.assign(bx, 0);
-    stuck_sel.assign(bx, 0);
-    for (int q = 0; q < bx; q++) {
+    std::vector<int> sel(cand.begin(), cand.begin() + std::min<size_t>(cand.size(), (size_t)ba));
+    const int ns = (int)sel.size();
+    theta_sel.resize(ns);
+    rel_sel.resize(ns);
+    bwd_sel.resize(ns);
+    stuck_sel.assign(ns, 0);
+    std::vector<uint8_t> lock(ns, 0);
+    for (int q = 0; q < ns; q++) {
       theta_sel[q] = th[sel[q]];
       rel_sel[q] = rel[sel[q]];
       bwd_sel[q] = bwd[sel[q]];
       // the same pair (its Ritz value within kSame of one of the previous cycle) whose residual has not
       // halved for two cycles, with a backward error below kStuck, has reached the accuracy the T
       // applications allow
-      stuck_sel[q] = 0;
       for (size_t p = 0; p < theta_prev.size(); p++)
         if (std::fabs(theta_sel[q] - theta_prev[p]) <= kSame * std::fabs(theta_sel[q])) {
           stuck_sel[q] = rel_sel[q] > 0.5 * rel_prev[p] ? stuck_prev[p] + 1 : 0;
           break;
         }
-      conv_sel[q] =
-          (rel_sel[q] < tol || bwd_sel[q] < kBackward || (stuck_sel[q] >= 2 && bwd_sel[q] < kStuck)) ? 1 : 0;
+      lock[q] = (rel_sel[q] < tol || bwd_sel[q] < kBackward || (stuck_sel[q] >= 2 && bwd_sel[q] < kStuck)) ? 1 : 0;
     }
+    // newly converged pairs join the locked set (at most 32 locked vectors); the rest stay active
+    std::vector<int> to_lock, to_keep;
+    for (int q = 0; q < ns; q++) {
+      if (lock[q] && nl + (int)to_lock.size() < 32)
+        to_lock.push_back(q);
+      else
+        to_keep.push_back(q);
+    }
+    auto gather = [&](const std::vector<int>& idx, double* Xd, double* AXd, double* BXd) {
+      const int w = (int)idx.size();
+      if (w == 0) return;
+      std::vector<double> Ys((size_t)ma * w);
+      for (int i = 0; i < ma; i++)
+        for (int q = 0; q < w; q++) Ys[(size_t)i * w + q] = Y[(size_t)i * m2 + sel[idx[q]]];
+      D.gemm(Va, mmax, ma, Ys, w, 0.0, Xd, 32);
+      D.gemm(AVa, mmax, ma, Ys, w, 0.0, AXd, 32);
+      D.gemm(BVa, mmax, ma, Ys, w, 0.0, BXd, 32);
+    };
+    gather(to_lock, XL.p + nl, AXL.p + nl, BXL.p + nl);
+    for (int q : to_lock) {
+      theta_l.push_back(theta_sel[q]);
+      rel_l.push_back(rel_sel[q]);
+      bwd_l.push_back(bwd_sel[q]);
+    }
+    nl += (int)to_lock.size();
+    gather(to_keep, X.p, AX.p, BX.p);
+    {
+      std::vector<double> t2, r2, b2;
+      std::vector<int> s2;
+      for (int q : to_keep) {
+        t2.push_back(theta_sel[q]);
+        r2.push_back(rel_sel[q]);
+        b2.push_back(bwd_sel[q]);
+        s2.push_back(stuck_sel[q]);
+      }
+      theta_sel = t2;
+      rel_sel = r2;
+      bwd_sel = b2;
+      stuck_sel = s2;
+    }
+    bx = (int)to_keep.size();
     theta_prev = theta_sel;
     rel_prev = rel_sel;
     stuck_prev = stuck_sel;
+    merge_nearest();
     double worst = 0, worst_bwd = 0;
-    bool all_conv = true, by_bwd = false;
-    for (int q = 0; q < k; q++) {
-      worst = std::max(worst, rel_sel[q]);
-      worst_bwd = std::max(worst_bwd, bwd_sel[q]);
-      all_conv = all_conv && conv_sel[q];
-      by_bwd = by_bwd || rel_sel[q] >= tol;
+    bool all_locked = (int)nearest.size() == k, by_bwd = false;
+    for (const auto& e : nearest) {
+      const double r = e.first ? rel_l[e.second] : rel_sel[e.second];
+      const double bw = e.first ? bwd_l[e.second] : bwd_sel[e.second];
+      worst = std::max(worst, r);
+      worst_bwd = std::max(worst_bwd, bw);
+      all_locked = all_locked && e.first;
+      by_bwd = by_bwd || r >= tol;
     }
     if (o.verbose)
-      fprintf(stderr, "[gpu_solve_gep] cycle %d basis %d worst residual %.3e backward error %.3e theta0 %.12f\n",
-              cycles, m, worst, worst_bwd, theta_sel[0]);
+      fprintf(stderr, "[gpu_solve_gep] cycle %d basis %d (%d locked) worst residual %.3e backward error %.3e\n",
+              cycles, m, nl, worst, worst_bwd);
     if (o.verbose > 1)
-      for (int q = 0; q < k; q++)
-        fprintf(stderr, "    pair %2d theta %.12f residual %.3e backward error %.3e%s\n", q, theta_sel[q], rel_sel[q],
-                bwd_sel[q], conv_sel[q] ? " converged" : "");
-    if (all_conv) {
+      for (const auto& e : nearest)
+        fprintf(stderr, "    theta %.12f residual %.3e backward error %.3e%s\n",
+                e.first ? theta_l[e.second] : theta_sel[e.second], e.first ? rel_l[e.second] : rel_sel[e.second],
+                e.first ? bwd_l[e.second] : bwd_sel[e.second], e.first ? " locked" : "");
+    if (all_locked) {
       converged = true;
       attained = by_bwd;
       cycles++;
@@ -1013,19 +1073,27 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       cycles++;
       break;
     }
-    full = false;
+    if (bx == 0) fail(FEM2D_E_NOT_CONVERGED, "gpu_solve_gep: no active Ritz vectors left to expand");
   }
+  if (nearest.empty()) merge_nearest();
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t2 = std::chrono::steady_clock::now();
+  // the k output pairs, nearest sigma first: vectors gathered from the locked and active blocks
+  const int kout = (int)nearest.size();
+  std::vector<double> theta_out(kout), rel_out(kout), bwd_out(kout);
+  DBuf<double> XO;
+  XO.alloc_on((size_t)n * 32, c.stream);
+  for (int q = 0; q < kout; q++) {
+    const auto& e = nearest[q];
+    theta_out[q] = e.first ? theta_l[e.second] : theta_sel[e.second];
+    D.copy((e.first ? XL.p : X.p) + e.second, 32, 1, XO.p + q, 32);
+  }
   if (st) {
     st->outer_iters = cycles;
     st->inner_iters_total = (int)napply;
     st->converged = converged ? 1 : 0;
     st->t_setup_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     st->t_solve_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
-    double w = 0;
-    for (int q = 0; q < k; q++) w = std::max(w, rel_sel[q]);
-    st->max_rel_residual = w;
     st->spmv_count = spmv;
     st->refine_spd = nref_p;
     st->refine_indefinite = nref_m;
@@ -1037,42 +1105,42 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // back to the original pencil: x = D x~ (B-orthonormal), residuals in the original norms
   {
     if (blocked) {
-      bsc.unscale(c, X.p, 32, bx);
+      bsc.unscale(c, XO.p, 32, kout);
     } else {
-      const int64_t blocks = std::min<int64_t>((n * bx + 255) / 256, (int64_t)c.num_sms * 8);
-      scale_rows_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, bx, sc.p, X.p, 32);
+      const int64_t blocks = std::min<int64_t>((n * kout + 255) / 256, (int64_t)c.num_sms * 8);
+      scale_rows_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, kout, sc.p, XO.p, 32);
       c.launches++;
     }
     D.va = d.a.p;
     D.vb = d.b.p;
-    D.spmm(1.0, 0.0, X.p, 32, bx, AX.p, 32);
-    D.spmm(0.0, 1.0, X.p, 32, bx, BX.p, 32);
+    D.spmm(1.0, 0.0, XO.p, 32, kout, AX.p, 32);
+    D.spmm(0.0, 1.0, XO.p, 32, kout, BX.p, 32);
     DBuf<double> th_d, P;
-    th_d.upload_on(theta_sel, c.stream);
+    th_d.upload_on(theta_out, c.stream);
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
-    P.alloc_on((size_t)nblk * 3 * bx, c.stream);
-    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AX.p, BX.p, X.p, 32, bx, th_d.p, rpb, P.p);
+    P.alloc_on((size_t)nblk * 3 * kout, c.stream);
+    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AX.p, BX.p, XO.p, 32, kout, th_d.p, rpb, P.p);
     c.launches++;
     const double na0 = pencil_norm(1.0, 0.0), nb0 = pencil_norm(0.0, 1.0);
-    std::vector<double> Ph((size_t)nblk * 3 * bx);
+    std::vector<double> Ph((size_t)nblk * 3 * kout);
     FEM2D_CUDA(cudaMemcpyAsync(Ph.data(), P.p, Ph.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-    for (int j = 0; j < bx; j++) {
+    for (int j = 0; j < kout; j++) {
       double sr = 0, sbb = 0, sx = 0;
       for (int q = 0; q < nblk; q++) {
-        sr += Ph[(size_t)q * 3 * bx + j];
-        sbb += Ph[(size_t)q * 3 * bx + bx + j];
-        sx += Ph[(size_t)q * 3 * bx + 2 * bx + j];
+        sr += Ph[(size_t)q * 3 * kout + j];
+        sbb += Ph[(size_t)q * 3 * kout + kout + j];
+        sx += Ph[(size_t)q * 3 * kout + 2 * kout + j];
       }
-      rel_sel[j] = std::sqrt(sr) / (std::fabs(theta_sel[j]) * std::sqrt(sbb) + 1e-300);
-      bwd_sel[j] = std::sqrt(sr) / ((na0 + std::fabs(theta_sel[j]) * nb0) * std::sqrt(sx) + 1e-300);
+      rel_out[j] = std::sqrt(sr) / (std::fabs(theta_out[j]) * std::sqrt(sbb) + 1e-300);
+      bwd_out[j] = std::sqrt(sr) / ((na0 + std::fabs(theta_out[j]) * nb0) * std::sqrt(sx) + 1e-300);
     }
     if (st) {
       double w = 0, wb = 0;
-      for (int q = 0; q < k; q++) {
-        w = std::max(w, rel_sel[q]);
-        wb = std::max(wb, bwd_sel[q]);
+      for (int q = 0; q < kout; q++) {
+        w = std::max(w, rel_out[q]);
+        wb = std::max(wb, bwd_out[q]);
       }
       st->max_rel_residual = w;
       st->max_backward_error = wb;
@@ -1080,11 +1148,11 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   }
   // outputs: B-normalised (the Ritz vectors are B-orthonormal), sign fixed by the largest entry
   std::vector<double> Xh((size_t)n * 32);
-  FEM2D_CUDA(cudaMemcpyAsync(Xh.data(), X.p, Xh.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  FEM2D_CUDA(cudaMemcpyAsync(Xh.data(), XO.p, Xh.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-  for (int q = 0; q < k; q++) {
-    if (values) values[q] = theta_sel[q];
-    if (residuals) residuals[q] = rel_sel[q];
+  for (int q = 0; q < kout; q++) {
+    if (values) values[q] = theta_out[q];
+    if (residuals) residuals[q] = rel_out[q];
     if (vectors) {
       int64_t imax = 0;
       for (int64_t i = 0; i < n; i++)
