@@ -810,8 +810,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // relative residual attainable in FP64 rises with it.
   constexpr double kBackward = 1e-14;
   // The attainable backward error is set by the forward accuracy of the T applications, which falls
-  // with cond(A - sigma B): a pair whose residual stopped falling for two cycles while its backward
-  // error is below kStuck is converged too (its Ritz value, second order in the residual, is settled).
+  // with cond(A - sigma B): a pair whose residual stopped falling for one cycle with a backward error
+  // below kStuck / 10, or for two cycles below kStuck, is converged too (its Ritz value, second order
+  // in the residual, is settled).
   constexpr double kSame = 1e-8, kStuck = 1e-11;
   // Converged pairs are locked: their vectors and exact products are kept as they are, every new
   // direction is B-orthogonalised against them, and the Rayleigh-Ritz step runs on the active part of
@@ -988,7 +989,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
           stuck_sel[q] = rel_sel[q] > 0.5 * rel_prev[p] ? stuck_prev[p] + 1 : 0;
           break;
         }
-      lock[q] = (rel_sel[q] < tol || bwd_sel[q] < kBackward || (stuck_sel[q] >= 2 && bwd_sel[q] < kStuck)) ? 1 : 0;
+      lock[q] = (rel_sel[q] < tol || bwd_sel[q] < kBackward || (stuck_sel[q] >= 1 && bwd_sel[q] < 0.1 * kStuck) ||
+                 (stuck_sel[q] >= 2 && bwd_sel[q] < kStuck))
+                    ? 1
+                    : 0;
     }
     // newly converged pairs join the locked set (at most 32 locked vectors); the rest stay active
     std::vector<int> to_lock, to_keep;

@@ -95,7 +95,9 @@ def test_batch_concurrent_solves(oracle_lib, ctx, family):
     for k, g, r in zip(pick, geps, res):
         one = fg.gpu_solve_gep_n(g, 10.0, 4)
         assert np.allclose(r.values, one.values, rtol=1e-12, atol=0)
-        assert np.max(r.residuals) < 1e-9
+        # converged by relative residual, or by normwise backward error (monomial bases of order 8 put
+        # the attainable relative residual near 1e-9)
+        assert np.max(r.residuals) < 1e-9 or r.stats["max_backward_error"] < 1e-12
         if g.dimension <= 2500:
             A, B = g.scipy()
             w, _ = oracle_lib.dense_nearest_physical(A, B, 10.0, 4)
