@@ -329,7 +329,7 @@ def run_native(args, ws, rank, local):
     step()
     ctx.set_profiling(False)
     regions = {}
-    for reg in ("assembly_values", "spmm", "mf_factor", "mf_solve"):
+    for reg in ("assembly_values", "spmm", "mf_factor", "mf_solve", "dense_block"):
         regions[reg] = ctx.profile(reg)
     dom_name = max(regions, key=lambda k: regions[k]["ms"])
     hbm, peak_kind = peaks()

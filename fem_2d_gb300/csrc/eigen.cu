@@ -424,6 +424,7 @@ struct Dev {
   }
   // C (a x b, host row-major) = X^T Y
   void gram(const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b, std::vector<double>& C) {
+    ProfScope ps(c, "dense_block", 8.0 * h.n * (a + b), 2.0 * h.n * a * b);
     const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
     const int64_t rpb = (h.n + nblk - 1) / nblk;
     const int ab = a * b;
@@ -444,6 +445,7 @@ struct Dev {
   void gemm(const double* X, int64_t ldx, int a, const std::vector<double>& C, int b, double beta, double* Z,
             int64_t ldz) {
     if (a <= 0 || b <= 0) return;
+    ProfScope ps(c, "dense_block", 8.0 * h.n * (a + (beta != 0.0 ? 2.0 : 1.0) * b), 2.0 * h.n * a * b);
     const int chunk = std::max(1, std::min(b, (int)((96 * 1024) / (sizeof(double) * a))));
     std::vector<double> Ct;
     for (int j0 = 0; j0 < b; j0 += chunk) {
@@ -467,6 +469,7 @@ struct Dev {
   }
   // C (a x b, device, row-major) = X^T Y without leaving the device
   void gram_dev(const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b, double* Cd) {
+    ProfScope ps(c, "dense_block", 8.0 * h.n * (a + b), 2.0 * h.n * a * b);
     const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
     const int64_t rpb = (h.n + nblk - 1) / nblk;
     const int ab = a * b;
@@ -483,6 +486,7 @@ struct Dev {
   void gemm_dev(const double* X, int64_t ldx, int a, const double* Cd, int b, double alpha, double beta, double* Z,
                 int64_t ldz) {
     if (a <= 0 || b <= 0) return;
+    ProfScope ps(c, "dense_block", 8.0 * h.n * (a + (beta != 0.0 ? 2.0 : 1.0) * b), 2.0 * h.n * a * b);
     const size_t smem = (size_t)a * b * sizeof(double);
     if (smem > 96 * 1024) fail(FEM2D_E_INVALID_ARG, "device-resident projection block too large");
     const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
