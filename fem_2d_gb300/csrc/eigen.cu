@@ -747,28 +747,37 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     spmv += 2 * nb;
     napply += nb;
   };
-  // W = V[:, m0:m0+r]: B-orthogonalise against V[:, :m0] (CGS2, B*W tracked linearly), orthonormalise
-  // within the block (eigen-decomposition of its Gram matrix, rank-revealing), then store the exact
-  // products A*W and B*W in AV and BV. Returns the number of columns kept.
+  // W = V[:, m0:m0+r]: B-orthogonalise against V[:, :m0] (CGS2 with the stored B V), form B W once,
+  // orthonormalise within the block (eigen-decomposition of its Gram matrix, rank-revealing; the same
+  // transforms applied to B W), then store the exact product A*W in AV and B*W in BV. Returns the number
+  // of columns kept. Per new column: one product with B and one with A.
   DBuf<double> Cproj;
   Cproj.alloc_on((size_t)mmax * 32, c.stream);
   auto borth_new = [&](int m0, int r) -> int {
     if (r <= 0) return 0;
     double* Wb = V.p + m0;
     double* BWb = BV.p + m0;
-    D.spmm(0.0, 1.0, Wb, mmax, r, BWb, mmax);
-    spmv += r;
     std::vector<double> G, w, z;
-    // W -= V (V^T B W), B W -= (B V)(V^T B W): coefficients stay on the device (no host round trip)
+    // W -= V ((B V)^T W): the first two CGS passes need no product with B (the basis carries B V);
+    // coefficients stay on the device (no host round trip)
+    auto project_w = [&](int cols) {
+      D.gram_dev(BV.p, mmax, m0, Wb, mmax, cols, Cproj.p);
+      D.gemm_dev(V.p, mmax, m0, Cproj.p, cols, -1.0, 1.0, Wb, mmax);
+    };
+    // W -= V (V^T B W), B W -= (B V)(V^T B W): B W tracked linearly through a late, small correction
     auto project = [&](int cols) {
       D.gram_dev(V.p, mmax, m0, BWb, mmax, cols, Cproj.p);
       D.gemm_dev(V.p, mmax, m0, Cproj.p, cols, -1.0, 1.0, Wb, mmax);
       D.gemm_dev(BV.p, mmax, m0, Cproj.p, cols, -1.0, 1.0, BWb, mmax);
     };
     if (m0 > 0) {
-      project(r);
-      project(r);
+      project_w(r);
+      project_w(r);
     }
+    // the exact product of the projected block; the orthonormalising transforms below are applied to
+    // W and B W alike
+    D.spmm(0.0, 1.0, Wb, mmax, r, BWb, mmax);
+    spmv += r;
     int keep = r;
     for (int pass = 0; pass < 2; pass++) {
       D.gram(Wb, mmax, keep, BWb, mmax, keep, G);
@@ -792,9 +801,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       keep = nk;
       if (pass == 0 && m0 > 0) project(keep);
     }
-    D.spmm(0.0, 1.0, Wb, mmax, keep, BWb, mmax);
     D.spmm(1.0, 0.0, Wb, mmax, keep, AV.p + m0, mmax);
-    spmv += 2 * keep;
+    spmv += keep;
     return keep;
   };
 

@@ -557,7 +557,10 @@ __device__ __forceinline__ void forward_small_front(int fr, const SolveArgs& a, 
   }
 }
 
-__global__ void __launch_bounds__(256) mf_forward_small_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
+// NT threads per front: 256 for wide levels, 1024 for the narrow upper levels of the tree, where a
+// few fronts occupy the GPU and each front's dependent dot products set the level's latency
+template <int NT>
+__global__ void __launch_bounds__(NT) mf_forward_small_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
   extern __shared__ double sm[];
   forward_small_front(lf[blockIdx.x], a, sm);
 }
@@ -599,7 +602,8 @@ __device__ __forceinline__ void backward_small_front(int fr, const SolveArgs& a,
   }
 }
 
-__global__ void __launch_bounds__(256) mf_backward_small_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT) mf_backward_small_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
   extern __shared__ double sm[];
   backward_small_front(lf[blockIdx.x], a, sm);
 }
@@ -827,9 +831,13 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
   if (c.device >= 0 && c.device < 256 && !attr_done[c.device]) {
     FEM2D_CUDA(cudaFuncSetAttribute(mf_invdiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmallP * kSmallP * (int)sizeof(double)));
-    FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
-    FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kSmallF * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmallF * 32 * (int)sizeof(double)));
     attr_done[c.device] = true;
   }
@@ -948,7 +956,10 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)(level_small_f[l] + level_small_p[l]) * nb * sizeof(double);
-      mf_forward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
+      if (2 * ns <= c.num_sms)
+        mf_forward_small_kernel<1024><<<ns, 1024, smem, st>>>(lsmall.p + small_ptr[l], a);
+      else
+        mf_forward_small_kernel<256><<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
       c.launches++;
     }
     if (nl > 0) {
@@ -962,7 +973,10 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)level_small_f[l] * nb * sizeof(double);
-      mf_backward_small_kernel<<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
+      if (2 * ns <= c.num_sms)
+        mf_backward_small_kernel<1024><<<ns, 1024, smem, st>>>(lsmall.p + small_ptr[l], a);
+      else
+        mf_backward_small_kernel<256><<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
       c.launches++;
     }
     if (nl > 0) {
