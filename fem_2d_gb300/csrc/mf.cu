@@ -608,6 +608,127 @@ __global__ void __launch_bounds__(NT) mf_backward_small_kernel(const int32_t* __
   backward_small_front(lf[blockIdx.x], a, sm);
 }
 
+// The narrow upper levels of the tree hold a few fronts each, and GB300's FP64 rate per SM (about two
+// FMA per clock) makes one CTA per front the bottleneck there: these variants spread one front over a
+// cluster of CL CTAs (CL SMs). Every CTA gathers the front's right-hand side (cheap) and owns a
+// contiguous slice of its rows; the block that all rows need (y of the forward pass, z of the backward
+// pass) is exchanged through the front's workspace in global memory across one cluster barrier (cluster
+// scope orders the global writes before the reads).
+__device__ __forceinline__ void row_slice(int rows, int r, int& r0, int& r1) {
+  const int per = (rows + CL - 1) / CL;
+  r0 = min(rows, r * per);
+  r1 = min(rows, r0 + per);
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
+    mf_forward_small_cluster_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
+  extern __shared__ double sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int fr = lf[blockIdx.x / CL];
+  const FrontDesc* __restrict__ fd = a.fd;
+  const int32_t* __restrict__ emap = a.emap;
+  const int32_t* __restrict__ ipm = a.iperm + a.piv_off[fr];
+  const int32_t* __restrict__ pm = a.perm + a.piv_off[fr];
+  const int nb = a.nb;
+  const FrontDesc d = fd[fr];
+  const int f = d.f, p = d.p, s = f - p;
+  double* v = sm;            // v[c * f + i]: the whole gathered right-hand side
+  double* y = sm + f * nb;   // y[c * p + i]: the whole pivot block after the exchange
+  const int32_t* D = a.dofs + d.dptr;
+  const double* A = a.F + d.off;
+  double* out = a.W + a.woff[fr];
+  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) v[t] = 0.0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    atomicAdd(v + c * f + i, a.B[(int64_t)D[pm[i]] * a.ldb + c]);
+  }
+  for (int slot = 0; slot < MAXKIDS; slot++) {
+    const int ch = d.kid[slot];
+    if (ch < 0) continue;
+    const FrontDesc cd = fd[ch];
+    const int sz = cd.f - cd.p;
+    const double* cw = a.W + a.woff[ch];
+    const int32_t* m = emap + cd.eptr;
+    for (int t = threadIdx.x; t < sz * nb; t += blockDim.x) {
+      const int i = t % sz, c = t / sz;
+      const int mi = m[i];
+      const int row = mi < p ? ipm[mi] : mi;
+      atomicAdd(v + c * f + row, cw[(int64_t)c * cd.f + cd.p + i]);
+    }
+  }
+  __syncthreads();
+  // y = L11^-1 v[0:p] for this CTA's slice of pivot rows, straight into the workspace
+  int r0, r1;
+  row_slice(p, r, r0, r1);
+  const int pr = r1 - r0;
+  for (int t = threadIdx.x; t < pr * nb; t += blockDim.x) {
+    const int i = r0 + t % pr, c = t / pr;
+    const double* vc = v + c * f;
+    out[(int64_t)c * f + i] = vc[i] + col_dot(A + i, f, vc, 0, i);
+  }
+  cluster.sync();
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    y[c * p + i] = out[(int64_t)c * f + i];
+  }
+  __syncthreads();
+  // out[p:f] = v[p:f] - L21 y for this CTA's slice of the remaining rows
+  row_slice(s, r, r0, r1);
+  const int sr = r1 - r0;
+  for (int t = threadIdx.x; t < sr * nb; t += blockDim.x) {
+    const int i = p + r0 + t % sr, c = t / sr;
+    const double* yc = y + c * p;
+    out[(int64_t)c * f + i] = v[c * f + i] - col_dot(A + i, f, yc, 0, p);
+  }
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
+    mf_backward_small_cluster_kernel(const int32_t* __restrict__ lf, SolveArgs a) {
+  extern __shared__ double sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int fr = lf[blockIdx.x / CL];
+  const int nb = a.nb;
+  const FrontDesc d = a.fd[fr];
+  const int f = d.f, p = d.p;
+  if (p == 0) return;   // uniform over the cluster: every CTA of it leaves before any barrier
+  const int s = f - p;
+  double* xs = sm;            // xs[c * s + j]: solved struct unknowns
+  double* z = sm + s * nb;    // z[c * p + i]: the whole pivot block after the exchange
+  const int32_t* D = a.dofs + d.dptr;
+  const double* A = a.F + d.off;
+  double* v = a.W + a.woff[fr];
+  for (int t = threadIdx.x; t < s * nb; t += blockDim.x) {
+    const int j = t % s, c = t / s;
+    xs[t] = a.X[(int64_t)D[p + j] * a.ldx + c];
+  }
+  __syncthreads();
+  // z = y - U12 xs for this CTA's slice of pivot rows, in place over y in the workspace (each row is
+  // read and written by its owner only before the barrier)
+  int r0, r1;
+  row_slice(p, r, r0, r1);
+  const int pr = r1 - r0;
+  for (int t = threadIdx.x; t < pr * nb; t += blockDim.x) {
+    const int i = r0 + t % pr, c = t / pr;
+    const double* xc = xs + c * s;
+    v[(int64_t)c * f + i] = v[(int64_t)c * f + i] - col_dot(A + (int64_t)p * f + i, f, xc, 0, s);
+  }
+  cluster.sync();
+  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
+    const int i = t % p, c = t / p;
+    z[c * p + i] = v[(int64_t)c * f + i];
+  }
+  __syncthreads();
+  // x = U11^-1 z for the same slice
+  for (int t = threadIdx.x; t < pr * nb; t += blockDim.x) {
+    const int i = r0 + t % pr, c = t / pr;
+    const double* zc = z + c * p;
+    a.X[(int64_t)D[i] * a.ldx + c] = col_dot(A + i, f, zc, i, p);
+  }
+}
+
 // X = Kinv B for a dense inverse (n x n, row-major): one warp per row, lane c owns right-hand side c;
 // four accumulators keep the inverse-row and B-row loads in flight
 __global__ void __launch_bounds__(256) dense_inverse_apply_kernel(int64_t n, const double* __restrict__ Kinv,
@@ -839,6 +960,10 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
                                     kSmallF * 32 * (int)sizeof(double)));
     FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmallF * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kSmallF * 32 * (int)sizeof(double)));
     attr_done[c.device] = true;
   }
 }
@@ -956,7 +1081,9 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)(level_small_f[l] + level_small_p[l]) * nb * sizeof(double);
-      if (2 * ns <= c.num_sms)
+      if (ns * CL <= 2 * c.num_sms)
+        mf_forward_small_cluster_kernel<<<ns * CL, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
+      else if (2 * ns <= c.num_sms)
         mf_forward_small_kernel<1024><<<ns, 1024, smem, st>>>(lsmall.p + small_ptr[l], a);
       else
         mf_forward_small_kernel<256><<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
@@ -973,7 +1100,9 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)level_small_f[l] * nb * sizeof(double);
-      if (2 * ns <= c.num_sms)
+      if (ns * CL <= 2 * c.num_sms)
+        mf_backward_small_cluster_kernel<<<ns * CL, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
+      else if (2 * ns <= c.num_sms)
         mf_backward_small_kernel<1024><<<ns, 1024, smem, st>>>(lsmall.p + small_ptr[l], a);
       else
         mf_backward_small_kernel<256><<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
