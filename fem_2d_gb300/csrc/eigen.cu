@@ -599,14 +599,19 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
     if (hb) fail(FEM2D_E_B_NOT_SPD, "B has a non-positive diagonal entry");
   }
-  // Row-run block scaling (default): S = blockdiag(L_g^-1) over runs of rows with one column list, L_g the
-  // Cholesky factor of B's diagonal block of run g; S A S^T and S B S^T keep the pattern, their diagonal
-  // blocks of B become identities, and cond(B) drops by orders of magnitude for monomial bases, which
-  // lowers the forward error of every shifted solve. A run block that is not numerically positive
-  // definite falls back to the Jacobi scaling (unless the block scaling was asked for).
+  // Row-run block scaling (default from kLargeN DoFs): S = blockdiag(L_g^-1) over runs of rows with one
+  // column list, L_g the Cholesky factor of B's diagonal block of run g; S A S^T and S B S^T keep the
+  // pattern, their diagonal blocks of B become identities, and cond(B) drops by orders of magnitude for
+  // monomial bases, which lowers the forward error of every shifted solve. A run block that is not
+  // numerically positive definite falls back to the Jacobi scaling (unless the block scaling was asked
+  // for). Below kLargeN DoFs the Jacobi scaling is kept unless the factorizations prove inaccurate
+  // (below): there the rounding smear of the null space is small and the block set-up would cost more
+  // than the solve gains (about 8 ms per solve at 2-4k DoFs).
+  constexpr int64_t kLargeN = 10000;
+  const bool large = n >= kLargeN;
   BlockScale bsc;
   bool blocked = false;
-  if (o.scaling != 1) {
+  if (o.scaling == 2 || (o.scaling == 0 && large)) {
     try {
       bsc.build(c, h, d, sa.p, sb.p);
       blocked = true;
@@ -618,11 +623,13 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   }
   MFDevice* M = &mf_plan(plan, c, dom, h);
   MFFactor fm, fp;
-  // A + c B (c > 0) is SPD: factored without pivoting. c = |sigma| by default: the null space of the
-  // curl-curl operator, smeared by rounding to |lambda| <~ eps ||A|| / lambda_min(B), is damped by
-  // lambda / (lambda + c) in every application of T, and the physical modes below sigma keep
-  // |mu| = lambda / ((lambda + c)(sigma - lambda)) above the far end of a 20-pair window.
-  const double cshift = (o.damping > 0 ? o.damping : 1.0) * std::fabs(sigma);
+  // A + c B (c > 0) is SPD: factored without pivoting. c = |sigma| by default from kLargeN DoFs: the null
+  // space of the curl-curl operator, smeared by rounding to |lambda| <~ eps ||A|| / lambda_min(B) (which
+  // grows with p^4 / h^2), is damped by lambda / (lambda + c) in every application of T, and the
+  // physical modes below sigma keep |mu| = lambda / ((lambda + c)(sigma - lambda)) above the far end of
+  // a 20-pair window. Smaller GEPs keep c = 0.05 |sigma| (their smear is negligible and the modes below
+  // sigma converge faster).
+  const double cshift = (o.damping > 0 ? o.damping : (large ? 1.0 : 0.05)) * std::fabs(sigma);
   int delayed = 0;
   auto factor_both = [&]() {
     M->factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
@@ -728,6 +735,22 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   double rel_p = 0, rel_m = 0;
   int nref_p = calibrate(fp, 1.0, cshift, rel_p);
   int nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+  if ((rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense && o.scaling == 0) {
+    // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
+    try {
+      bsc.build(c, h, d, sa.p, sb.p);
+      blocked = true;
+      factor_both();
+      nref_p = calibrate(fp, 1.0, cshift, rel_p);
+      nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+    } catch (const Error&) {
+      scale_csr_kernel<<<(int)jblocks, 256, 0, c.stream>>>(n, d.row_ptr.p, d.col.p, d.a.p, d.b.p, sc.p, sa.p, sb.p);
+      c.launches++;
+      factor_both();
+      nref_p = calibrate(fp, 1.0, cshift, rel_p);
+      nref_m = calibrate(fm, 1.0, -sigma, rel_m);
+    }
+  }
   // small GEPs whose sparse factorization stays inaccurate after refinement (pivoting restricted to
   // each front's fully-summed rows can grow badly on indefinite pencils of ill-conditioned bases)
   // switch to one dense front with partial pivoting over all rows; the choice is kept in the plan

@@ -222,10 +222,11 @@ typedef struct fem2d_solve_opts {
   int verbose;
   int krylov_steps;     /* block Krylov steps per restart cycle (at most 8), 0 = default 4 */
   double damping;       /* null-space damping c / |sigma| of T = (A - sigma B)^-1 A (A + c B)^-1 B,
-                           0 = default */
-  int scaling;          /* 0 = automatic (Jacobi; row-run blocks when the Jacobi-scaled factorizations are
-                           inaccurate), 1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's
-                           diagonal blocks over runs of rows with one column list) */
+                           0 = default (1 from 10,000 DoFs, 0.05 below) */
+  int scaling;          /* 0 = automatic (row-run blocks from 10,000 DoFs; below, Jacobi, switching to
+                           row-run blocks when the Jacobi-scaled factorizations are inaccurate),
+                           1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's diagonal blocks
+                           over runs of rows with one column list) */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {
