@@ -574,7 +574,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   if (b < k) b = k;
   if (b > 32) fail(FEM2D_E_INVALID_ARG, "block size above 32 (n_pairs too large for one block)");
   const int steps = o.krylov_steps > 0 ? std::min(o.krylov_steps, 8) : 4;
-  const int mmax = b * (steps + 1);
+  // basis columns: the Krylov space of a cycle, and room for up to 32 locked pairs, a 32-column active
+  // block and its first expansion (96) whatever the block size
+  const int mmax = std::max(b * (steps + 1), 96);
   const double tol = o.tol > 0 ? o.tol : 1e-10;
   const int max_cycles = o.max_outer > 0 ? o.max_outer : 40;
   const double spur = 1e-6 * std::max(1.0, std::fabs(sigma));
@@ -896,6 +898,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       D.copy(AX.p, 32, bx, AV.p + nl, mmax);
       D.copy(BX.p, 32, bx, BV.p + nl, mmax);
       m = nl + bx;
+      if (m + bx > mmax) fail(FEM2D_E_NOT_CONVERGED, "gpu_solve_gep: basis capacity exceeded");
       // expand with T applied to the active Ritz vectors: T kills their null-space part and damps
       // high-frequency content, which also pushes spurious Ritz vectors out of the basis
       apply_T(X.p, 32, V.p + m, mmax, bx);

@@ -60,3 +60,16 @@ def test_hierpoly_repeat_solve_is_stable(ctx):
     again = fg.gpu_solve_gep_n(g, 10.0, 20)
     assert again.stats["converged"]
     assert np.allclose(np.sort(first.values), np.sort(again.values), rtol=1e-11, atol=0)
+
+
+def test_scaling_and_damping_options_agree(ctx):
+    """Jacobi and row-run block scaling, and the two damping regimes, reach the same eigenvalues."""
+    w = configs.precision(seed=1, nx=8, ny=4)
+    d = fg.Domain.from_mesh(configs.build_mesh(w))
+    g = fg.galerkin_sample_gep_hcurl(fg.KOLeg, fg.CurlCurl, fg.L2Inner, d, [10, 10], ctx=ctx)
+    runs = [fg.gpu_solve_gep_n(g, 10.0, 6, scaling=sc, damping=dm) for sc in (1, 2) for dm in (0.05, 1.0)]
+    ref = np.sort(runs[0].values)
+    for r in runs:
+        assert r.stats["converged"]
+        assert np.allclose(np.sort(r.values), ref, rtol=1e-11, atol=0)
+    assert [r.stats["block_scaled"] for r in runs] == [0, 0, 1, 1]
