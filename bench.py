@@ -310,13 +310,24 @@ def run_native(args, ws, rank, local):
     # end to end through the public API from host data
     e2e_ms = 0.0
     h2d = d2h = 0
+    parts = {}
     for _ in range(max(1, args.steps)):
         ctx.synchronize()
         t0 = time.perf_counter()
         d2 = fg.Domain.from_mesh(mesh)
+        t1 = time.perf_counter()
         g2 = fg.galerkin_sample_gep_hcurl(bs, fg.CurlCurl, fg.L2Inner, d2, list(w.glq), ctx=ctx)
+        t2 = time.perf_counter()
         r2 = fg.gpu_solve_gep_n(g2, w.target, w.n_pairs)
-        e2e_ms += 1e3 * (time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        e2e_ms += 1e3 * (t3 - t0)
+        tg = g2.timings()
+        # the last iteration's phases (ms): host DoF enumeration, GEP construction (host symbolic
+        # phase, uploads, device assembly), solve set-up (factorization plan, scaling, factorizations)
+        # and Krylov phase, download included in the solve
+        parts = {"domain_ms": 1e3 * (t1 - t0), "gep_ms": 1e3 * (t2 - t1), "gep_symbolic_ms": float(tg[3]),
+                 "gep_upload_ms": float(tg[4]), "gep_assembly_ms": float(tg[2]), "solve_ms": 1e3 * (t3 - t2),
+                 "solve_setup_ms": r2.stats["t_setup_ms"], "solve_krylov_ms": r2.stats["t_solve_ms"]}
         h2d = g2.h2d_bytes + 8 * n * (w.n_pairs + max(4, w.n_pairs // 2))
         d2h = 8 * w.n_pairs * (n + 2)
         del g2, d2, r2
@@ -374,7 +385,7 @@ def run_native(args, ws, rank, local):
            "t_assembly_s": t_asm / args.steps / 1e3, "t_eigensolve_s": t_eig / args.steps / 1e3,
            "wall_s_timed": wall, "gpu_launches": launches,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                   "ms_per_step": e2e_ms},
+                   "ms_per_step": e2e_ms, "phases": parts},
            "roofline": roofline, "region_ms_profiled": share,
            "region_rooflines": {k: roof(k) for k in regions if k != dom_name},
            "solve_stats": res.stats if res is not None else None,

@@ -504,7 +504,8 @@ class GEP:
         _check(lib().fem2d_gep_recompute(self.ctx._h, self._h))
 
     def timings(self):
-        out = np.zeros(3)
+        """[tables, values, tables + values] ms of the last assembly, then [host symbolic, upload] ms."""
+        out = np.zeros(5)
         _check(lib().fem2d_gep_timings(self._h, _ptr(out, ctypes.c_double)))
         return out
 

@@ -579,6 +579,8 @@ int fem2d_gep_timings(const fem2d_gep* g, double* out) {
   out[0] = g->t_tables_ms;
   out[1] = g->t_values_ms;
   out[2] = g->t_tables_ms + g->t_values_ms;
+  out[3] = g->t_symbolic_ms;
+  out[4] = g->t_upload_ms;
   API_END
 }
 

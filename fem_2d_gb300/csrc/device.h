@@ -100,11 +100,13 @@ struct DBuf {
     n = count;
     st = s;
   }
-  void upload_on(const std::vector<T>& v, cudaStream_t s) {
+  template <class Alloc>
+  void upload_on(const std::vector<T, Alloc>& v, cudaStream_t s) {
     alloc_on(v.size(), s);
     if (!v.empty()) FEM2D_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
   }
-  void upload(const std::vector<T>& v, cudaStream_t s) {
+  template <class Alloc>
+  void upload(const std::vector<T, Alloc>& v, cudaStream_t s) {
     alloc(v.size());
     if (!v.empty()) FEM2D_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
   }

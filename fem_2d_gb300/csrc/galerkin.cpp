@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <thread>
 
 #include "common.h"
@@ -38,6 +39,18 @@ static void parallel_for(int64_t n, F f) {
     if (a >= b) break;
     th.emplace_back([=]() { f(a, b); });
   }
+  for (auto& x : th) x.join();
+}
+
+// f(t) on nt threads (t = 0..nt-1), inline when nt == 1
+template <class F>
+static void run_threads(int nt, F f) {
+  if (nt <= 1) {
+    f(0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; t++) th.emplace_back([=]() { f(t); });
   for (auto& x : th) x.join();
 }
 
@@ -176,10 +189,10 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   const int64_t V = voff[nb];
   g.visits = V;
 
-  // ---- bucket visits by key row
+  // ---- bucket visits by key row: each thread counts the rows of a contiguous range of blocks (ranges
+  // balanced by visit count), per-row offsets are laid out thread by thread, then each thread writes
+  // its own positions (no atomics; the per-row sort below makes the order canonical)
   const int64_t n = d.ndofs;
-  std::vector<std::atomic<int64_t>> cnt(n + 1);
-  for (auto& c : cnt) c.store(0, std::memory_order_relaxed);
   auto visit_block = [&](int64_t b, auto&& emit) {
     const BInfo& bi = binfo[b];
     const Spec* P = &d.specs[d.spec_ptr[bi.p]];
@@ -193,23 +206,46 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
         for (int64_t k = 0; k < nq; k++) emit(P[i].dof, Q[k].dof, (uint32_t)i, (uint32_t)k);
     }
   };
-  parallel_for(nb, [&](int64_t b0, int64_t b1) {
-    for (int64_t b = b0; b < b1; b++)
-      visit_block(b, [&](int32_t dp, int32_t dq, uint32_t, uint32_t) {
-        cnt[std::min(dp, dq)].fetch_add(1, std::memory_order_relaxed);
-      });
+  const int nt = (V < 65536 || num_host_threads() <= 1) ? 1 : num_host_threads();
+  std::vector<int64_t> brange(nt + 1, 0);
+  for (int t = 1; t < nt; t++) {
+    const int64_t target = V / nt * t;
+    brange[t] = std::lower_bound(voff.begin(), voff.end(), target) - voff.begin();
+  }
+  brange[nt] = nb;
+  std::vector<std::vector<int64_t>> tcnt(nt);
+  run_threads(nt, [&](int t) {
+    std::vector<int64_t>& c = tcnt[t];
+    c.assign(n, 0);
+    for (int64_t b = brange[t]; b < brange[t + 1]; b++)
+      visit_block(b, [&](int32_t dp, int32_t dq, uint32_t, uint32_t) { c[std::min(dp, dq)]++; });
   });
   std::vector<int64_t> bptr(n + 1, 0);
-  for (int64_t r = 0; r < n; r++) bptr[r + 1] = bptr[r] + cnt[r].load(std::memory_order_relaxed);
-  for (int64_t r = 0; r < n; r++) cnt[r].store(bptr[r], std::memory_order_relaxed);
+  for (int64_t r = 0; r < n; r++) {
+    int64_t s = 0;
+    for (int t = 0; t < nt; t++) s += tcnt[t][r];
+    bptr[r + 1] = bptr[r] + s;
+  }
+  parallel_for(n, [&](int64_t r0, int64_t r1) {
+    for (int64_t r = r0; r < r1; r++) {
+      int64_t o = bptr[r];
+      for (int t = 0; t < nt; t++) {
+        const int64_t c = tcnt[t][r];
+        tcnt[t][r] = o;
+        o += c;
+      }
+    }
+  });
   struct Item { int32_t col; uint64_t code; };
-  std::vector<Item> items(V);
-  parallel_for(nb, [&](int64_t b0, int64_t b1) {
-    for (int64_t b = b0; b < b1; b++)
+  // scratch arrays are left uninitialised (every element is written before it is read): zeroing them
+  // would add a full serial pass over hundreds of MB at 1M DoFs
+  std::unique_ptr<Item[]> items(new Item[V]);
+  run_threads(nt, [&](int t) {
+    std::vector<int64_t>& pos = tcnt[t];
+    for (int64_t b = brange[t]; b < brange[t + 1]; b++)
       visit_block(b, [&](int32_t dp, int32_t dq, uint32_t i, uint32_t k) {
-        int32_t r = std::min(dp, dq), c = std::max(dp, dq);
-        int64_t pos = cnt[r].fetch_add(1, std::memory_order_relaxed);
-        items[pos] = {c, make_code((uint32_t)b, i, k)};
+        const int32_t r = std::min(dp, dq), c = std::max(dp, dq);
+        items[pos[r]++] = {c, make_code((uint32_t)b, i, k)};
       });
   });
 
@@ -217,8 +253,8 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   std::vector<int64_t> ucnt(n, 0);
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
-      Item* a = items.data() + bptr[r];
-      Item* z = items.data() + bptr[r + 1];
+      Item* a = items.get() + bptr[r];
+      Item* z = items.get() + bptr[r + 1];
       std::sort(a, z, [](const Item& x, const Item& y) { return x.col != y.col ? x.col < y.col : x.code < y.code; });
       int64_t u = 0;
       for (Item* it = a; it < z; it++)
@@ -230,8 +266,8 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   for (int64_t r = 0; r < n; r++) uptr[r + 1] = uptr[r] + ucnt[r];
   const int64_t nu = uptr[n];
   g.nnz_upper = nu;
-  std::vector<int32_t> ucol(nu);
-  std::vector<int64_t> uc0(nu + 1);   // start of each upper entry's items (items are grouped by entry)
+  std::unique_ptr<int32_t[]> ucol(new int32_t[nu]);
+  std::unique_ptr<int64_t[]> uc0(new int64_t[nu + 1]);   // start of each upper entry's items (grouped by entry)
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
       int64_t u = uptr[r];
@@ -245,38 +281,84 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   });
   uc0[nu] = V;
 
-  // ---- full symmetric CSR: row r = (entries (c, r) of upper rows c < r, ascending c) + upper row r
-  std::vector<int64_t> lcnt(n, 0);
-  for (int64_t r = 0; r < n; r++)
-    for (int64_t u = uptr[r]; u < uptr[r + 1]; u++)
-      if (ucol[u] != r) lcnt[ucol[u]]++;
+  // ---- full symmetric CSR: row r = (entries (c, r) of upper rows c < r, ascending c) + upper row r.
+  // The transposed (lower) entries are counted and placed per thread over contiguous, ascending ranges
+  // of upper rows (balanced by entry count), which keeps each lower row sorted without atomics.
+  std::vector<int64_t> rrange(nt + 1, 0);
+  for (int t = 1; t < nt; t++) {
+    const int64_t target = nu / nt * t;
+    rrange[t] = std::lower_bound(uptr.begin(), uptr.end(), target) - uptr.begin();
+  }
+  rrange[nt] = n;
+  run_threads(nt, [&](int t) {
+    std::vector<int64_t>& c = tcnt[t];
+    std::fill(c.begin(), c.end(), 0);
+    for (int64_t r = rrange[t]; r < rrange[t + 1]; r++)
+      for (int64_t u = uptr[r]; u < uptr[r + 1]; u++)
+        if (ucol[u] != r) c[ucol[u]]++;
+  });
   g.row_ptr.assign(n + 1, 0);
-  for (int64_t r = 0; r < n; r++) g.row_ptr[r + 1] = g.row_ptr[r] + lcnt[r] + (uptr[r + 1] - uptr[r]);
+  std::vector<int64_t> lcnt(n, 0);
+  for (int64_t r = 0; r < n; r++) {
+    int64_t l = 0;
+    for (int t = 0; t < nt; t++) l += tcnt[t][r];
+    lcnt[r] = l;
+    g.row_ptr[r + 1] = g.row_ptr[r] + l + (uptr[r + 1] - uptr[r]);
+  }
   const int64_t nf = g.row_ptr[n];
   g.nnz_full = nf;
-  g.col.assign(nf, 0);
-  std::vector<int64_t> src(nf);
-  std::vector<int64_t> cur(n);
-  for (int64_t r = 0; r < n; r++) cur[r] = g.row_ptr[r];
-  for (int64_t r = 0; r < n; r++)
-    for (int64_t u = uptr[r]; u < uptr[r + 1]; u++)
-      if (ucol[u] != r) {
-        int64_t c = ucol[u];
-        g.col[cur[c]] = (int32_t)r;
-        src[cur[c]] = u;
-        cur[c]++;
-      }
+  g.col.resize(nf);
+  std::unique_ptr<int64_t[]> src(new int64_t[nf]);
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
-      int64_t pos = cur[r];
+      int64_t o = g.row_ptr[r];
+      for (int t = 0; t < nt; t++) {
+        const int64_t c = tcnt[t][r];
+        tcnt[t][r] = o;
+        o += c;
+      }
+    }
+  });
+  run_threads(nt, [&](int t) {
+    std::vector<int64_t>& pos = tcnt[t];
+    for (int64_t r = rrange[t]; r < rrange[t + 1]; r++)
+      for (int64_t u = uptr[r]; u < uptr[r + 1]; u++)
+        if (ucol[u] != r) {
+          const int64_t p = pos[ucol[u]]++;
+          g.col[p] = (int32_t)r;
+          src[p] = u;
+        }
+  });
+  parallel_for(n, [&](int64_t r0, int64_t r1) {
+    for (int64_t r = r0; r < r1; r++) {
+      int64_t pos = g.row_ptr[r] + lcnt[r];
       for (int64_t u = uptr[r]; u < uptr[r + 1]; u++, pos++) {
         g.col[pos] = ucol[u];
         src[pos] = u;
       }
     }
   });
-  g.cptr.assign(nf + 1, 0);
-  for (int64_t e = 0; e < nf; e++) g.cptr[e + 1] = g.cptr[e] + (uc0[src[e] + 1] - uc0[src[e]]);
+  // visit lists per full entry: lengths, a two-pass parallel prefix sum, then the copies
+  g.cptr.resize(nf + 1);
+  g.cptr[0] = 0;
+  {
+    const int64_t chunk = (nf + nt - 1) / nt;
+    std::vector<int64_t> part(nt + 1, 0);
+    run_threads(nt, [&](int t) {
+      const int64_t e0 = std::min(nf, t * chunk), e1 = std::min(nf, e0 + chunk);
+      int64_t acc = 0;
+      for (int64_t e = e0; e < e1; e++) {
+        acc += uc0[src[e] + 1] - uc0[src[e]];
+        g.cptr[e + 1] = acc;
+      }
+      part[t + 1] = acc;
+    });
+    for (int t = 0; t < nt; t++) part[t + 1] += part[t];
+    run_threads(nt, [&](int t) {
+      const int64_t e0 = std::min(nf, t * chunk), e1 = std::min(nf, e0 + chunk);
+      for (int64_t e = e0; e < e1; e++) g.cptr[e + 1] += part[t];
+    });
+  }
   g.codes.resize(g.cptr[nf]);
   parallel_for(nf, [&](int64_t e0, int64_t e1) {
     for (int64_t e = e0; e < e1; e++) {

@@ -9,6 +9,9 @@
 // that product, in FP64, for each CSR entry.
 #pragma once
 #include <cstdint>
+#include <memory>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace fem2d {
@@ -32,6 +35,24 @@ inline uint64_t make_code(uint32_t blk, uint32_t p, uint32_t q) {
 
 struct DeviceGEP;   // device buffers (assemble.cu)
 
+// std::vector storage whose resize leaves new elements uninitialised (default-initialised): the
+// symbolic phase writes every element of its large arrays, and zeroing them first would cost a full
+// serial pass over hundreds of MB at 1M DoFs
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind { using other = NoInitAlloc<U>; };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) { ::new ((void*)p) U; }
+  template <class U, class... Args>
+  void construct(U* p, Args&&... args) { ::new ((void*)p) U(std::forward<Args>(args)...); }
+};
+template <class T>
+using HostVec = std::vector<T, NoInitAlloc<T>>;
+
 struct HostGEP {
   int64_t n = 0;                       // DoFs
   int64_t nnz_upper = 0, nnz_full = 0;
@@ -40,10 +61,10 @@ struct HostGEP {
   int pmax = 0;                        // table stride - 1 (max order over both axes)
   // full symmetric CSR pattern (A and B share it)
   std::vector<int64_t> row_ptr;        // n + 1
-  std::vector<int32_t> col;            // nnz_full
+  HostVec<int32_t> col;                // nnz_full
   // per full entry, its contribution list (codes), in a fixed order
-  std::vector<int64_t> cptr;           // nnz_full + 1
-  std::vector<uint64_t> codes;
+  HostVec<int64_t> cptr;               // nnz_full + 1
+  HostVec<uint64_t> codes;
   // visit blocks, packed specs, intervals
   std::vector<GBlock> blocks;
   std::vector<uint32_t> specs;         // i | j << 8 | dir << 16

@@ -11,12 +11,37 @@
 #include <cmath>
 #include <functional>
 
+#include <atomic>
+#include <thread>
+
 #include "common.h"
 #include "domain.h"
 #include "gep.h"
 #include "mf.h"
 
 namespace fem2d {
+
+int num_host_threads();
+
+namespace {
+// f(t, i0, i1) on up to nt threads over [0, n) in contiguous chunks (inline for small n)
+template <class F>
+void chunked(int64_t n, F f) {
+  const int nt = n < 64 ? 1 : num_host_threads();
+  if (nt <= 1) {
+    f(0, (int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int64_t chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; t++) {
+    const int64_t a = t * chunk, b = std::min(n, a + chunk);
+    if (a >= b) break;
+    th.emplace_back([=]() { f(t, a, b); });
+  }
+  for (auto& x : th) x.join();
+}
+}  // namespace
 
 void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s, const std::vector<uint8_t>* lift) {
   const Mesh& m = d.mesh;
@@ -116,23 +141,41 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s, const std::ve
       for (int32_t x : piv[f]) order[x] = k++;
   }
 
-  // ---- struct sets (bottom-up)
-  std::vector<std::vector<int32_t>> st(NF);
-  std::vector<int32_t> mark(n, -1);
+  // ---- struct sets (bottom-up): fronts numbered in post-order, so a level's fronts depend only on
+  // lower levels; the fronts of one level are processed in parallel, one mark array per thread
+  std::vector<int32_t> lev(NF, 0);
+  int nlev = 0;
   for (int f = 0; f < NF; f++) {
-    std::vector<int32_t> cand;
-    auto add = [&](int32_t y) {
-      if (mark[y] == f) return;
-      if (!is_proper_anc(node[y], f)) return;
-      mark[y] = f;
-      cand.push_back(y);
-    };
-    for (int32_t x : piv[f])
-      for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) add(g.col[k]);
-    for (int32_t c : kids[f])
-      for (int32_t y : st[c]) add(y);
-    std::sort(cand.begin(), cand.end(), [&](int32_t a, int32_t b) { return order[a] < order[b]; });
-    st[f] = std::move(cand);
+    for (int32_t c : kids[f]) lev[f] = std::max(lev[f], 1 + lev[c]);
+    nlev = std::max(nlev, lev[f] + 1);
+  }
+  std::vector<std::vector<int32_t>> by_level(nlev);
+  for (int f = 0; f < NF; f++) by_level[lev[f]].push_back(f);
+  std::vector<std::vector<int32_t>> st(NF);
+  const int nthr = std::max(1, num_host_threads());
+  std::vector<std::vector<int32_t>> marks(nthr);
+  for (int l = 0; l < nlev; l++) {
+    const std::vector<int32_t>& fl = by_level[l];
+    chunked((int64_t)fl.size(), [&](int t, int64_t i0, int64_t i1) {
+      std::vector<int32_t>& mark = marks[t];
+      if ((int64_t)mark.size() != n) mark.assign(n, -1);
+      for (int64_t i = i0; i < i1; i++) {
+        const int f = fl[i];
+        std::vector<int32_t> cand;
+        auto add = [&](int32_t y) {
+          if (mark[y] == f) return;
+          if (!is_proper_anc(node[y], f)) return;
+          mark[y] = f;
+          cand.push_back(y);
+        };
+        for (int32_t x : piv[f])
+          for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) add(g.col[k]);
+        for (int32_t c : kids[f])
+          for (int32_t y : st[c]) add(y);
+        std::sort(cand.begin(), cand.end(), [&](int32_t a, int32_t b) { return order[a] < order[b]; });
+        st[f] = std::move(cand);
+      }
+    });
   }
 
   // ---- fronts, maps, levels
@@ -161,38 +204,70 @@ void mf_symbolic(const Domain& d, const HostGEP& g, MFSymbolic& s, const std::ve
     s.mat_off[f + 1] = s.mat_off[f] + (int64_t)s.f[f] * s.f[f];
   }
   s.mat_total = s.mat_off[NF];
-  std::vector<int32_t> pos(n, -1);
-  s.asm_ptr.assign(NF + 1, 0);
-  s.ea_ptr.assign(NF + 1, 0);
+  // assembly maps: per front, the positions of its pivot rows' CSR entries (and their mirrors) in the
+  // dense front, and the positions of each child's update rows in it. Counted and filled front by
+  // front in parallel (one position array per thread), laid out in front order.
+  std::vector<int64_t> acount(NF, 0);
   std::vector<std::vector<int32_t>> ea(NF);
-  for (int f = 0; f < NF; f++) {
-    const int32_t* D = s.dofs.data() + s.dof_ptr[f];
-    const int F = s.f[f], P = s.p[f];
-    for (int i = 0; i < F; i++) pos[D[i]] = i;
-    for (int i = 0; i < P; i++) {
-      int32_t x = D[i];
-      for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) {
-        // entries whose column was eliminated in a descendant front were assembled there
-        const int32_t nc = node[g.col[k]];
-        if (nc < f && nc >= first_desc[f]) continue;
-        int32_t pc = pos[g.col[k]];
-        if (pc < 0) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: coupling outside the front");
-        s.asm_pos.push_back((int64_t)i * F + pc);
-        s.asm_csr.push_back(k);
-        if (pc >= P) {
-          s.asm_pos.push_back((int64_t)pc * F + i);
-          s.asm_csr.push_back(k);
+  std::vector<std::vector<int32_t>> posv(nthr);
+  std::atomic<int> bad_coupling{0}, bad_update{0};
+  for (int pass = 0; pass < 2; pass++) {
+    chunked((int64_t)NF, [&](int t, int64_t f0, int64_t f1) {
+      std::vector<int32_t>& pos = posv[t];
+      if ((int64_t)pos.size() != n) pos.assign(n, -1);
+      for (int64_t f = f0; f < f1; f++) {
+        const int32_t* D = s.dofs.data() + s.dof_ptr[f];
+        const int F = s.f[f], P = s.p[f];
+        for (int i = 0; i < F; i++) pos[D[i]] = i;
+        int64_t w = pass == 0 ? 0 : s.asm_ptr[f];
+        for (int i = 0; i < P; i++) {
+          int32_t x = D[i];
+          for (int64_t k = g.row_ptr[x]; k < g.row_ptr[x + 1]; k++) {
+            // entries whose column was eliminated in a descendant front were assembled there
+            const int32_t nc = node[g.col[k]];
+            if (nc < f && nc >= first_desc[f]) continue;
+            int32_t pc = pos[g.col[k]];
+            if (pc < 0) {   // (reported after the threads join: no exception may leave a worker)
+              bad_coupling = 1;
+              continue;
+            }
+            if (pass == 0) {
+              w += pc >= P ? 2 : 1;
+              continue;
+            }
+            s.asm_pos[w] = (int64_t)i * F + pc;
+            s.asm_csr[w++] = k;
+            if (pc >= P) {
+              s.asm_pos[w] = (int64_t)pc * F + i;
+              s.asm_csr[w++] = k;
+            }
+          }
         }
+        if (pass == 0) {
+          acount[f] = w;
+          for (int32_t ch : kids[f]) {
+            std::vector<int32_t>& m = ea[ch];
+            m.resize(st[ch].size());
+            for (size_t q = 0; q < st[ch].size(); q++) {
+              const int32_t y = st[ch][q];
+              if (pos[y] < 0) bad_update = 1;
+              m[q] = pos[y];
+            }
+          }
+        }
+        for (int i = 0; i < F; i++) pos[D[i]] = -1;
       }
+    });
+    if (bad_coupling) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: coupling outside the front");
+    if (bad_update) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: child update outside the parent front");
+    if (pass == 0) {
+      s.asm_ptr.assign(NF + 1, 0);
+      for (int f = 0; f < NF; f++) s.asm_ptr[f + 1] = s.asm_ptr[f] + acount[f];
+      s.asm_pos.resize(s.asm_ptr[NF]);
+      s.asm_csr.resize(s.asm_ptr[NF]);
     }
-    s.asm_ptr[f + 1] = (int64_t)s.asm_pos.size();
-    for (int32_t ch : kids[f])
-      for (int32_t y : st[ch]) {
-        if (pos[y] < 0) fail(FEM2D_E_INVALID_ARG, "multifrontal symbolic: child update outside the parent front");
-        ea[ch].push_back(pos[y]);
-      }
-    for (int i = 0; i < F; i++) pos[D[i]] = -1;
   }
+  s.ea_ptr.assign(NF + 1, 0);
   for (int f = 0; f < NF; f++) s.ea_ptr[f + 1] = s.ea_ptr[f] + (int64_t)ea[f].size();
   s.ea_map.reserve(s.ea_ptr[NF]);
   for (int f = 0; f < NF; f++) s.ea_map.insert(s.ea_map.end(), ea[f].begin(), ea[f].end());

@@ -121,7 +121,8 @@ int64_t fem2d_ctx_kernel_launches(const fem2d_ctx* c);
 int fem2d_ctx_timer_start(fem2d_ctx* c);
 int fem2d_ctx_timer_stop(fem2d_ctx* c, double* ms);
 /* per-region device timing (synchronising, for measurement runs): regions "assembly_values", "spmm",
- * "mf_factor", "mf_forward", "mf_backward"; query returns total ms, launches and algorithmic bytes */
+ * "mf_factor", "mf_solve" (one forward + backward solve), "dense_block" (the eigensolver's FP64 grams and
+ * block products); query returns total ms, calls and algorithmic bytes */
 int fem2d_ctx_set_profiling(fem2d_ctx* c, int on);
 int fem2d_ctx_profile_reset(fem2d_ctx* c);
 int fem2d_ctx_profile_query(const fem2d_ctx* c, const char* region, double* ms, int64_t* count, double* bytes);
@@ -186,8 +187,9 @@ int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64
 int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, double* a, double* b);
 /* full symmetric CSR (row_ptr: ndofs+1, col/val: nnz_full) of A or B */
 int fem2d_gep_export_csr(const fem2d_gep* g, int which, int64_t* row_ptr, int32_t* col, double* val);
-/* device timings (ms) of the last galerkin/recompute call: [tables, values, total] */
-int fem2d_gep_timings(const fem2d_gep* g, double* out3);
+/* timings (ms): [tables, values, tables + values] of the last galerkin/recompute call (device), then
+   [host symbolic phase, upload] of the galerkin call that built the GEP */
+int fem2d_gep_timings(const fem2d_gep* g, double* out5);
 /* visit count P_visits = sum_E [n(E)(n(E)+1)/2 + n(E) sum_D n(D)] (the reference's integrate calls) */
 int64_t fem2d_gep_num_visits(const fem2d_gep* g);
 /* bytes copied host -> device when the GEP was built (pattern, contribution lists, tables) */
