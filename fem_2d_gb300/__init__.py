@@ -124,6 +124,7 @@ def lib():
         "fem2d_gep_export_upper": (ctypes.c_int, [P, i32p, i32p, dp, dp]),
         "fem2d_gep_export_csr": (ctypes.c_int, [P, ctypes.c_int, i64p, i32p, dp]),
         "fem2d_gep_timings": (ctypes.c_int, [P, dp]),
+        "fem2d_gep_by_parts": (ctypes.c_int, [P, P, dp]),
         "fem2d_gep_num_visits": (i64, [P]),
         "fem2d_gep_h2d_bytes": (i64, [P]),
         "fem2d_ctx_timer_start": (ctypes.c_int, [P]),
@@ -508,6 +509,15 @@ class GEP:
         out = np.zeros(5)
         _check(lib().fem2d_gep_timings(self._h, _ptr(out, ctypes.c_double)))
         return out
+
+    def by_parts(self):
+        """integrate_by_parts over the Galerkin visit set on the device: (rows, cols, vals) in upper_coo's
+        order, vals[:, 0] the CurlCurl face term, vals[:, 1:5] its edge terms, vals[:, 5] the L2Inner
+        value (integrals.rs:94-237, 356-418)."""
+        r, c, _, _ = self.upper_coo()
+        v = np.zeros((len(r), 6))
+        _check(lib().fem2d_gep_by_parts(self.ctx._h, self._h, _ptr(v, ctypes.c_double)))
+        return r, c, v
 
     def upper_coo(self):
         n, nu, nf = self.dims()

@@ -7,6 +7,7 @@
 #include <mutex>
 #include <sstream>
 
+#include "byparts.h"
 #include "common.h"
 #include "device.h"
 #include "domain.h"
@@ -610,6 +611,14 @@ int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, dou
       if (b) b[k] = vb[e];
       k++;
     }
+  API_END
+}
+
+int fem2d_gep_by_parts(fem2d_ctx* c, const fem2d_gep* g, double* vals6) {
+  API_BEGIN
+  if (!c || !g || !vals6) fail(FEM2D_E_INVALID_ARG, "null argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  gep_by_parts(c->c, g->h, g->d, vals6);
   API_END
 }
 

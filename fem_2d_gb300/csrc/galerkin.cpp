@@ -139,6 +139,7 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   std::vector<BInfo> binfo;
   std::vector<int64_t> desc;
   g.blocks.clear();
+  g.braw.clear();
   for (int64_t e = 0; e < ne; e++) {
     int64_t np = d.nspecs(e);
     if (np == 0) continue;
@@ -173,6 +174,11 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
       b.cb[0] = wB * P.ji_u0 * Q.ji_u0;
       b.cb[1] = wB * P.ji_v1 * Q.ji_v1;
       g.blocks.push_back(b);
+      // the raw geometry of the pair for integrate_by_parts: P (a, b, det, ji_u0, ji_v1), Q (same),
+      // the material of P's root element (mu_re, eps_re)
+      const double raw[12] = {P.a, P.b, P.det, P.ji_u0, P.ji_v1, Q.a, Q.b, Q.det, Q.ji_u0, Q.ji_v1,
+                              root.mu_re, root.eps_re};
+      g.braw.insert(g.braw.end(), raw, raw + 12);
       int64_t nq = d.nspecs(q);
       binfo.push_back({e, q, local ? np * (np + 1) / 2 : np * nq, local});
     };

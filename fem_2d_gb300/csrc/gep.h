@@ -67,6 +67,7 @@ struct HostGEP {
   HostVec<uint64_t> codes;
   // visit blocks, packed specs, intervals
   std::vector<GBlock> blocks;
+  std::vector<double> braw;            // per block, 12 doubles of raw pair geometry (integrate_by_parts)
   std::vector<uint32_t> specs;         // i | j << 8 | dir << 16
   std::vector<double> ivl_s, ivl_o;    // interval scale and offset (index 0 = identity)
   std::vector<double> glq_u_x, glq_u_w, glq_v_x, glq_v_w;

@@ -185,6 +185,12 @@ void fem2d_gep_free(fem2d_gep* g);
 int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64_t* nnz_full);
 /* upper triangle as COO sorted by (row, col), like SparseMatrix::iter_upper_tri (sparse_matrix.rs:122-126) */
 int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, double* a, double* b);
+/* integrate_by_parts (CurlCurl integrals.rs:94-237, L2Inner integrals.rs:356-418) evaluated on the device
+ * over the GEP's Galerkin visit set (galerkin.rs:73-184; the reference has no by-parts driver): per upper
+ * entry, in fem2d_gep_export_upper's order, 6 doubles [CurlCurl face term, edge terms 0..3, L2Inner],
+ * each summed over the entry's visits. Samplers with second derivatives and GLQ points plus the
+ * endpoints (glq.rs:179-222), the GEP's own GLQ sizes. face + edges equals A up to rounding. */
+int fem2d_gep_by_parts(fem2d_ctx* c, const fem2d_gep* g, double* vals6);
 /* full symmetric CSR (row_ptr: ndofs+1, col/val: nnz_full) of A or B */
 int fem2d_gep_export_csr(const fem2d_gep* g, int which, int64_t* row_ptr, int32_t* col, double* val);
 /* timings (ms): [tables, values, tables + values] of the last galerkin/recompute call (device), then

@@ -923,8 +923,8 @@ static int default_ngq(int max_order) {   // basis.rs:172-177
 // ---------------------------------------------------------------------------
 // Shape-function spaces (hierarchical_basis_fns.rs)
 // ---------------------------------------------------------------------------
-struct ShapeSpace {   // norm = N, tang = T, with first derivatives
-  std::vector<std::vector<double>> n, nd, t, td;
+struct ShapeSpace {   // norm = N, tang = T, with first (and, when sampled for integrate_by_parts, second) derivatives
+  std::vector<std::vector<double>> n, nd, t, td, nd2, td2;
 };
 
 // HierPoly without 2nd derivatives: hierarchical_basis_fns.rs:102-162
@@ -1023,6 +1023,56 @@ static ShapeSpace koleg(int nmax, const std::vector<double>& x) {
   return s;
 }
 
+// Second derivatives of the shape spaces, as the samplers built with compute_2nd_derivs = true hold them.
+// HierPoly::new_with_d2 (hierarchical_basis_fns.rs:24-100): norm_d2 = d2(x^n) (2, 6x, n(n-1)x^(n-2));
+// tang_d2 returns the same table (hierarchical_basis_fns.rs:194-197).
+static void add_d2_hier_poly(ShapeSpace& s, int nmax, const std::vector<double>& x) {
+  size_t np = x.size();
+  for (int k = 0; k <= nmax; k++) {
+    std::vector<double> d2(np, 0.0);
+    if (k == 2) {
+      for (size_t p = 0; p < np; p++) d2[p] = 2.0;
+    } else if (k == 3) {
+      for (size_t p = 0; p < np; p++) d2[p] = 6.0 * x[p];
+    } else if (k > 3) {
+      const double kf = (double)k;
+      for (size_t p = 0; p < np; p++) d2[p] = kf * (kf - 1.0) * s.n[k - 2][p];
+    }
+    s.nd2.push_back(d2);
+  }
+  s.td2 = s.nd2;
+}
+// LegendrePoly::with_specs_with_2nd_derivs (hierarchical_basis_fns.rs:466-590): P_2'' = 3, P_n'' =
+// (2x P_n' - n(n+1) P_n) / (1 - x^2) with the denominator replaced by 1 at x = +-1; the Q functions'
+// second derivatives are the weighted Legendre sums (QFunction::with_specs_with_2nd_derivs 356-395,
+// weighted_double_prime_sum 620-644)
+static void add_d2_koleg(ShapeSpace& s, int nmax, const std::vector<double>& x) {
+  size_t np = x.size();
+  std::vector<double> den(np);
+  for (size_t p = 0; p < np; p++) den[p] = 1.0 - std::pow(x[p], 2);
+  if (std::fabs(std::fabs(x[0]) - 1.0) < 1e-15) den[0] = 1.0;
+  if (std::fabs(std::fabs(x[np - 1]) - 1.0) < 1e-15) den[np - 1] = 1.0;
+  std::vector<std::vector<double>> L2(nmax + 1, std::vector<double>(np, 0.0));
+  for (int i = 2; i <= nmax; i++) {
+    const double f = (double)i;
+    for (size_t p = 0; p < np; p++)
+      L2[i][p] = i == 2 ? 3.0 : (2.0 * x[p] * s.nd[i][p] - (f * (f + 1.0)) * s.n[i][p]) / den[p];
+  }
+  s.nd2 = L2;
+  for (int i = 0; i <= nmax; i++) {
+    std::vector<double> q(np, 0.0);
+    if (i >= 2) {
+      int index = i - 2;
+      for (int k = 0; k < i + 1; k++) {
+        double w = q_num(index, k) / (double)Q_DENOM[index];
+        for (size_t p = 0; p < np; p++) q[p] += w * L2[k][p];
+      }
+      for (size_t p = 0; p < np; p++) q[p] *= EUC_NORM_COEFFS[index];
+    }
+    s.td2.push_back(q);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // HierCurlBasisFn (basis.rs:209-423) — for affine Elems the Jacobian is constant
 // but it is still evaluated per point, as the reference does.
@@ -1040,7 +1090,7 @@ struct BasisFn {
 };
 
 static BasisFn defined_over(const Mesh& mesh, const Elem& el, const Elem* desc, const std::vector<double>& up,
-                            const std::vector<double>& vp, int imax, int jmax, int basis) {
+                            const std::vector<double>& vp, int imax, int jmax, int basis, bool d2 = false) {
   BasisFn b;
   std::vector<double> us = up, vs = vp;
   double su = 1.0, sv = 1.0;
@@ -1079,6 +1129,15 @@ static BasisFn defined_over(const Mesh& mesh, const Elem& el, const Elem* desc, 
   b.ps[1] = sv;
   b.us = basis == 0 ? hier_poly(imax, us) : koleg(imax, us);
   b.vs = basis == 0 ? hier_poly(jmax, vs) : koleg(jmax, vs);
+  if (d2) {
+    if (basis == 0) {
+      add_d2_hier_poly(b.us, imax, us);
+      add_d2_hier_poly(b.vs, jmax, vs);
+    } else {
+      add_d2_koleg(b.us, imax, us);
+      add_d2_koleg(b.vs, jmax, vs);
+    }
+  }
   return b;
 }
 
@@ -1163,6 +1222,137 @@ static double l2_inner(const std::vector<double>& uw, const std::vector<double>&
     v = gauss_quad(uw, vw, [&](int m, int n) { return dot(f_v(p, pi, pj, m, n), f_u(q, qi, qj, m, n)) * pm(m, n); });
   else if (pd == BD_V && qd == BD_V)
     v = gauss_quad(uw, vw, [&](int m, int n) { return dot(f_v(p, pi, pj, m, n), f_v(q, qi, qj, m, n)) * pm(m, n); });
+  return eps_re * (p.ps[0] * p.ps[1]) * (q.ps[0] * q.ps[1]) * v;
+}
+
+// ---------------------------------------------------------------------------
+// integrate_by_parts (integrals.rs:94-237 CurlCurl, 356-418 L2Inner) on samplers with second
+// derivatives: GLQ points with the endpoints -1 and +1 appended (weight 1.0, glq.rs:215-222), the
+// face term over the interior points (real_gauss_quad_inner glq.rs:53-77) and four edge terms
+// (real_gauss_quad_edge glq.rs:101-156). basis.rs:254-292 for the second derivatives.
+// ---------------------------------------------------------------------------
+static void glq_with_endpoints(int n, std::vector<double>& pts, std::vector<double>& wts) {
+  gauss_quadrature_points(n, pts, wts);
+  pts.insert(pts.begin(), -1.0);
+  pts.push_back(1.0);
+  wts.insert(wts.begin(), 1.0);
+  wts.push_back(1.0);
+}
+static inline V2 f_u_d2(const BasisFn& b, int i, int j, int m, int n, const double* ps) {
+  const M2& ji = b.ji(m, n);
+  V2 a = {ji.u0 * (b.us.n[i][m] * b.vs.td2[j][n]), ji.u1 * (b.us.nd2[i][m] * b.vs.t[j][n])};
+  return {a.x * ps[0] * ps[0], a.y * ps[1] * ps[1]};
+}
+static inline V2 f_v_d2(const BasisFn& b, int i, int j, int m, int n, const double* ps) {
+  const M2& ji = b.ji(m, n);
+  V2 a = {ji.v0 * (b.us.t[i][m] * b.vs.nd2[j][n]), ji.v1 * (b.us.td2[i][m] * b.vs.n[j][n])};
+  return {a.x * ps[0] * ps[0], a.y * ps[1] * ps[1]};
+}
+static inline V2 f_u_dd(const BasisFn& b, int i, int j, int m, int n, const double* ps) {
+  const M2& ji = b.ji(m, n);
+  return {ji.u0 * b.us.nd[i][m] * b.vs.td[j][n] * ps[0] * ps[1], ji.u1 * b.us.nd[i][m] * b.vs.td[j][n] * ps[0] * ps[1]};
+}
+static inline V2 f_v_dd(const BasisFn& b, int i, int j, int m, int n, const double* ps) {
+  const M2& ji = b.ji(m, n);
+  return {ji.v0 * b.us.td[i][m] * b.vs.nd[j][n] * ps[0] * ps[1], ji.v1 * b.us.td[i][m] * b.vs.nd[j][n] * ps[0] * ps[1]};
+}
+template <class F>
+static inline double gauss_quad_inner(const std::vector<double>& uw, const std::vector<double>& vw, F f) {
+  double sol = 0.0;
+  for (size_t m = 1; m + 1 < uw.size(); m++) {
+    double inner = 0.0;
+    for (size_t n = 1; n + 1 < vw.size(); n++) inner += f((int)m, (int)n) * vw[n];
+    sol += inner * uw[m];
+  }
+  return sol;
+}
+template <class F>
+static inline double gauss_quad_edge(const std::vector<double>& uw, const std::vector<double>& vw, int edge, F f) {
+  double sol = 0.0;
+  const int nu = (int)uw.size(), nv = (int)vw.size();
+  if (edge == 0)
+    for (int m = 1; m < nu - 1; m++) sol += f(m, 0) * uw[m];
+  else if (edge == 1)
+    for (int m = nu - 2; m >= 1; m--) sol += f(m, nv - 1) * uw[m];
+  else if (edge == 2)
+    for (int n = nv - 2; n >= 1; n--) sol += f(0, n) * vw[n];
+  else
+    for (int n = 1; n < nv - 1; n++) sol += f(nu - 1, n) * vw[n];
+  return sol;
+}
+static const V2 EDGE_UNIT[4] = {{-1.0, 0.0}, {1.0, 0.0}, {0.0, -1.0}, {0.0, 1.0}};   // integrals.rs:242-247
+
+// out: face, edge 0..3 (IntegralResult::ByParts)
+static void curl_curl_by_parts(const std::vector<double>& uw, const std::vector<double>& vw, BasisDir pd,
+                               BasisDir qd, int pi, int pj, int qi, int qj, const BasisFn& p, const BasisFn& q,
+                               double mu_re, double* out) {
+  auto dot = [](V2 a, V2 b) { return a.x * b.x + a.y * b.y; };
+  const double gp = p.ps[0] * p.ps[1], gq = q.ps[0] * q.ps[1];
+  double face = 0.0;
+  if (pd == BD_U && qd == BD_U)
+    face = gauss_quad_inner(uw, vw, [&](int m, int n) {
+             V2 d2 = f_u_d2(p, pi, pj, m, n, q.ps), dd = f_u_dd(p, pi, pj, m, n, q.ps);
+             V2 pv = {dd.y + d2.x, d2.y + dd.x};
+             return dot(pv, f_u(q, qi, qj, m, n)) / std::pow(gq, 2) * max_uv(p, q, m, n);
+           }) * -1.0;
+  else if (pd == BD_U && qd == BD_V)
+    face = gauss_quad_inner(uw, vw, [&](int m, int n) {
+      V2 d2 = f_u_d2(p, pi, pj, m, n, q.ps), dd = f_u_dd(p, pi, pj, m, n, q.ps);
+      V2 pv = {dd.y + d2.x, d2.y + dd.x};
+      return dot(pv, f_v(q, qi, qj, m, n)) / std::pow(gq, 2);
+    });
+  else if (pd == BD_V && qd == BD_U)
+    face = gauss_quad_inner(uw, vw, [&](int m, int n) {
+      V2 d2 = f_v_d2(p, pi, pj, m, n, q.ps), dd = f_v_dd(p, pi, pj, m, n, q.ps);
+      V2 pv = {dd.y + d2.x, d2.y + dd.x};
+      return dot(pv, f_u(q, qi, qj, m, n)) / std::pow(gq, 2);
+    });
+  else if (pd == BD_V && qd == BD_V)
+    face = gauss_quad_inner(uw, vw, [&](int m, int n) {
+             V2 d2 = f_v_d2(p, pi, pj, m, n, q.ps), dd = f_v_dd(p, pi, pj, m, n, q.ps);
+             V2 pv = {dd.y + d2.x, d2.y + dd.x};
+             return dot(pv, f_v(q, qi, qj, m, n)) / std::pow(gq, 2) * max_vu(p, q, m, n);
+           }) * -1.0;
+  out[0] = (1.0 / mu_re) * gp * gq * face;
+  for (int e = 0; e < 4; e++) {
+    const double pe = e < 2 ? p.ps[0] : p.ps[1], qe = e < 2 ? q.ps[0] : q.ps[1];
+    double v = 0.0;
+    if (pd == BD_U && qd == BD_U && e < 2)
+      v = gauss_quad_edge(uw, vw, e, [&](int m, int n) {
+        return curl(f_u_d1(p, pi, pj, m, n, q.ps)) * dot(f_u(q, qi, qj, m, n), EDGE_UNIT[e]) / gq * max_uv(p, q, m, n);
+      });
+    else if (pd == BD_V && qd == BD_U && e < 2)
+      v = gauss_quad_edge(uw, vw, e, [&](int m, int n) {
+        return curl(f_v_d1(p, pi, pj, m, n, q.ps)) * dot(f_u(q, qi, qj, m, n), EDGE_UNIT[e]) / gq;
+      });
+    else if (pd == BD_U && qd == BD_V && e >= 2)
+      v = gauss_quad_edge(uw, vw, e, [&](int m, int n) {
+            return curl(f_u_d1(p, pi, pj, m, n, q.ps)) * dot(f_v(q, qi, qj, m, n), EDGE_UNIT[e]) / gq;
+          }) * -1.0;
+    else if (pd == BD_V && qd == BD_V && e >= 2)
+      v = gauss_quad_edge(uw, vw, e, [&](int m, int n) {
+            return curl(f_v_d1(p, pi, pj, m, n, q.ps)) * dot(f_v(q, qi, qj, m, n), EDGE_UNIT[e]) / gq *
+                   max_vu(p, q, m, n);
+          }) * -1.0;
+    out[1 + e] = -1.0 * (1.0 / mu_re) * pe * qe * v;
+  }
+}
+
+// L2Inner::integrate_by_parts: the full integral over the interior points
+static double l2_inner_by_parts(const std::vector<double>& uw, const std::vector<double>& vw, BasisDir pd,
+                                BasisDir qd, int pi, int pj, int qi, int qj, const BasisFn& p, const BasisFn& q,
+                                double eps_re) {
+  auto dot = [](V2 a, V2 b) { return a.x * b.x + a.y * b.y; };
+  auto pm = [&](int m, int n) { return std::max(p.dt(m, n), q.dt(m, n)); };
+  double v = 0.0;
+  if (pd == BD_U && qd == BD_U)
+    v = gauss_quad_inner(uw, vw, [&](int m, int n) { return dot(f_u(p, pi, pj, m, n), f_u(q, qi, qj, m, n)) * pm(m, n); });
+  else if (pd == BD_U && qd == BD_V)
+    v = gauss_quad_inner(uw, vw, [&](int m, int n) { return dot(f_u(p, pi, pj, m, n), f_v(q, qi, qj, m, n)) * pm(m, n); });
+  else if (pd == BD_V && qd == BD_U)
+    v = gauss_quad_inner(uw, vw, [&](int m, int n) { return dot(f_v(p, pi, pj, m, n), f_u(q, qi, qj, m, n)) * pm(m, n); });
+  else if (pd == BD_V && qd == BD_V)
+    v = gauss_quad_inner(uw, vw, [&](int m, int n) { return dot(f_v(p, pi, pj, m, n), f_v(q, qi, qj, m, n)) * pm(m, n); });
   return eps_re * (p.ps[0] * p.ps[1]) * (q.ps[0] * q.ps[1]) * v;
 }
 
@@ -1277,6 +1467,71 @@ static GEPResult galerkin(const Domain& dom, int basis, int nu, int nv, int nthr
   return r;
 }
 
+// The Galerkin visit set of galerkin_elem with integrate_by_parts in place of integrate: per upper key
+// (collisions summed in elem order) the CurlCurl face term, its four edge terms and the L2Inner value.
+struct ByPartsResult {
+  std::vector<uint32_t> rows, cols;
+  std::vector<double> vals;   // 6 per key: face, edge 0..3, B
+};
+static ByPartsResult galerkin_by_parts(const Domain& dom, int basis, int nu, int nv) {
+  if (dom.ndofs == 0) throw std::runtime_error("EmptyDOFSet");
+  auto mo = dom.mesh.max_expansion_orders();
+  int imax = mo[0], jmax = mo[1];
+  if (nu <= 0) nu = default_ngq(imax);
+  if (nv <= 0) nv = default_ngq(jmax);
+  std::vector<double> up, uw, vp, vw;
+  glq_with_endpoints(nu, up, uw);
+  glq_with_endpoints(nv, vp, vw);
+  const Mesh& mesh = dom.mesh;
+  std::map<std::pair<uint32_t, uint32_t>, std::array<double, 6>> acc;
+  auto add = [&](size_t r, size_t c, const double* v) {
+    std::pair<uint32_t, uint32_t> key = r <= c ? std::make_pair((uint32_t)r, (uint32_t)c)
+                                               : std::make_pair((uint32_t)c, (uint32_t)r);
+    auto it = acc.find(key);
+    if (it == acc.end()) {
+      std::array<double, 6> a;
+      for (int k = 0; k < 6; k++) a[k] = v[k];
+      acc.emplace(key, a);
+    } else {
+      for (int k = 0; k < 6; k++) it->second[k] += v[k];
+    }
+  };
+  for (size_t eid = 0; eid < mesh.elems.size(); eid++) {
+    const Elem& el = mesh.elems[eid];
+    const Element& elt = mesh.elements[el.element];
+    const auto& L = dom.basis_specs[eid];
+    if (L.empty()) continue;
+    BasisFn bl = defined_over(mesh, el, nullptr, up, vp, imax, jmax, basis, true);
+    double v[6];
+    for (size_t i = 0; i < L.size(); i++)
+      for (size_t k = i; k < L.size(); k++) {
+        const BasisSpec& ps = L[i];
+        const BasisSpec& qs = L[k];
+        curl_curl_by_parts(uw, vw, ps.dir, qs.dir, ps.i, ps.j, qs.i, qs.j, bl, bl, elt.mu_re, v);
+        v[5] = l2_inner_by_parts(uw, vw, ps.dir, qs.dir, ps.i, ps.j, qs.i, qs.j, bl, bl, elt.eps_re);
+        add((size_t)ps.dof_id, (size_t)qs.dof_id, v);
+      }
+    std::vector<size_t> desc = mesh.descendant_elems(eid);
+    for (size_t d : desc) {
+      BasisFn bp = defined_over(mesh, el, &mesh.elems[d], up, vp, imax, jmax, basis, true);
+      BasisFn bq = defined_over(mesh, mesh.elems[d], nullptr, up, vp, imax, jmax, basis, true);
+      for (const BasisSpec& ps : L)
+        for (const BasisSpec& qs : dom.basis_specs[d]) {
+          curl_curl_by_parts(uw, vw, ps.dir, qs.dir, ps.i, ps.j, qs.i, qs.j, bp, bq, elt.mu_re, v);
+          v[5] = l2_inner_by_parts(uw, vw, ps.dir, qs.dir, ps.i, ps.j, qs.i, qs.j, bp, bq, elt.eps_re);
+          add((size_t)ps.dof_id, (size_t)qs.dof_id, v);
+        }
+    }
+  }
+  ByPartsResult r;
+  for (auto& kv : acc) {
+    r.rows.push_back(kv.first.first);
+    r.cols.push_back(kv.first.second);
+    for (int k = 0; k < 6; k++) r.vals.push_back(kv.second[k]);
+  }
+  return r;
+}
+
 // fields.rs:386-389
 static std::vector<double> uniform_range(double min, double max, size_t n) {
   double step = (max - min) / ((double)(n - 1));
@@ -1333,6 +1588,7 @@ struct OracleState {
   Mesh mesh;
   std::unique_ptr<Domain> dom;
   GEPResult gep;
+  ByPartsResult bp;
   std::vector<double> glq_p, glq_w;
 };
 
@@ -1475,6 +1731,25 @@ int oracle_galerkin(void* h, int basis, int nu, int nv, int nthreads, int64_t* n
     if ((nu > 0 && nu < 4) || (nv > 0 && nv < 4)) throw std::runtime_error("InvalidGLQSettings");
     s->gep = galerkin(*s->dom, basis, nu, nv, nthreads);
     *nnz_upper = (int64_t)s->gep.rows.size();
+  })
+}
+int oracle_galerkin_by_parts(void* h, int basis, int nu, int nv, int64_t* nnz_upper) {
+  auto* s = (OracleState*)h;
+  ORACLE_TRY({
+    if (!s->dom) throw std::runtime_error("domain not built");
+    if ((nu > 0 && nu < 4) || (nv > 0 && nv < 4)) throw std::runtime_error("InvalidGLQSettings");
+    s->bp = galerkin_by_parts(*s->dom, basis, nu, nv);
+    *nnz_upper = (int64_t)s->bp.rows.size();
+  })
+}
+int oracle_by_parts_export(void* h, int32_t* rows, int32_t* cols, double* vals6) {
+  auto* s = (OracleState*)h;
+  ORACLE_TRY({
+    for (size_t k = 0; k < s->bp.rows.size(); k++) {
+      rows[k] = (int32_t)s->bp.rows[k];
+      cols[k] = (int32_t)s->bp.cols[k];
+    }
+    std::copy(s->bp.vals.begin(), s->bp.vals.end(), vals6);
   })
 }
 int oracle_num_leaves(void* h) {

@@ -56,6 +56,8 @@ def lib():
         L.oracle_specs.argtypes = [P, i64p]
         L.oracle_galerkin.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]
         L.oracle_gep_export.argtypes = [P, i32p, i32p, f64p, f64p]
+        L.oracle_galerkin_by_parts.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]
+        L.oracle_by_parts_export.argtypes = [P, i32p, i32p, f64p]
         L.oracle_glq.argtypes = [ctypes.c_int, f64p, f64p]
         L.oracle_shapes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, f64p]
         L.oracle_default_ngq.argtypes = [ctypes.c_int]
@@ -182,6 +184,21 @@ class OracleMesh:
         _check(lib().oracle_xy_fields(self.h, basis, d0, d1, _p(sol, ctypes.c_double), len(sol),
                                       _p(x, ctypes.c_double), _p(y, ctypes.c_double)))
         return x, y
+
+    def galerkin_by_parts(self, basis=HIERPOLY, nu=0, nv=0):
+        """The Galerkin visit set evaluated with integrate_by_parts (integrals.rs:94-237, 356-418) on
+        samplers with second derivatives (GLQ points plus the endpoints): (rows, cols, vals), vals[:, 0]
+        the CurlCurl face term, vals[:, 1:5] its edge terms, vals[:, 5] the L2Inner value, summed per
+        upper-triangle key in elem order."""
+        nnz = ctypes.c_int64(0)
+        _check(lib().oracle_galerkin_by_parts(self.h, basis, nu, nv, ctypes.byref(nnz)))
+        n = nnz.value
+        r = np.zeros(n, np.int32)
+        c = np.zeros(n, np.int32)
+        v = np.zeros((n, 6), np.float64)
+        _check(lib().oracle_by_parts_export(self.h, _p(r, ctypes.c_int32), _p(c, ctypes.c_int32),
+                                            _p(v, ctypes.c_double)))
+        return r, c, v
 
     def galerkin(self, basis=HIERPOLY, nu=0, nv=0, threads=1):
         """Upper-triangle COO (rows, cols, a, b), sorted by (row, col) like the reference's BTreeMap."""
