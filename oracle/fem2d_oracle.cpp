@@ -1752,6 +1752,18 @@ int oracle_by_parts_export(void* h, int32_t* rows, int32_t* cols, double* vals6)
     std::copy(s->bp.vals.begin(), s->bp.vals.end(), vals6);
   })
 }
+// the doc examples of real_gauss_quad_inner / real_gauss_quad_edge (glq.rs:36-52, 79-100): u^2 v^2 over
+// n GLQ points per axis plus the endpoints; out = [inner, edge 0, edge 1, edge 2, edge 3]
+int oracle_quad_doc(int n, double* out5) {
+  ORACLE_TRY({
+    std::vector<double> up, uw, vp, vw;
+    glq_with_endpoints(n, up, uw);
+    glq_with_endpoints(n, vp, vw);
+    auto f = [&](int m, int k) { return std::pow(up[m], 2) * std::pow(vp[k], 2); };
+    out5[0] = gauss_quad_inner(uw, vw, f);
+    for (int e = 0; e < 4; e++) out5[1 + e] = gauss_quad_edge(uw, vw, e, f);
+  })
+}
 int oracle_num_leaves(void* h) {
   auto* s = (OracleState*)h;
   int n = 0;

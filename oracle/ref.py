@@ -58,6 +58,7 @@ def lib():
         L.oracle_gep_export.argtypes = [P, i32p, i32p, f64p, f64p]
         L.oracle_galerkin_by_parts.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]
         L.oracle_by_parts_export.argtypes = [P, i32p, i32p, f64p]
+        L.oracle_quad_doc.argtypes = [ctypes.c_int, f64p]
         L.oracle_glq.argtypes = [ctypes.c_int, f64p, f64p]
         L.oracle_shapes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, f64p]
         L.oracle_default_ngq.argtypes = [ctypes.c_int]
@@ -212,6 +213,13 @@ class OracleMesh:
         _check(lib().oracle_gep_export(self.h, _p(r, ctypes.c_int32), _p(c, ctypes.c_int32),
                                        _p(a, ctypes.c_double), _p(b, ctypes.c_double)))
         return r, c, a, b
+
+
+def quad_doc(n):
+    """[inner, edge 0..3] of u^2 v^2 by the by-parts quadratures (glq.rs:36-52, 79-100 doc examples)."""
+    out = np.zeros(5)
+    _check(lib().oracle_quad_doc(n, _p(out, ctypes.c_double)))
+    return out
 
 
 def glq(n):

@@ -28,3 +28,11 @@ def test_by_parts_sums_to_integrate(basis, seed):
     assert np.max(np.abs(v[:, 5] - b)) <= 1e-13 * np.max(np.abs(b))
     assert np.max(np.abs(v[:, 1:5])) > 1e-3 * np.max(np.abs(a))
     assert np.max(np.abs(v[:, 0] - a)) > 1e-3 * np.max(np.abs(a))
+
+
+def test_quadratures_match_reference_doc_examples():
+    """glq.rs:36-52 and 79-100: with 10 GLQ points plus the endpoints, the interior sum of u^2 v^2 is 4/9
+    and each edge sum 2/3."""
+    out = ref.quad_doc(10)
+    assert abs(out[0] - 4.0 / 9.0) < 1e-12
+    assert np.all(np.abs(out[1:] - 2.0 / 3.0) < 1e-12)
