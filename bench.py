@@ -9,9 +9,14 @@ gpu_solve_gep (two multifrontal factorizations + the shift-invert block eigensol
 
 Prints one JSON line. `value` is DoFs/s with the GEP structures already resident in device memory;
 `e2e` is the same metric through the public API from host data (host symbolic phase, uploads and the
-eigenpair download inside the timed region). The reference arm times the CPU restatement of the
-reference's path (the oracle: literal 2-D quadrature assembly on all host threads + FP64 sparse
-shift-invert eigensolve) on the same workload.
+eigenpair download inside the timed region; `e2e.phases` splits the last such step). The reference arm
+times the CPU restatement of the reference's path (the oracle: literal 2-D quadrature assembly on all
+host threads + FP64 sparse shift-invert eigensolve) on the same workload. Outside the timed regions:
+`parity` (the FP64 oracle, up to 60k DoFs) and `accuracy` (the eigenvalues against the analytic
+eigenvalues of the PEC rectangle and against a solve of the same mesh in the other basis).
+
+Other workloads: `full_1m` (the full-form configuration at 1,070,625 DoFs, HierPoly, 20 pairs) and
+`batch` (256 seeded waveguide meshes: one batched assembly plus 256 concurrent solves per step).
 """
 import argparse
 import json
