@@ -1,22 +1,26 @@
 """Benchmark: Galerkin GEP assembly + sparse eigensolve on one GB300 (fem_2d's hot path).
 
-Workload (default): the precision family - [0,2]x[0,1] meshed as 16x8 base Elems, expansion orders
-(6,6), three seeded rounds refining 30% of the leaves with T/U/V, KOLeg basis, GLQ [10,10]; the
-10 eigenpairs nearest 10.0. A step is one assembly (tables + values on the device) plus one
-gpu_solve_gep (two multifrontal factorizations + the shift-invert block eigensolver).
+Workload (default, `full_1m`): the full form at scale - [0,2]x[0,1] meshed as 64x32 base Elems,
+per-Elem expansion orders uniform in 3..8 per direction, four seeded rounds of T/U/V h-refinement of
+44% of the leaves (1,070,625 DoFs), HierPoly basis, GLQ [10,10]; the 20 eigenpairs nearest 10.0. A step
+is one assembly (tables + values on the device) plus one gpu_solve_gep (two multifrontal
+factorizations + the shift-invert block eigensolver).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference] [--workload NAME]
 
 Prints one JSON line. `value` is DoFs/s with the GEP structures already resident in device memory;
 `e2e` is the same metric through the public API from host data (host symbolic phase, uploads and the
-eigenpair download inside the timed region; `e2e.phases` splits the last such step). The reference arm
-times the CPU restatement of the reference's path (the oracle: literal 2-D quadrature assembly on all
-host threads + FP64 sparse shift-invert eigensolve) on the same workload. Outside the timed regions:
-`parity` (the FP64 oracle, up to 60k DoFs) and `accuracy` (the eigenvalues against the analytic
-eigenvalues of the PEC rectangle and against a solve of the same mesh in the other basis).
+eigenpair download inside the timed region; `e2e.phases` splits the last such step). Outside the timed
+regions: `parity` (against the FP64 oracle: run here up to 60k DoFs, or read from the committed oracle
+fixture of the workload, tests/golden/full_form_*.json, made by tests/golden/make_full_form_fixture.py)
+and `accuracy` (the eigenvalues against the analytic eigenvalues of the PEC rectangle and against a solve
+of the same mesh in the other basis). `cpu_baseline` times the oracle's CPU restatement of the path on
+a bounded sample; the reference arm (`--impl reference`) times it on the workload itself, or prints an
+`unavailable` line when the whole run would not fit the time limit.
 
-Other workloads: `full_1m` (the full-form configuration at 1,070,625 DoFs, HierPoly, 20 pairs) and
-`batch` (256 seeded waveguide meshes: one batched assembly plus 256 concurrent solves per step).
+Other workloads: `precision` (16x8 Elems, orders 6, KOLeg, 10 pairs, 28,818 DoFs), `full_160k`
+(32x16 base Elems, 160,346 DoFs) and `batch` (256 seeded waveguide meshes: one batched assembly plus
+256 concurrent solves per step).
 """
 import argparse
 import json
@@ -34,26 +38,41 @@ METRIC = "assembly+eigensolve s and DoFs/s, learned vs plain GPU, eig rel err<=1
 UNIT = "DoFs/s"
 
 
-def workload(name):
+# full-form workloads with a committed FP64 oracle fixture: name -> configs.full_scale arguments
+FULL_FORM = {
+    "full_1m": dict(nx=64, ny=32, rounds=4, fraction=0.44),
+    "full_160k": dict(nx=32, ny=16, rounds=3, fraction=0.44),
+}
+
+
+def workload(name, replay=None):
+    """The named workload; `replay` is the mesh class its refinement script is built on (the product's
+    Mesh by default; the reference arm passes the oracle's, so it loads no product library)."""
     from fem_2d_gb300 import configs
 
+    kw = {} if replay is None else {"replay": replay}
     if name == "precision":
-        return configs.precision(seed=0)
+        return configs.precision(seed=0, **kw)
     if name == "waveguide":
-        return configs.waveguide_small()
+        return configs.waveguide_small(**kw)
+    if name in FULL_FORM:
+        return configs.full_scale(seed=0, basis=0, **FULL_FORM[name], **kw)
     if name == "full_small":
-        return configs.full_scale(seed=0, nx=32, ny=16, rounds=3)
+        return configs.full_scale(seed=0, nx=32, ny=16, rounds=3, **kw)
     if name == "full":
-        return configs.full_scale(seed=0)
-    if name == "full_koleg":
-        return configs.full_scale(seed=0, basis=1)
+        return configs.full_scale(seed=0, **kw)
     if name == "full_koleg_1m":
-        return configs.full_scale(seed=0, basis=1, fraction=0.44)
-    if name == "full_1m":
-        # the full-form configuration at ~1M DoFs: HierPoly, per-Elem orders 3..8, four T/U/V rounds of
-        # 44% of the leaves (1,070,625 DoFs; 30% gives 603,422)
-        return configs.full_scale(seed=0, basis=0, fraction=0.44)
+        return configs.full_scale(seed=0, basis=1, fraction=0.44, **kw)
     raise SystemExit("unknown workload " + name)
+
+
+def fixture(name):
+    """The committed FP64 oracle fixture of a full-form workload, or None."""
+    p = os.path.join(ROOT, "tests", "golden", "full_form_%s.json" % name)
+    if name not in FULL_FORM or not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
 
 
 def dist_env():
@@ -150,14 +169,46 @@ def profile_traffic():
     return {}
 
 
-def oracle_check(w, gep, res):
-    """FP64 oracle (literal assembly + sparse shift-invert), outside every timed region."""
+def oracle_check(w, key, gep, res):
+    """Parity against the FP64 oracle, outside every timed region. Up to 60k DoFs the oracle runs here
+    (literal assembly + FP64 sparse shift-invert); a full-form workload with a committed oracle fixture
+    is checked against it (pattern hash bit for bit, a seeded sample of entries, the 20 eigenvalues)."""
+    import hashlib
+
     import numpy as np
 
+    fx = fixture(key)
+    if fx is not None:
+        gr, gc, ga, gb = gep.upper_coo()
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(gr, dtype="<i4").tobytes())
+        h.update(np.ascontiguousarray(gc, dtype="<i4").tobytes())
+        sm = fx["sample"]
+        key_g = gr.astype(np.int64) * gep.dimension + gc
+        key_s = np.asarray(sm["rows"], np.int64) * gep.dimension + np.asarray(sm["cols"], np.int64)
+        pos = np.searchsorted(key_g, key_s)
+        pos = np.minimum(pos, len(key_g) - 1)
+        found = bool(np.all(key_g[pos] == key_s))
+        ea = float(np.max(np.abs(ga[pos] - np.asarray(sm["a"]))) / fx["max_abs_a"])
+        eb = float(np.max(np.abs(gb[pos] - np.asarray(sm["b"]))) / fx["max_abs_b"])
+        del gr, gc, ga, gb, key_g
+        ov = np.asarray(fx["eigenvalues"])
+        gv = np.sort(res.values)
+        rel = np.abs(gv - ov) / np.abs(ov)
+        out = {"oracle": "committed FP64 oracle fixture (tests/golden/full_form_%s.json): literal 2-D assembly + "
+                         "ARPACK shift-invert Lanczos with SuperLU solves" % key,
+               "ndofs_match": gep.dimension == fx["ndofs"], "nnz_upper_match": gep.dims()[1] == fx["nnz_upper"],
+               "pattern_bit_exact": h.hexdigest() == fx["pattern_sha256"], "sample_keys_found": found,
+               "sample_entries": len(key_s), "entry_err_A": ea, "entry_err_B": eb,
+               "eig_rel_err_max": float(np.max(rel)), "eig_rel_err": rel.tolist(),
+               "oracle_eig_err_bound_rel_max": float(np.max(np.asarray(fx["err_bound"]) / np.abs(ov)))}
+        if "cross_check" in fx:
+            out["oracle_methods_max_rel_diff"] = fx["cross_check"]["max_rel_diff"]
+        return out
+    if gep.dimension > 60000:
+        return {"skipped": "no oracle fixture for this workload; the oracle's solve runs here only up to 60k DoFs"}
     from oracle import ref
 
-    if gep.dimension > 60000:
-        return {"skipped": "the oracle's sparse solve takes minutes above 60k DoFs; accuracy checks the eigenvalues"}
     om = ref.OracleMesh(w.mesh_json)
     om.apply_ops(w.ops)
     n = om.domain()
@@ -168,13 +219,18 @@ def oracle_check(w, gep, res):
     eb = float(np.max(np.abs(gb - b)) / np.max(np.abs(b)))
     A = ref.full_sym(n, r, c, a)
     B = ref.full_sym(n, r, c, b)
-    ws, _, _ = ref.sparse_nearest_physical(A, B, w.target, w.n_pairs)
-    rel = float(np.max(np.abs(res.values - ws) / np.abs(ws)))
-    return {"pattern_bit_exact": same, "entry_err_A": ea, "entry_err_B": eb, "eig_rel_err_max": rel}
+    perm = ref.nd_order(ref.dof_boxes(om))
+    ws = ref.arpack_nearest_physical(A, B, w.target, w.n_pairs, perm, refine=0)["values"]
+    rel = float(np.max(np.abs(np.sort(res.values) - np.sort(ws)) / np.abs(np.sort(ws))))
+    return {"oracle": "FP64 oracle run here: literal 2-D assembly + ARPACK shift-invert Lanczos with SuperLU solves",
+            "pattern_bit_exact": same, "entry_err_A": ea, "entry_err_B": eb, "eig_rel_err_max": rel}
 
 
 def cpu_port_step(w, threads):
-    """One step of the CPU restatement: literal 2-D quadrature assembly + FP64 sparse shift-invert."""
+    """One step of the CPU restatement of the path (the oracle, on the host cores): the literal 2-D
+    quadrature assembly on `threads` threads, then the FP64 sparse shift-invert eigensolve (ARPACK
+    Lanczos on T with SuperLU solves under the oracle's nested-dissection ordering). Returns
+    (ndofs, assembly s, eigensolve s)."""
     from oracle import ref
 
     t0 = time.perf_counter()
@@ -185,20 +241,60 @@ def cpu_port_step(w, threads):
     t1 = time.perf_counter()
     A = ref.full_sym(n, r, c, a)
     B = ref.full_sym(n, r, c, b)
-    ref.sparse_nearest_physical(A, B, w.target, w.n_pairs, block=w.n_pairs + max(4, w.n_pairs // 2), steps=2,
-                                tol=1e-10)
+    perm = ref.nd_order(ref.dof_boxes(om))
+    ref.arpack_nearest_physical(A, B, w.target, w.n_pairs, perm, refine=0)
     t2 = time.perf_counter()
     return n, t1 - t0, t2 - t1
 
 
+# the bounded CPU sample of a full-form workload: the family's 16x8-base-Elem member (same orders,
+# rounds and refinement fraction), one full step of the CPU port
+def cpu_sample(name, replay=None):
+    from fem_2d_gb300 import configs
+
+    if name in FULL_FORM:
+        kw = dict(FULL_FORM[name], nx=16, ny=8)
+        if replay is not None:
+            kw["replay"] = replay
+        return configs.full_scale(seed=0, basis=0, **kw), "the full-form family's 16x8-base-Elem member"
+    return workload(name, replay), "the workload itself"
+
+
+def reference_config(w, n):
+    return {"workload": w.name, "ndofs": n, "basis": "KOLeg" if w.basis == 1 else "HierPoly", "glq": list(w.glq),
+            "n_pairs": w.n_pairs, "target": w.target, "seed": w.seed}
+
+
 def run_reference(args, ws, rank):
+    """The reference arm: the oracle's CPU restatement of the reference's path (literal 2-D quadrature
+    assembly on all host threads + FP64 sparse shift-invert eigensolve) on the same workload. Workload
+    scripts are replayed on the oracle's mesh, so no product library is loaded. When the committed
+    fixture's single-step time says that W + K steps cannot finish within the run limit, an
+    `unavailable` line says so instead."""
     if rank != 0:
         return
     from oracle import build as ob
 
     ob.build_oracle()
-    w = workload(args.workload)
+    from oracle import ref
+
+    w = workload(args.workload, ref.OracleReplay)
     threads = os.cpu_count() or 4
+    fx = fixture(args.workload)
+    if fx is not None:
+        one = fx["t_oracle_assembly_s"] + fx["t_oracle_eigensolve_s"]
+        if one * (args.steps + args.warmup) > args.reference_limit_s:
+            print(json.dumps({
+                "impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True,
+                "config": dict(reference_config(w, fx["ndofs"]), nnz_upper=fx["nnz_upper"]),
+                "unavailable": "one step of the CPU restatement of the path at %d DoFs took %.0f s on %d host threads "
+                               "(literal assembly %.0f s + FP64 ARPACK/SuperLU shift-invert %.0f s); %d steps would take "
+                               "about %.0f s, beyond the %d s limit; the native line's cpu_baseline times a bounded "
+                               "sample" % (fx["ndofs"], one, fx["threads"], fx["t_oracle_assembly_s"],
+                                           fx["t_oracle_eigensolve_s"], args.steps + args.warmup,
+                                           one * (args.steps + args.warmup), args.reference_limit_s)}), flush=True)
+            return
     for _ in range(args.warmup):
         cpu_port_step(w, threads)
     tot, ta, te, n = 0.0, 0.0, 0.0, 0
@@ -211,11 +307,11 @@ def run_reference(args, ws, rank):
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh family)",
-           "config": {"workload": w.name, "ndofs": n, "n_pairs": w.n_pairs, "target": w.target},
+           "config": reference_config(w, n),
            "t_assembly_s": ta / args.steps, "t_eigensolve_s": te / args.steps,
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": "full workload per step: literal 2-D quadrature assembly on %d threads + "
-                                      "FP64 sparse shift-invert (SuperLU + block Krylov, the GPU path's block and depth)" % threads},
+                            "sample": "full workload per step: literal 2-D quadrature assembly on %d threads + FP64 sparse "
+                                      "shift-invert (ARPACK Lanczos, SuperLU under nested dissection)" % threads},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -312,11 +408,12 @@ def run_native(args, ws, rank, local):
     ms_step = barrier_max((t_asm + t_eig) / args.steps, ws)
     value = ws * n / (ms_step / 1e3)
 
-    # end to end through the public API from host data
+    # end to end through the public API from host data (at most 5 repetitions: at 1M DoFs one takes ~6 s)
     e2e_ms = 0.0
     h2d = d2h = 0
     parts = {}
-    for _ in range(max(1, args.steps)):
+    e2e_reps = max(1, min(args.steps, 5))
+    for _ in range(e2e_reps):
         ctx.synchronize()
         t0 = time.perf_counter()
         d2 = fg.Domain.from_mesh(mesh)
@@ -336,13 +433,17 @@ def run_native(args, ws, rank, local):
         h2d = g2.h2d_bytes + 8 * n * (w.n_pairs + max(4, w.n_pairs // 2))
         d2h = 8 * w.n_pairs * (n + 2)
         del g2, d2, r2
-    e2e_ms = barrier_max(e2e_ms / max(1, args.steps), ws)
+    e2e_ms = barrier_max(e2e_ms / e2e_reps, ws)
     e2e = ws * n / (e2e_ms / 1e3)
 
     # profiling pass (one extra step, per-region CUDA events) for the roofline
     ctx.profile_reset()
     ctx.set_profiling(True)
+    ctx.synchronize()
+    tp0 = time.perf_counter()
     step()
+    ctx.synchronize()
+    ms_prof = 1e3 * (time.perf_counter() - tp0)
     ctx.set_profiling(False)
     regions = {}
     for reg in ("assembly_values", "spmm", "mf_factor", "mf_solve", "dense_block"):
@@ -390,24 +491,27 @@ def run_native(args, ws, rank, local):
            "t_assembly_s": t_asm / args.steps / 1e3, "t_eigensolve_s": t_eig / args.steps / 1e3,
            "wall_s_timed": wall, "gpu_launches": launches,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                   "ms_per_step": e2e_ms, "phases": parts},
+                   "ms_per_step": e2e_ms, "steps": e2e_reps, "phases": parts},
            "roofline": roofline, "region_ms_profiled": share,
+           "region_ms_unprofiled": ms_prof - sum(share.values()), "ms_profiled_step": ms_prof,
            "region_rooflines": {k: roof(k) for k in regions if k != dom_name},
            "solve_stats": res.stats if res is not None else None,
            "max_rel_residual": float(np.max(res.residuals)) if res is not None else None,
            "clocks": clocks}
     if rank == 0 and not args.no_check:
-        out["parity"] = oracle_check(w, gep, res)
+        out["parity"] = oracle_check(w, args.workload, gep, res)
     if rank == 0 and not args.no_check:
         out["accuracy"] = accuracy_check(w, mesh, ctx, res)
     if rank == 0 and ws == 1 and not args.no_learned:
         out["learned_vs_plain"] = learned_vs_plain(ctx)
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 4
-        cn, ca_, ce = cpu_port_step(w, threads)
+        sw, what = cpu_sample(args.workload)
+        cn, ca_, ce = cpu_port_step(sw, threads)
         out["cpu_baseline"] = {"value": cn / (ca_ + ce), "unit": UNIT, "cores": threads, "kind": "port",
-                               "sample": "one full step of the workload: literal 2-D quadrature assembly "
-                                         "(%.2f s) + FP64 sparse shift-invert (%.2f s)" % (ca_, ce)}
+                               "sample": "one full step of %s (%s, %d DoFs): literal 2-D quadrature assembly "
+                                         "(%.2f s) + FP64 ARPACK/SuperLU shift-invert (%.2f s)"
+                                         % (what, sw.name, cn, ca_, ce)}
     if rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -520,7 +624,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="precision")
+    ap.add_argument("--workload", default="full_1m")
+    ap.add_argument("--reference-limit-s", type=int, default=1500)
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true")

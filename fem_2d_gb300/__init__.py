@@ -97,6 +97,7 @@ def lib():
         "fem2d_galerkin_sample_gep_hcurl": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, PP]),
         "fem2d_gep_recompute": (ctypes.c_int, [P, P]),
         "fem2d_gep_values_noalloc": (ctypes.c_int, [P, P, ctypes.c_void_p, ctypes.c_void_p]),
+        "fem2d_gep_set_upper_values": (ctypes.c_int, [P, dp, dp]),
         "fem2d_galerkin_sample_gep_hcurl_batch": (ctypes.c_int, [P, PP, i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                           ctypes.c_int, PP, dp]),
         "fem2d_gep_batch_recompute": (ctypes.c_int, [P, PP, i64, ctypes.c_int, dp]),
@@ -528,6 +529,16 @@ class GEP:
         _check(lib().fem2d_gep_export_upper(self._h, _ptr(r, ctypes.c_int32), _ptr(c, ctypes.c_int32),
                                             _ptr(a, ctypes.c_double), _ptr(b, ctypes.c_double)))
         return r, c, a, b
+
+    def set_upper_values(self, a, b):
+        """Replace A and B by the given upper-triangle values (in ``upper_coo`` order); the reference's
+        GEP exposes its matrices as public fields (linalg.rs:29-34) that callers may edit."""
+        n, nu, nf = self.dims()
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if a.shape != (nu,) or b.shape != (nu,):
+            raise ValueError("expected %d upper-triangle values for A and for B" % nu)
+        _check(lib().fem2d_gep_set_upper_values(self._h, _ptr(a, ctypes.c_double), _ptr(b, ctypes.c_double)))
 
     def csr(self, which):
         n, nu, nf = self.dims()

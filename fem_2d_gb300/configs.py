@@ -10,7 +10,10 @@ five configurations the GPU path is measured on. A workload is a mesh JSON plus 
     ("hmix", ids, kinds)           execute_h_refinements with one kind per Elem
 
 Random choices use splitmix64 (seeded, identical on every machine); leaf sets are read back from the
-mesh after each round, so a script is built against the native mesh as it is refined.
+mesh after each round, so a script is built against a mesh as it is refined. The mesh a script is
+built on is a ``replay`` class: ``NativeReplay`` (this package's Mesh, the default) or any class with
+the same three members (the oracle's ``OracleReplay``); both give the same script, so a caller that
+must not load this package's library can still build every workload.
 """
 from __future__ import annotations
 
@@ -109,6 +112,22 @@ def apply_ops(mesh, ops):
             raise ValueError(op[0])
 
 
+class NativeReplay:
+    """A script under construction replayed on this package's Mesh."""
+
+    def __init__(self, mesh_json):
+        from . import Mesh
+
+        self.mesh = Mesh.from_json(mesh_json)
+
+    def apply(self, ops):
+        apply_ops(self.mesh, ops)
+
+    def elem_info(self):
+        """Per Elem: [is_leaf, ni, nj, parent, nodes(4), edges(4), h_u, h_v]."""
+        return self.mesh.elem_info()
+
+
 def _leaves(mesh):
     info = mesh.elem_info()
     return [int(e) for e in np.nonzero(info[:, 0] == 1)[0]]
@@ -120,19 +139,17 @@ def _random_rounds(mesh, ops, rng, rounds, fraction, kinds):
         pick = sorted(rng.sample(leaves, int(fraction * len(leaves))))
         ks = [kinds[rng.next() % len(kinds)] for _ in pick]
         op = ("hmix", pick, ks)
-        apply_ops(mesh, [op])
+        mesh.apply([op])
         ops.append(op)
 
 
-def waveguide_small():
+def waveguide_small(replay=NativeReplay):
     """[0,1]x[0,0.5] in 2 Elems, orders (4,4), global T, then U on the leaves touching the top-middle node
     (the README.md:45-61 sequence); HierPoly, GLQ [8,8], dense solve nearest 10.0 (TE10: pi^2)."""
-    from . import Mesh
-
     mj = grid_mesh_json(2, 1, 0.0, 1.0, 0.0, 0.5)
     ops = [("orders", 4, 4, None), ("href", 0, None, -1)]
-    m = Mesh.from_json(mj)
-    apply_ops(m, ops)
+    m = replay(mj)
+    m.apply(ops)
     info = m.elem_info()
     center = int(info[0, 4 + 3])   # elems[0].nodes[3]
     pick = [e for e in range(len(info)) if info[e, 0] == 1 and center in info[e, 4:8]]
@@ -140,25 +157,21 @@ def waveguide_small():
     return Workload("waveguide_small", mj, ops, basis=0, glq=(8, 8), target=10.0, n_pairs=1)
 
 
-def precision(seed=0, nx=16, ny=8, order=6, rounds=3, fraction=0.3):
+def precision(seed=0, nx=16, ny=8, order=6, rounds=3, fraction=0.3, replay=NativeReplay):
     """[0,2]x[0,1], 16x8 Elems, orders (6,6), three seeded rounds refining 30% of the leaves with T/U/V;
     KOLeg, GLQ [10,10], 10 pairs nearest 10.0."""
-    from . import Mesh
-
     mj = grid_mesh_json(nx, ny, 0.0, 2.0, 0.0, 1.0)
     ops = [("orders", order, order, None)]
-    m = Mesh.from_json(mj)
-    apply_ops(m, ops)
+    m = replay(mj)
+    m.apply(ops)
     _random_rounds(m, ops, SplitMix64(seed), rounds, fraction, [0, 1, 2])
     return Workload("precision_16x8_p6_koleg", mj, ops, basis=1, glq=(10, 10), target=10.0, n_pairs=10, seed=seed)
 
 
-def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8, basis=0):
+def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8, basis=0, replay=NativeReplay):
     """[0,2]x[0,1], 64x32 Elems, per-Elem orders uniform in pmin..pmax per direction, `rounds` seeded rounds
     of T/U/V refinement of `fraction` of the leaves; HierPoly (basis=0) or KOLeg (basis=1), GLQ [10,10],
     20 pairs nearest 10.0."""
-    from . import Mesh
-
     mj = grid_mesh_json(nx, ny, 0.0, 2.0, 0.0, 1.0)
     rng = SplitMix64(seed)
     groups = {}
@@ -166,33 +179,29 @@ def full_scale(seed=0, nx=64, ny=32, rounds=4, fraction=0.3, pmin=3, pmax=8, bas
         key = (rng.randint(pmin, pmax), rng.randint(pmin, pmax))
         groups.setdefault(key, []).append(e)
     ops = [("ordersmap", sorted(groups.items()))]
-    m = Mesh.from_json(mj)
-    apply_ops(m, ops)
+    m = replay(mj)
+    m.apply(ops)
     _random_rounds(m, ops, rng, rounds, fraction, [0, 1, 2])
     name = "full_%dx%d_p%d-%d_%s_r%d_f%g" % (nx, ny, pmin, pmax, "koleg" if basis else "hierpoly", rounds, fraction)
     return Workload(name, mj, ops, basis=basis, glq=(10, 10), target=10.0, n_pairs=20, seed=seed)
 
 
-def learned_family(seed=0, nx=32, ny=16, orders=(5, 7), rounds=2, fraction=1.0):
+def learned_family(seed=0, nx=32, ny=16, orders=(5, 7), rounds=2, fraction=1.0, replay=NativeReplay):
     """The learned-preconditioner family: [0,2]x[0,1], nx x ny Elems, orders (5,7), `rounds` seeded rounds of
     anisotropic (U/V) refinement of `fraction` of the leaves (two rounds from a uniform grid keep Elems that
     share an edge within two levels); KOLeg, GLQ [10,10], 10 pairs nearest 10.0. Full size 32x16."""
-    from . import Mesh
-
     mj = grid_mesh_json(nx, ny, 0.0, 2.0, 0.0, 1.0)
     ops = [("orders", orders[0], orders[1], None)]
-    m = Mesh.from_json(mj)
-    apply_ops(m, ops)
+    m = replay(mj)
+    m.apply(ops)
     _random_rounds(m, ops, SplitMix64(7919 * (seed + 1)), rounds, fraction, [1, 2])
     return Workload("learned_%dx%d_p%d-%d_seed%d" % (nx, ny, orders[0], orders[1], seed), mj, ops, basis=1,
                     glq=(10, 10), target=10.0, n_pairs=10, seed=seed)
 
 
-def batch_member(seed):
+def batch_member(seed, replay=NativeReplay):
     """One mesh of the batching family: a ~ U[1,3], (gx, gy) with gx*gy in [4,64] on [0,a]x[0,1],
     per-Elem orders (pu, pv) ~ U{2..8}^2, 0-2 random refinement rounds; GLQ [10,10], 4 pairs nearest 10."""
-    from . import Mesh
-
     rng = SplitMix64(1000003 * (seed + 1))
     a = 1.0 + 2.0 * rng.uniform()
     while True:
@@ -204,8 +213,8 @@ def batch_member(seed):
     for e in range(gx * gy):
         groups.setdefault((rng.randint(2, 8), rng.randint(2, 8)), []).append(e)
     ops = [("ordersmap", sorted(groups.items()))]
-    m = Mesh.from_json(mj)
-    apply_ops(m, ops)
+    m = replay(mj)
+    m.apply(ops)
     _random_rounds(m, ops, rng, rng.randint(0, 2), 0.3, [0, 1, 2])
     return Workload("batch_%d" % seed, mj, ops, basis=0, glq=(10, 10), target=10.0, n_pairs=4, seed=seed)
 

@@ -164,9 +164,16 @@ void device_values_noalloc(Ctx& c, const HostGEP& g, const DeviceGEP& d, double*
   if (c.device < 0 || c.device >= 256) fail(FEM2D_E_INVALID_ARG, "device ordinal out of range");
   double* tables = nullptr;
   {
+    // The array's device address, taken on this device (the caller made it current). It is looked up
+    // again on every call made outside a stream capture, so a context rebuilt after cudaDeviceReset
+    // (which reloads the module at a new address) is picked up; inside a capture the address from the
+    // last call outside one is used, which is why the first call on a device must precede any capture.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    FEM2D_CUDA(cudaStreamIsCapturing(c.stream, &cap));
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[c.device]) {
-      // one-time set-up on this device (the device is current: the caller made it so)
+    if (cap == cudaStreamCaptureStatusNone || !g_noalloc_addr[c.device]) {
+      if (cap != cudaStreamCaptureStatusNone)
+        fail(FEM2D_E_INVALID_ARG, "first allocation-free call on a device inside a stream capture");
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_tables);
       if (e != cudaSuccess) fail(FEM2D_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));

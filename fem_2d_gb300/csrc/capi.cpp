@@ -1,6 +1,7 @@
 // extern "C" boundary of fem2d_gb300 (declared in include/fem2d_gb300.h).
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -443,10 +444,34 @@ int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g) {
 }
 
 int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, double* d_b) {
+  int prev = -1;
   API_BEGIN
   if (!c || !g || !d_a || !d_b) fail(FEM2D_E_INVALID_ARG, "null argument");
   if (g->ctx != &c->c) fail(FEM2D_E_INVALID_ARG, "the GEP was built on another context");
+  // the caller's current device is put back on every return (its own later launches go there)
+  FEM2D_CUDA(cudaGetDevice(&prev));
+  struct Restore {
+    int dev;
+    ~Restore() {
+      if (dev >= 0) cudaSetDevice(dev);
+    }
+  } restore{prev};
   FEM2D_CUDA(cudaSetDevice(c->c.device));
+  // both arrays must be device (or managed) memory of the context's device: a host pointer or another
+  // GPU's array would otherwise fault inside the kernels (cudaPointerGetAttributes allocates nothing)
+  for (const double* p : {d_a, d_b}) {
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(FEM2D_E_INVALID_ARG, "output array is not CUDA memory");
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+      fail(FEM2D_E_INVALID_ARG, "output array is not device or managed memory");
+    if (at.type == cudaMemoryTypeDevice && at.device != c->c.device)
+      fail(FEM2D_E_INVALID_ARG, "output array lives on device " + std::to_string(at.device) + ", the context on " +
+                                    std::to_string(c->c.device));
+  }
   device_values_noalloc(c->c, g->h, g->d, d_a, d_b);
   API_END
 }
@@ -611,6 +636,40 @@ int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, dou
       if (b) b[k] = vb[e];
       k++;
     }
+  API_END
+}
+
+int fem2d_gep_set_upper_values(fem2d_gep* g, const double* a, const double* b) {
+  API_BEGIN
+  if (!g || !a || !b) fail(FEM2D_E_INVALID_ARG, "null argument");
+  const HostGEP& h = g->h;
+  for (int64_t k = 0; k < h.nnz_upper; k++)
+    if (!std::isfinite(a[k]) || !std::isfinite(b[k]))
+      fail(FEM2D_E_INVALID_ARG, "A or B has a non-finite entry (upper-triangle index " + std::to_string(k) + ")");
+  std::vector<double> va(h.nnz_full), vb(h.nnz_full);
+  int64_t k = 0;
+  for (int64_t r = 0; r < h.n; r++)
+    for (int64_t e = h.row_ptr[r]; e < h.row_ptr[r + 1]; e++) {
+      const int32_t cc = h.col[e];
+      if (cc < r) continue;
+      va[e] = a[k];
+      vb[e] = b[k];
+      if (cc != r) {   // the mirrored entry (cc, r) in row cc
+        const int32_t* c0 = h.col.data() + h.row_ptr[cc];
+        const int32_t* c1 = h.col.data() + h.row_ptr[cc + 1];
+        const int32_t* it = std::lower_bound(c0, c1, (int32_t)r);
+        if (it == c1 || *it != r) fail(FEM2D_E_INVALID_ARG, "GEP pattern is not symmetric");
+        va[it - h.col.data()] = a[k];
+        vb[it - h.col.data()] = b[k];
+      }
+      k++;
+    }
+  FEM2D_CUDA(cudaSetDevice(g->ctx->device));
+  if (h.nnz_full) {
+    FEM2D_CUDA(cudaMemcpyAsync(g->d.a.p, va.data(), h.nnz_full * 8, cudaMemcpyHostToDevice, g->ctx->stream));
+    FEM2D_CUDA(cudaMemcpyAsync(g->d.b.p, vb.data(), h.nnz_full * 8, cudaMemcpyHostToDevice, g->ctx->stream));
+    FEM2D_CUDA(cudaStreamSynchronize(g->ctx->stream));
+  }
   API_END
 }
 

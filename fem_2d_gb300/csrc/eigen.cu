@@ -917,6 +917,11 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     }
     // Rayleigh-Ritz on the active columns [nl, m): (V^T A V, V^T B V)
     const int ma = m - nl;
+    if (ma <= 0)
+      fail(nl > 0 ? FEM2D_E_NOT_CONVERGED : FEM2D_E_SPURIOUS,
+           nl > 0 ? "gpu_solve_gep: the search space collapsed onto the locked pairs"
+                  : "gpu_solve_gep: T vanishes on the start block (A has only null-space directions); only spurious "
+                    "modes exist");
     const double* Va = V.p + nl;
     const double* AVa = AV.p + nl;
     const double* BVa = BV.p + nl;

@@ -853,6 +853,7 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
   max_f = s.max_f;
   max_p = s.max_p;
   nb_cap = nb_max;
+  factor_flops = s.flops;
   // fronts laid out level by level so each level's storage is contiguous
   std::vector<int64_t> off(nf, 0), poff(nf, 0), woff_h(nf, 0);
   std::vector<std::array<int32_t, MAXKIDS>> kids(nf);
@@ -979,7 +980,7 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
   FEM2D_CUDA(cudaMemsetAsync(weak_count.p, 0, sizeof(int), st));
   out.weak.clear();
   const FrontDesc* fd = reinterpret_cast<const FrontDesc*>(desc.p);
-  ProfScope ps(c, "mf_factor", 8.0 * (double)mat_total);
+  ProfScope ps(c, "mf_factor", 8.0 * (double)mat_total, cholesky ? 0.5 * factor_flops : factor_flops);
   out.inv_n = 0;
   if (nf == 1 && max_p == max_f && max_f <= 4096) {
     // one dense front (a small GEP): its explicit inverse by Gauss-Jordan, kept in F; solves are then

@@ -26,6 +26,7 @@ struct MFFactor {
 struct MFDevice {
   int nf = 0, nlevels = 0, max_f = 0, max_p = 0, nb_cap = 0;
   int64_t mat_total = 0, piv_total = 0;
+  double factor_flops = 0;   // LU flops of all fronts, 2/3 (f^3 - (f - p)^3) each (half for Cholesky)
   std::vector<int32_t> level_ptr;
   std::vector<int64_t> level_off;
   std::vector<int32_t> level_max_f, level_max_p;

@@ -152,10 +152,12 @@ int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g);
  * needing more (2 x intervals x 5 x (max order + 1)^2) is rejected with FEM2D_E_TOO_LARGE. Each GPU
  * that loads the library holds that array until the process exits. The first call on a device looks
  * up the array's device address (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the one array: calls that overlap on the GPU (other streams, other host
- * threads) race on it. Nothing in it needs clearing between calls. Returns after the work is queued
- * on the context's stream; synchronise before reading d_a and d_b. No cudaMalloc, cudaFree or other
- * allocating call is made. */
+ * capture. Later calls outside a capture look it up again, so a context rebuilt after
+ * cudaDeviceReset is handled. All calls share the one array: calls that overlap on the GPU (other
+ * streams, other host threads) race on it. Nothing in it needs clearing between calls. d_a and d_b
+ * must be device (or managed) memory of the context's device, else FEM2D_E_INVALID_ARG. The caller's
+ * current device is restored on return. Returns after the work is queued on the context's stream;
+ * synchronise before reading d_a and d_b. No cudaMalloc, cudaFree or other allocating call is made. */
 int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, double* d_b);
 /* galerkin_sample_gep_hcurl over many Domains at once (galerkin.rs:33-187 per Domain; the reference
  * has no batched form: a caller loops over Domains). Each Domain gets its own host symbolic phase and
@@ -185,6 +187,12 @@ void fem2d_gep_free(fem2d_gep* g);
 int fem2d_gep_dims(const fem2d_gep* g, int64_t* ndofs, int64_t* nnz_upper, int64_t* nnz_full);
 /* upper triangle as COO sorted by (row, col), like SparseMatrix::iter_upper_tri (sparse_matrix.rs:122-126) */
 int fem2d_gep_export_upper(const fem2d_gep* g, int32_t* rows, int32_t* cols, double* a, double* b);
+/* replace A and B by caller values, given per upper-triangle entry in fem2d_gep_export_upper's order
+ * (mirrored into the full symmetric pattern on the device); the reference's GEP exposes its matrices as
+ * public fields (`pub a: SparseMatrix, pub b: SparseMatrix`, linalg.rs:29-34) that callers may edit
+ * before a solve. The pattern is kept. Rejects a non-finite entry with FEM2D_E_INVALID_ARG. A later
+ * fem2d_gep_recompute overwrites the values with the assembled ones. */
+int fem2d_gep_set_upper_values(fem2d_gep* g, const double* a, const double* b);
 /* integrate_by_parts (CurlCurl integrals.rs:94-237, L2Inner integrals.rs:356-418) evaluated on the device
  * over the GEP's Galerkin visit set (galerkin.rs:73-184; the reference has no by-parts driver): per upper
  * entry, in fem2d_gep_export_upper's order, 6 doubles [CurlCurl face term, edge terms 0..3, L2Inner],

@@ -1764,6 +1764,23 @@ int oracle_quad_doc(int n, double* out5) {
     for (int e = 0; e < 4; e++) out5[1 + e] = gauss_quad_edge(uw, vw, e, f);
   })
 }
+// Per Elem (x0, y0, x1, y1) from its lower-left and upper-right nodes (Elem::nodes order is
+// [lower-left, lower-right, upper-left, upper-right], elem.rs:12-36); used only to order the
+// oracle's own sparse factorizations (nested dissection), never in any value it computes.
+int oracle_elem_bounds(void* h, double* out) {
+  auto* s = (OracleState*)h;
+  ORACLE_TRY({
+    for (size_t e = 0; e < s->mesh.elems.size(); e++) {
+      const Elem& el = s->mesh.elems[e];
+      const Point& a = s->mesh.nodes[el.nodes[0]].coords;
+      const Point& b = s->mesh.nodes[el.nodes[3]].coords;
+      out[4 * e + 0] = a.x;
+      out[4 * e + 1] = a.y;
+      out[4 * e + 2] = b.x;
+      out[4 * e + 3] = b.y;
+    }
+  })
+}
 int oracle_num_leaves(void* h) {
   auto* s = (OracleState*)h;
   int n = 0;

@@ -63,6 +63,7 @@ def lib():
         L.oracle_shapes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, f64p]
         L.oracle_default_ngq.argtypes = [ctypes.c_int]
         L.oracle_num_leaves.argtypes = [P]
+        L.oracle_elem_bounds.argtypes = [P, f64p]
         L.oracle_xy_fields.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, ctypes.c_int64, f64p, f64p]
         _LIB = L
     return _LIB
@@ -162,6 +163,12 @@ class OracleMesh:
         _check(lib().oracle_elem_info(self.h, _p(out, ctypes.c_int64)))
         return out
 
+    def elem_bounds(self):
+        """Per Elem (x0, y0, x1, y1)."""
+        out = np.zeros((self.num_elems(), 4), dtype=np.float64)
+        _check(lib().oracle_elem_bounds(self.h, _p(out, ctypes.c_double)))
+        return out
+
     def domain(self):
         nd = ctypes.c_int64(0)
         _check(lib().oracle_domain(self.h, ctypes.byref(nd)))
@@ -213,6 +220,20 @@ class OracleMesh:
         _check(lib().oracle_gep_export(self.h, _p(r, ctypes.c_int32), _p(c, ctypes.c_int32),
                                        _p(a, ctypes.c_double), _p(b, ctypes.c_double)))
         return r, c, a, b
+
+
+class OracleReplay:
+    """The oracle mesh as a ``replay`` class of fem_2d_gb300.configs: workload scripts built on it are
+    the same as on the product's Mesh, and loading it loads no product library."""
+
+    def __init__(self, mesh_json):
+        self.mesh = OracleMesh(mesh_json)
+
+    def apply(self, ops):
+        self.mesh.apply_ops(ops)
+
+    def elem_info(self):
+        return self.mesh.elem_info()
 
 
 def quad_doc(n):
@@ -301,7 +322,7 @@ def _borth_block(W, V, B, drop=1e-8):
     return W
 
 
-def sparse_nearest_physical(A, B, sigma, k, block=None, steps=3, tol=1e-11, max_cycles=40, spurious=1e-6):
+def sparse_nearest_physical(A, B, sigma, k, block=None, steps=3, tol=1e-11, max_cycles=40, spurious=1e-6, perm=None):
     """FP64 oracle for gpu_solve_gep: the k eigenpairs nearest sigma excluding the curl null space.
 
     Search space from T = (A - sigma B)^-1 A (A + c B)^-1 B, c = 0.05 |sigma|, with sparse LU solves (SuperLU),
@@ -313,8 +334,12 @@ def sparse_nearest_physical(A, B, sigma, k, block=None, steps=3, tol=1e-11, max_
 
     n = A.shape[0]
     b = block or min(n, k + max(8, k))
-    luM = sla.splu((A - sigma * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
-    luP = sla.splu((A + 0.05 * abs(sigma) * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
+    if perm is None:
+        luM = sla.splu((A - sigma * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
+        luP = sla.splu((A + 0.05 * abs(sigma) * B).tocsc(), permc_spec="MMD_AT_PLUS_A")
+    else:
+        luM = NDLU((A - sigma * B).tocsc(), perm)
+        luP = NDLU((A + 0.05 * abs(sigma) * B).tocsc(), perm)
 
     def T(X):
         return luM.solve(A @ luP.solve(B @ X))
@@ -447,3 +472,195 @@ def petsc_vec_bytes(values):
     import struct
 
     return struct.pack(">ii", 1211214, len(values)) + struct.pack(">%dd" % len(values), *values)
+
+
+def dof_boxes(om):
+    """Support box (x0, y0, x1, y1) of every DoF: the union of the boxes of the Elems whose basis
+    specs carry it (one Elem for an Elem-type DoF, the Elems on both sides for an edge-type DoF)."""
+    if om.ndofs is None:
+        om.domain()
+    eb = om.elem_bounds()
+    sp = om.specs()
+    ids = sp[:, 5]
+    box = np.empty((om.ndofs, 4))
+    box[:, :2] = np.inf
+    box[:, 2:] = -np.inf
+    e = eb[sp[:, 0]]
+    np.minimum.at(box[:, 0], ids, e[:, 0])
+    np.minimum.at(box[:, 1], ids, e[:, 1])
+    np.maximum.at(box[:, 2], ids, e[:, 2])
+    np.maximum.at(box[:, 3], ids, e[:, 3])
+    return box
+
+
+def nd_order(box, leaf=256):
+    """Geometric nested dissection of the DoFs by their support boxes: the oracle's own fill-reducing
+    ordering for its sparse LU (an ordering changes no value, only the fill and the rounding order).
+
+    Two DoFs couple only if their supports overlap with positive area (an Elem pairs with itself and
+    its descendants, and an edge DoF's support spans both sides of its edge), so a line x = s splits
+    the DoFs into those wholly left of it, those wholly right of it, and a separator of the DoFs whose
+    boxes straddle it. Each level tries both axes and, between the 30% and 70% quantiles of the box
+    centres, the cut with the fewest straddling DoFs; the order is left part, right part, separator,
+    recursively, down to parts of ``leaf`` DoFs.
+    """
+    import sys
+
+    out = []
+
+    def cut(idx):
+        best = None
+        for ax in (0, 1):
+            lo, hi = box[idx, ax], box[idx, ax + 2]
+            c = np.sort(0.5 * (lo + hi))
+            q0, q1 = c[int(0.3 * (len(c) - 1))], c[int(0.7 * (len(c) - 1))]
+            cand = np.unique(np.concatenate([lo, hi]))
+            cand = cand[(cand >= q0) & (cand <= q1)]
+            if len(cand) == 0:
+                continue
+            slo, shi = np.sort(lo), np.sort(hi)
+            left = np.searchsorted(shi, cand, side="right")             # hi <= s
+            right = len(idx) - np.searchsorted(slo, cand, side="left")   # lo >= s
+            score = (len(idx) - left - right) * len(idx) + np.abs(left - right)
+            k = int(np.argmin(score))
+            if best is None or score[k] < best[0]:
+                best = (score[k], ax, cand[k])
+        return best
+
+    def rec(idx):
+        if len(idx) <= leaf:
+            out.append(idx)
+            return
+        b = cut(idx)
+        if b is None:
+            out.append(idx)
+            return
+        _, ax, s = b
+        lo, hi = box[idx, ax], box[idx, ax + 2]
+        L, R = idx[hi <= s], idx[lo >= s]
+        if len(L) == 0 or len(R) == 0:
+            out.append(idx)
+            return
+        rec(L)
+        rec(R)
+        out.append(idx[(lo < s) & (hi > s)])
+
+    sys.setrecursionlimit(max(10000, sys.getrecursionlimit()))
+    rec(np.arange(len(box)))
+    return np.concatenate(out)
+
+
+class NDLU:
+    """SuperLU factorization of a sparse matrix under a given symmetric ordering (``nd_order``) with
+    diagonal-preferring threshold pivoting; ``solve`` works in the original numbering."""
+
+    def __init__(self, K, perm, pivot=0.1):
+        import scipy.sparse.linalg as sla
+
+        self.perm = perm
+        self.inv = np.empty_like(perm)
+        self.inv[perm] = np.arange(len(perm))
+        Kp = K.tocsr()[perm][:, perm].tocsc()
+        self.lu = sla.splu(Kp, permc_spec="NATURAL", diag_pivot_thresh=pivot, options={"SymmetricMode": True})
+
+    def solve(self, X):
+        return self.lu.solve(np.ascontiguousarray(X[self.perm]))[self.inv]
+
+
+def _cluster_bounds(th_sel, rb, th_all, rel_tol=1e-6):
+    """Quadratic (Kato-Temple type) eigenvalue error bounds for Ritz values th_sel with B^-1-norm
+    residuals rb. Ritz values within rel_tol of each other form a cluster C (degenerate modes of the
+    rectangle come in such pairs); with r_C = sqrt(sum_{j in C} rb_j^2) and g the distance from the
+    cluster to the nearest Ritz value outside it, the bound is r_C^2 / (g - r_C) when g > 2 r_C, else
+    r_C (some eigenvalue always lies within rb of a Ritz value). The gap is taken to the other computed
+    Ritz values, which assumes no eigenvalue of the pencil is missing near the cluster."""
+    out = np.empty(len(th_sel))
+    for i, t in enumerate(th_sel):
+        inc = np.abs(th_sel - t) <= rel_tol * abs(t)
+        rc = float(np.sqrt(np.sum(rb[inc] ** 2)))
+        others = th_all[np.abs(th_all - t) > rel_tol * abs(t)]
+        g = float(np.min(np.abs(others - t))) if len(others) else np.inf
+        out[i] = rc * rc / (g - rc) if g > 2 * rc else rc
+    return out
+
+
+def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1e-6, tol=1e-13, seed=0,
+                            refine=2, reject=1e-2):
+    """Second, independent FP64 sparse oracle for large pencils: ARPACK (implicitly restarted Lanczos
+    in the B inner product, through scipy ``eigsh``) on T = (A - sigma B)^-1 A (A + c B)^-1 B.
+
+    T's eigenvalues mu = lambda / ((lambda - sigma)(lambda + c)) vanish on the curl null space and grow
+    without bound as lambda nears sigma, so the largest |mu| are the physical modes near sigma. The
+    solves are SuperLU factorizations under ``perm``. The k + extra Lanczos vectors X are then refined
+    ``refine`` times by one Rayleigh-Ritz step on (A, B) over span[X, T X] in FP64, and the k Ritz
+    values nearest sigma with |lambda| > spurious |sigma| and relative residual below ``reject`` are
+    returned with:
+
+    * ``rel_residual`` ||A x - lambda B x|| / (|lambda| ||B x||) and ``backward_error``
+      ||A x - lambda B x|| / ((||A||_1 + |lambda| ||B||_1) ||x||);
+    * ``resid_binv`` = ||r||_{B^-1} for B-normalised x (some eigenvalue of the pencil lies within it of
+      the Ritz value) and ``err_bound`` from ``_cluster_bounds``;
+    * ``mu_min``: the smallest |mu| ARPACK returned. ``extra`` pairs beyond k (default k) are asked for
+      because the order by |mu| is not the order by |lambda - sigma| below sigma; an eigenvalue missed
+      has |mu| below ``mu_min``.
+    """
+    import scipy.sparse.linalg as sla
+
+    n = A.shape[0]
+    c = abs(sigma) if c is None else c
+    extra = k if extra is None else extra
+    luM = NDLU((A - sigma * B).tocsc(), perm)
+    luP = NDLU((A + c * B).tocsc(), perm)
+    luB = NDLU(B.tocsc(), perm)
+    Ac, Bc = A.tocsr(), B.tocsr()
+    count = [0]
+
+    def T(X):
+        count[0] += 1 if X.ndim == 1 else X.shape[1]
+        return luM.solve(Ac @ luP.solve(Bc @ X))
+
+    m = k + extra
+    Aop = sla.LinearOperator((n, n), matvec=lambda x: Bc @ T(x), dtype=np.float64)
+    Mi = sla.LinearOperator((n, n), matvec=luB.solve, dtype=np.float64)
+    v0 = np.random.default_rng(seed).standard_normal(n)
+    mu, V = sla.eigsh(Aop, k=m, M=Bc, Minv=Mi, which="LM", tol=tol, v0=v0, ncv=min(n - 1, max(2 * m + 1, m + 32)))
+    mu_min = float(np.min(np.abs(mu)))
+
+    def rayleigh_ritz(V):
+        BV = Bc @ V
+        G = V.T @ BV
+        w, U = np.linalg.eigh((G + G.T) / 2)
+        keep = w > w.max() * 1e-14
+        W = V @ (U[:, keep] / np.sqrt(w[keep]))
+        AW, BW = Ac @ W, Bc @ W
+        H = W.T @ AW
+        th, Y = np.linalg.eigh((H + H.T) / 2)
+        return th, W @ Y, AW @ Y, BW @ Y
+
+    def residuals(th, X, AX, BX):
+        R = AX - BX * th
+        rn = np.linalg.norm(R, axis=0)
+        rel = rn / (np.abs(th) * np.linalg.norm(BX, axis=0) + 1e-300)
+        # Rayleigh-Ritz on (A, B) over a space that holds T-application error can return Ritz values
+        # that are mixtures of null-space and high-frequency directions; their residuals are O(1) or
+        # larger, so they are not selected
+        ok = np.nonzero((np.abs(th) > spurious * abs(sigma)) & (rel < reject))[0]
+        return R, rn, rel, ok[np.argsort(np.abs(th[ok] - sigma), kind="stable")]
+
+    th, X, AX, BX = rayleigh_ritz(V)
+    for _ in range(refine):
+        _, _, _, order = residuals(th, X, AX, BX)
+        Xs = X[:, order[:m]]
+        th, X, AX, BX = rayleigh_ritz(np.hstack([Xs, T(Xs)]))
+    R, rn, rel, order = residuals(th, X, AX, BX)
+    nA, nB = sla.norm(Ac, 1), sla.norm(Bc, 1)
+    bwd = rn / ((nA + np.abs(th) * nB) * np.linalg.norm(X, axis=0))
+    idx = order[:k]
+    ok = order
+    Rs = R[:, idx]
+    Z = luB.solve(Rs)
+    rb = np.sqrt(np.abs(np.einsum("ij,ij->j", Rs, Z)))
+    phys = th[ok]
+    return {"values": th[idx], "vectors": X[:, idx], "rel_residual": rel[idx], "backward_error": bwd[idx],
+            "resid_binv": rb, "err_bound": _cluster_bounds(th[idx], rb, phys), "mu_min": mu_min,
+            "applications": count[0]}

@@ -83,3 +83,40 @@ def test_barrier_max_over_two_gloo_ranks():
         p.join(timeout=120)
         assert p.exitcode == 0
     assert got == [(0, 2.5), (1, 2.5)]
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm builds its workload on the oracle's mesh and times only oracle code: the
+    product's shared library must never be mapped into its process."""
+    code = ("import sys, json; sys.argv=['bench.py','--impl','reference','--workload','waveguide','--steps','1',"
+            "'--warmup','0']; import bench; bench.main(); maps=open('/proc/self/maps').read(); "
+            "print('LOADED' if 'libfem2d_gb300' in maps else 'CLEAN')")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().splitlines()[-1] == "CLEAN"
+    line = _json_lines(r.stdout)[0]
+    assert line["config"]["basis"] == "HierPoly" and line["config"]["glq"] == [8, 8]
+
+
+def test_reference_arm_unavailable_line_from_fixture():
+    """At the full-form 1M workload the committed oracle fixture's single-step time rules out the
+    driver's step count: the arm prints one reasoned `unavailable` line and exits 0."""
+    if not os.path.exists(os.path.join(ROOT, "tests", "golden", "full_form_full_1m.json")):
+        pytest.skip("full_1m oracle fixture not generated")
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "20", "--warmup", "5"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1 and lines[0]["impl"] == "reference"
+    assert "unavailable" in lines[0] and lines[0]["config"]["ndofs"] == 1070625
+
+
+def test_workload_scripts_identical_on_oracle_and_product_meshes():
+    sys.path.insert(0, ROOT)
+    from fem_2d_gb300 import configs
+    from oracle import ref
+
+    for make in (lambda r: configs.precision(replay=r), lambda r: configs.waveguide_small(replay=r),
+                 lambda r: configs.full_scale(seed=0, nx=16, ny=8, rounds=3, fraction=0.44, replay=r),
+                 lambda r: configs.learned_family(4, 8, 4, replay=r), lambda r: configs.batch_member(3, replay=r)):
+        assert make(configs.NativeReplay).ops == make(ref.OracleReplay).ops
