@@ -42,7 +42,7 @@ class _fem2d_solve_opts(ctypes.Structure):
     _fields_ = [("precond", ctypes.c_int), ("max_outer", ctypes.c_int), ("max_inner", ctypes.c_int),
                 ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("block", ctypes.c_int),
                 ("verbose", ctypes.c_int), ("krylov_steps", ctypes.c_int),
-                ("damping", ctypes.c_double), ("scaling", ctypes.c_int)]
+                ("damping", ctypes.c_double), ("scaling", ctypes.c_int), ("dense", ctypes.c_int)]
 
 
 class _fem2d_solve_stats(ctypes.Structure):
@@ -98,6 +98,9 @@ def lib():
         "fem2d_gep_recompute": (ctypes.c_int, [P, P]),
         "fem2d_gep_values_noalloc": (ctypes.c_int, [P, P, ctypes.c_void_p, ctypes.c_void_p]),
         "fem2d_gep_set_upper_values": (ctypes.c_int, [P, dp, dp]),
+        "fem2d_domain_table_doubles": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]),
+        "fem2d_block_gram_device": (ctypes.c_int, [P, ctypes.c_int, i64, ctypes.c_void_p, i64, ctypes.c_int,
+                                                   ctypes.c_void_p, i64, ctypes.c_int, ctypes.c_void_p]),
         "fem2d_galerkin_sample_gep_hcurl_batch": (ctypes.c_int, [P, PP, i64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                           ctypes.c_int, PP, dp]),
         "fem2d_gep_batch_recompute": (ctypes.c_int, [P, PP, i64, ctypes.c_int, dp]),
@@ -379,6 +382,14 @@ class Domain:
         out = np.zeros((n, 6), dtype=np.int64)
         _check(lib().fem2d_domain_basis_specs(self._h, _ptr(out, ctypes.c_int64)))
         return out
+
+
+def domain_table_doubles(domain, bspace, glq=(0, 0)):
+    """FP64 contraction-table size (doubles) a GEP of this Domain needs with basis space ``bspace``
+    (HierPoly or KOLeg) and GLQ sizes ``glq`` (host only, no GPU)."""
+    out = ctypes.c_int64(0)
+    _check(lib().fem2d_domain_table_doubles(domain._h, int(bspace.ID), int(glq[0]), int(glq[1]), ctypes.byref(out)))
+    return out.value
 
 
 def domain_pattern(domain):
@@ -767,19 +778,29 @@ def nalgebra_solve_gep(gep, target_eigenvalue):
 
 
 PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
+GRAM_TENSOR, GRAM_FP64 = 0, 1
+
+
+def block_gram_device(ctx, method, n, d_x, ldx, a, d_y, ldy, b, d_c):
+    """C = X^T Y on device blocks (raw pointers, row-major): method GRAM_TENSOR (tcgen05 FP64 emulation)
+    or GRAM_FP64 (CUDA cores). Synchronises."""
+    _check(lib().fem2d_block_gram_device(ctx._h, int(method), int(n), ctypes.c_void_p(d_x), int(ldx), int(a),
+                                         ctypes.c_void_p(d_y), int(ldy), int(b), ctypes.c_void_p(d_c)))
 
 
 def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOBI, tol=0.0, max_outer=0,
-                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0, damping=0.0, scaling=0):
+                    max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0, damping=0.0, scaling=0,
+                    dense=0):
     """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
-    the context the GEP was built on)."""
+    the context the GEP was built on). dense=1 keeps the Gram products on the FP64 CUDA cores instead of
+    the tensor-core FP64 emulation."""
     ctx = ctx or gep.ctx
     n = gep.dimension
     vals = np.zeros(n_pairs)
     vecs = np.zeros((n_pairs, n))
     res = np.zeros(n_pairs)
     o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose, krylov_steps, damping,
-                          scaling)
+                          scaling, dense)
     st = _fem2d_solve_stats()
     _check(lib().fem2d_gpu_solve_gep(ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
                                      _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),

@@ -491,6 +491,18 @@ static void check_galerkin_args(const fem2d_domain* d, int basis, int nq_u, int 
   if (d->d.ndofs >= (1ll << 31)) fail(FEM2D_E_INVALID_ARG, "more than 2^31 DoFs");
 }
 
+int fem2d_domain_table_doubles(const fem2d_domain* d, int basis, int nq_u, int nq_v, int64_t* doubles) {
+  API_BEGIN
+  if (!d || !doubles) fail(FEM2D_E_INVALID_ARG, "null argument");
+  check_galerkin_args(d, basis, nq_u, nq_v);
+  HostGEP h;
+  build_symbolic(d->d, basis, nq_u, nq_v, h);
+  const int64_t P = h.pmax + 1;
+  *doubles = 2 * (int64_t)h.ivl_s.size() * 5 * P * P;
+  API_END
+}
+
+
 static void batch_report_out(const BatchReport& r, double* report) {
   if (!report) return;
   report[0] = r.ms_tables;
@@ -796,6 +808,17 @@ int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c
   if (g->ctx->device != c->c.device) fail(FEM2D_E_INVALID_ARG, "the GEP lives on another device");
   FEM2D_CUDA(cudaSetDevice(c->c.device));
   gep_spmm(c->c, g->h, g->d, c_a, c_b, d_x, ldx, nb, d_y, ldy);
+  API_END
+}
+
+int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
+                            const double* d_y, int64_t ldy, int b, double* d_c) {
+  API_BEGIN
+  if (!c || !d_x || !d_y || !d_c) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (n < 0 || a < 1 || b < 1 || ldx < a || ldy < b) fail(FEM2D_E_INVALID_ARG, "bad block sizes");
+  if (method != 0 && method != 1) fail(FEM2D_E_INVALID_ARG, "method must be 0 (tensor) or 1 (FP64)");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  block_gram(c->c, method, n, d_x, ldx, a, d_y, ldy, b, d_c);
   API_END
 }
 

@@ -31,6 +31,7 @@
 
 #include "blockscale.h"
 #include "eigen.h"
+#include "ozaki.h"
 #include "mf.h"
 #include "mfdev.h"
 #include "symeig.h"
@@ -396,7 +397,32 @@ struct Dev {
   const double* vb;
   DBuf<double> part;
   DBuf<double> small;
+  int dense_mode = 0;    // Gram products: 0 FP64 emulated on the tensor cores (ozaki.cu), 1 FP64 CUDA cores
+  DBuf<double> ozw;      // tensor Gram workspace (partial tiles)
+  DBuf<int> ozerr;       // set by the tensor Gram kernel when a bounded wait expired
   int grid_rows() const { return std::max(1, c.num_sms * 2); }
+
+  // C (device, a x b) = X^T Y on the tensor cores; false when the FP64 CUDA-core kernels must be used
+  bool tensor_gram(const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b, double* Cd) {
+    if (dense_mode != 0 || a > 512 || b > 256 || a <= 0 || b <= 0) return false;
+    ProfScope ps(c, "gram_tc", 8.0 * h.n * (a + b), 2.0 * h.n * a * b);
+    const size_t need = ozaki_gram_workspace(h.n, a, b, c.num_sms);
+    if (ozw.n < need) ozw.alloc_on(std::max(need, ozaki_gram_workspace(h.n, 160, 160, c.num_sms)), c.stream);
+    if (ozerr.n == 0) {
+      ozerr.alloc_on(1, c.stream);
+      FEM2D_CUDA(cudaMemsetAsync(ozerr.p, 0, sizeof(int), c.stream));
+    }
+    ozaki_gram(c, h.n, X, ldx, a, Y, ldy, b, Cd, ozw.p, ozw.n, ozerr.p);
+    return true;
+  }
+  // the tensor Gram kernel's error flag (synchronises the stream)
+  void check_tensor() {
+    if (ozerr.n == 0) return;
+    int e = 0;
+    FEM2D_CUDA(cudaMemcpyAsync(&e, ozerr.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+    if (e) fail(FEM2D_E_TIMEOUT, "tensor-core Gram kernel: a bounded wait expired");
+  }
 
   void spmm(double ca, double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
     const double nv = (ca != 0.0) + (cb != 0.0);
@@ -424,10 +450,18 @@ struct Dev {
   }
   // C (a x b, host row-major) = X^T Y
   void gram(const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b, std::vector<double>& C) {
+    const int ab = a * b;
+    if (small.n < (size_t)ab) small.alloc_on(std::max<size_t>(ab, 16384), c.stream);
+    if (tensor_gram(X, ldx, a, Y, ldy, b, small.p)) {
+      C.resize(ab);
+      FEM2D_CUDA(cudaMemcpyAsync(C.data(), small.p, ab * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      check_tensor();
+      return;
+    }
     ProfScope ps(c, "dense_block", 8.0 * h.n * (a + b), 2.0 * h.n * a * b);
     const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
     const int64_t rpb = (h.n + nblk - 1) / nblk;
-    const int ab = a * b;
+
     if (part.n < (size_t)nblk * ab) part.alloc_on((size_t)nblk * ab, c.stream);
     if (small.n < (size_t)ab) small.alloc_on(std::max<size_t>(ab, 16384), c.stream);
     const size_t smem = (size_t)32 * (a + b) * sizeof(double);
@@ -469,6 +503,7 @@ struct Dev {
   }
   // C (a x b, device, row-major) = X^T Y without leaving the device
   void gram_dev(const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b, double* Cd) {
+    if (tensor_gram(X, ldx, a, Y, ldy, b, Cd)) return;
     ProfScope ps(c, "dense_block", 8.0 * h.n * (a + b), 2.0 * h.n * a * b);
     const int nblk = std::min<int64_t>(grid_rows(), std::max<int64_t>(1, (h.n + 255) / 256));
     const int64_t rpb = (h.n + nblk - 1) / nblk;
@@ -654,6 +689,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   auto t1 = std::chrono::steady_clock::now();
 
   Dev D{c, h, d, sa.p, sb.p};
+  D.dense_mode = o.dense;
   DBuf<double> V, AV, BV, X, AX, BX, G0, W1, W2, W3;
   V.alloc_on((size_t)n * mmax, c.stream);
   AV.alloc_on((size_t)n * mmax, c.stream);
@@ -1325,6 +1361,26 @@ void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP&
     // small systems the sparse plan cannot solve accurately are redone with one dense front
     if (worst <= 1e-10 || plan.dense || n > 4096) break;
   }
+}
+
+}  // namespace fem2d
+
+namespace fem2d {
+
+// C (device, row-major a x b) = X^T Y with the FP64 CUDA-core kernels (method 1) or the tensor-core
+// emulation (method 0); synchronises
+void block_gram(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Y, int64_t ldy,
+                int b, double* Cd) {
+  setup_gemm_smem(c.device);
+  HostGEP hg;
+  hg.n = n;
+  DeviceGEP dg;
+  Dev D{c, hg, dg, nullptr, nullptr};
+  D.dense_mode = method == 0 ? 0 : 1;
+  if (method == 0 && (a > 512 || b > 256)) fail(FEM2D_E_INVALID_ARG, "tensor Gram: a <= 512 and b <= 256");
+  D.gram_dev(X, ldx, a, Y, ldy, b, Cd);
+  D.check_tensor();
+  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
 }
 
 }  // namespace fem2d

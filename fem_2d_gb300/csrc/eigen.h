@@ -19,5 +19,8 @@ void gep_spmm(Ctx& c, const HostGEP& h, const DeviceGEP& d, double ca, double cb
 void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double ca,
                    double cb, bool spd,
                    int nrhs, const double* rhs, double* x);
+// C (device, row-major a x b) = X^T Y: method 0 on the tensor cores (ozaki.cu), 1 on the FP64 CUDA cores
+void block_gram(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Y, int64_t ldy,
+                int b, double* Cd);
 
 }  // namespace fem2d

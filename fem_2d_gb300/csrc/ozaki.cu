@@ -1,0 +1,422 @@
+// FP64 block Gram products C = X^T Y on the 5th-generation tensor cores (tcgen05, sm_103a) by exact
+// integer slicing (the Ozaki scheme).
+//
+// The eigensolver's B-orthogonalisation and Rayleigh-Ritz steps form C (a x b) = X^T Y for tall
+// blocks X (n x a) and Y (n x b) with n up to ~1e6 and a, b <= 160. GB300 runs FP64 on its CUDA cores
+// at ~1 TFLOP/s, against ~2 PFLOP/s of BF16 tensor throughput, so these products are FP64-bound by
+// a wide margin. Here every FP64 value is written exactly as a sum of eight signed 7-bit digits
+// relative to the largest magnitude of its column within a 128-row chunk:
+//
+//     x = 2^(E - 1022) * sum_{s<8} d_s 2^(-7(s+1)),   |d_s| <= 127   (56 bits, FP64 has 53)
+//
+// Digits are integers, so they are exact in BF16, and a digit product is an integer below 2^14.
+// Products of digit pairs (s, t) with s + t = g are summed into one FP32 accumulator g in TMEM by
+// tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulation); with at most 8 pairs per g and 128 rows
+// per chunk every partial sum stays below 2^24, so the FP32 accumulation is exact. Pairs with
+// s + t >= 8 are dropped: the truncation error is below 2^-52 of |x_max| |y_max| of the chunk, i.e.
+// at FP64 rounding level in the normwise sense. After each chunk the eight exact accumulators are
+// combined exactly into two int64 sums and added, scaled, into FP64 register accumulators. Cost per
+// output element and chunk: 36 digit-pair MMAs on the tensor pipe, and on the FP64 pipe two
+// conversions and two FMAs instead of 128 FMAs.
+//
+// One CTA (4 warps, one row of C per thread) owns a 128 x 32 tile of C and a range of rows of X and
+// Y. Per 128-row chunk: a pass over the chunk finds each column's exponent; then four 32-row
+// sub-blocks are sliced into shared memory (8 digit planes per operand, K-major core-matrix layout
+// without swizzle) and thread 0 issues the 72 MMAs of the sub-block; their completion is tracked by
+// an mbarrier. Partial tiles of all CTAs are summed by a second, deterministic kernel.
+//
+// Every wait on the mbarrier is bounded (about one second of GPU time): on expiry the kernel raises
+// an error flag, waits once more (bounded) for its MMAs in flight, frees its TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "device.h"
+#include "ozaki.h"
+
+namespace fem2d {
+
+namespace {
+
+constexpr int kDigits = 8;     // digits per FP64 value
+constexpr int kChunk = 128;    // rows per exact accumulation
+constexpr int kSub = 32;       // rows per shared-memory sub-block
+constexpr int kM = 128;        // tile rows (columns of X)
+constexpr int kN = 32;         // tile columns (columns of Y)
+constexpr int kThreads = 128;
+constexpr uint32_t kTmemCols = kDigits * kN;   // one FP32 accumulator of kN columns per digit sum
+constexpr int kPlaneA = kM * kSub * 2;         // bytes of one digit plane of X (128 rows x 32 bf16)
+constexpr int kPlaneB = kN * kSub * 2;         // bytes of one digit plane of Y
+constexpr int kSmemBytes = kDigits * (kPlaneA + kPlaneB) + 1024;
+constexpr uint64_t kWaitNs = 1000000000ull;    // bounded waits: 1 s
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// shared-memory matrix descriptor: no swizzle, K-major core matrices of 8 rows x 16 bytes;
+// lbo = byte distance between core matrices adjacent in K, sbo = between 8-row groups
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+  d |= (uint64_t)1 << 46;   // descriptor version of the sm_100 family; base offset 0, no swizzle
+  return d;
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t instr_desc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for the mbarrier phase; false when the time limit passed
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  if (mbar_try(mbar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (!mbar_try(mbar, parity))
+    if (global_ns() - t0 > kWaitNs) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int q = 0; q < 8; q++) v[q] = __uint_as_float(r[q]);
+}
+
+// the eight digits of v relative to the biased exponent E of its column's largest magnitude
+__device__ __forceinline__ void digits8(double v, int E, float (&d)[kDigits]) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  const int shift = E - ex;
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const unsigned long long A = (ex == 0 || shift > 55) ? 0ull : ((mant << 3) >> shift);
+  const bool neg = (bits >> 63) != 0;
+#pragma unroll
+  for (int s = 0; s < kDigits; s++) {
+    const int dg = (int)((A >> (49 - 7 * s)) & 0x7F);
+    d[s] = (float)(neg ? -dg : dg);
+  }
+}
+
+__device__ __forceinline__ int biased_exp(double v) {
+  return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF);
+}
+
+// 2^e as a double (0 below the normal range)
+__device__ __forceinline__ double pow2(int e) {
+  if (e < -1022) return 0.0;
+  if (e > 1023) e = 1023;
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// byte offset of core matrix (row group rg, k group kg) in a K-major tile with kSub columns
+__device__ __forceinline__ int core_off(int rg, int kg) { return (rg * (kSub / 8) + kg) * 128; }
+
+__global__ void __launch_bounds__(kThreads, 2)
+    ozaki_gram_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ Y,
+                      int64_t ldy, int b, int64_t rows_per_cta, double* __restrict__ P, int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;                                   // kDigits planes of kM x kSub bf16
+  uint8_t* sB = smem + kDigits * kPlaneA;               // kDigits planes of kN x kSub bf16
+  int* eX = reinterpret_cast<int*>(sB + kDigits * kPlaneB);   // kM column exponents of the chunk
+  int* eY = eX + kM;                                    // kN
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(eY + kN);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int col0 = blockIdx.z * kM;    // first column of X in this tile
+  const int cy0 = blockIdx.y * kN;     // first column of Y
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
+  const int64_t r1 = min(n, r0 + rows_per_cta);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t mb = smem_addr(mbar);
+  uint32_t phase = 0;
+  bool failed = false;
+
+  double acc[kN];
+#pragma unroll
+  for (int j = 0; j < kN; j++) acc[j] = 0.0;
+
+  const int my_col = col0 + tid;   // this thread's column of X (its row of C)
+  const bool col_ok = my_col < a;
+  constexpr uint32_t idesc = instr_desc(kM, kN);
+
+  for (int64_t c0 = r0; c0 < r1 && !failed; c0 += kChunk) {
+    const int rows = (int)min((int64_t)kChunk, r1 - c0);
+    // column exponents of the chunk
+    // (loads issued 16 at a time so that many are in flight: this pass is latency-bound otherwise)
+    {
+      int e = 0;
+      if (col_ok) {
+        const double* xp = X + c0 * ldx + my_col;
+        int r = 0;
+        for (; r + 16 <= rows; r += 16) {
+          double v[16];
+#pragma unroll
+          for (int q = 0; q < 16; q++) v[q] = __ldg(xp + (int64_t)(r + q) * ldx);
+#pragma unroll
+          for (int q = 0; q < 16; q++) e = max(e, biased_exp(v[q]));
+        }
+        for (; r < rows; r++) e = max(e, biased_exp(__ldg(xp + (int64_t)r * ldx)));
+      }
+      eX[tid] = e;
+      if (tid < kN) eY[tid] = 0;
+    }
+    __syncthreads();
+    {
+      const int j = tid % kN, part = tid / kN;   // 4 threads per column of Y, 32 rows each
+      int e = 0;
+      if (cy0 + j < b) {
+        const double* yp = Y + c0 * ldy + cy0 + j;
+        const int rb = part * 32, re = min(rows, part * 32 + 32);
+        int r = rb;
+        for (; r + 16 <= re; r += 16) {
+          double v[16];
+#pragma unroll
+          for (int q = 0; q < 16; q++) v[q] = __ldg(yp + (int64_t)(r + q) * ldy);
+#pragma unroll
+          for (int q = 0; q < 16; q++) e = max(e, biased_exp(v[q]));
+        }
+        for (; r < re; r++) e = max(e, biased_exp(__ldg(yp + (int64_t)r * ldy)));
+      }
+      atomicMax(&eY[j], e);
+    }
+    __syncthreads();
+    const int Ex = eX[tid];
+    for (int sb = 0; sb < kChunk / kSub && !failed; sb++) {
+      const int64_t s0 = c0 + sb * kSub;
+      // X digits: this thread's column, 32 rows = 4 core matrices along K per digit plane
+      double xv[kSub];   // this thread's 32 values of the sub-block, all loads issued before use
+#pragma unroll
+      for (int r = 0; r < kSub; r++) {
+        const int64_t ra = s0 + r;
+        xv[r] = (col_ok && ra < r1) ? __ldg(X + ra * ldx + my_col) : 0.0;
+      }
+#pragma unroll
+      for (int kg = 0; kg < kSub / 8; kg++) {
+        uint32_t pk[kDigits][4];
+#pragma unroll
+        for (int r8 = 0; r8 < 8; r8 += 2) {
+          float d0[kDigits], d1[kDigits];
+          const double va = xv[kg * 8 + r8];
+          const double vb = xv[kg * 8 + r8 + 1];
+          digits8(va, Ex, d0);
+          digits8(vb, Ex, d1);
+#pragma unroll
+          for (int s = 0; s < kDigits; s++) pk[s][r8 >> 1] = pack_bf16(d0[s], d1[s]);
+        }
+        const int off = core_off(tid >> 3, kg) + (tid & 7) * 16;
+#pragma unroll
+        for (int s = 0; s < kDigits; s++)
+          *reinterpret_cast<uint4*>(sA + s * kPlaneA + off) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+      }
+      // Y digits: column j, one k group of 8 rows per thread
+      {
+        const int j = tid % kN, kg = tid / kN;
+        const int Ey = eY[j];
+        const bool ok = cy0 + j < b;
+        uint32_t pk[kDigits][4];
+        double yv[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          const int64_t ra = s0 + kg * 8 + r;
+          yv[r] = (ok && ra < r1) ? __ldg(Y + ra * ldy + cy0 + j) : 0.0;
+        }
+#pragma unroll
+        for (int r8 = 0; r8 < 8; r8 += 2) {
+          float d0[kDigits], d1[kDigits];
+          const double va = yv[r8];
+          const double vb = yv[r8 + 1];
+          digits8(va, Ey, d0);
+          digits8(vb, Ey, d1);
+#pragma unroll
+          for (int s = 0; s < kDigits; s++) pk[s][r8 >> 1] = pack_bf16(d0[s], d1[s]);
+        }
+        const int off = core_off(j >> 3, kg) + (j & 7) * 16;
+#pragma unroll
+        for (int s = 0; s < kDigits; s++)
+          *reinterpret_cast<uint4*>(sB + s * kPlaneB + off) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+      }
+      // the generic-proxy stores above must be visible to the tensor core's (async) proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        const uint32_t aBase = smem_addr(sA), bBase = smem_addr(sB);
+#pragma unroll 1
+        for (int g = 0; g < kDigits; g++)
+          for (int s = 0; s <= g; s++) {
+            const int t = g - s;
+#pragma unroll
+            for (int kk = 0; kk < kSub / 16; kk++) {
+              const uint64_t da = smem_desc(aBase + s * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
+              const uint64_t db = smem_desc(bBase + t * kPlaneB + kk * 256, 128, (kSub / 8) * 128);
+              const uint32_t accum = (sb > 0 || s > 0 || kk > 0) ? 1u : 0u;
+              mma_bf16(tmem + (uint32_t)(g * kN), da, db, idesc, accum);
+            }
+          }
+        mma_commit(mb);
+      }
+      // the MMAs read the digit planes: wait before the next sub-block overwrites them
+      if (!mbar_wait(mb, phase)) failed = true;
+      phase ^= 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (failed) break;
+    // combine the eight exact digit-sum accumulators of this chunk (this thread's row, 8 columns at
+    // a time). acc_g <= (g + 1) 128 127^2 < 2^24; in int64, exactly,
+    //   T_hi = sum_{g<4} acc_g 2^(7 (3 - g)) < 2^43,   T_lo = sum_{g>=4} acc_g 2^(7 (7 - g)) < 2^47,
+    // and the chunk's contribution is (T_hi + T_lo 2^-28) 2^-35 2^(Ex - 1022) 2^(Ey - 1022)
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int cb = 0; cb < kN; cb += 8) {
+      long long Th[8], Tl[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) Th[q] = Tl[q] = 0;
+#pragma unroll
+      for (int g = 0; g < kDigits; g++) {
+        float v[8];
+        tmem_ld8(lane_base + (uint32_t)(g * kN + cb), v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const long long iv = (long long)__float2int_rn(v[q]);
+          if (g < 4) Th[q] += iv << (7 * (3 - g));
+          else Tl[q] += iv << (7 * (7 - g));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int j = cb + q;
+        const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
+        acc[j] = fma(t, pow2(Ex + eY[j] - 2044 - 35), acc[j]);
+      }
+    }
+    // every thread's TMEM reads are complete before the next chunk's MMAs overwrite the accumulators
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (failed) {
+    atomicOr(err, 1);
+    mbar_wait(mb, phase ^ 1);   // bounded: let MMAs still in flight finish before TMEM is freed
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  // this CTA's partial tile (kM x kN, row-major)
+  const int64_t tile = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  double* out = P + tile * (kM * kN) + (int64_t)tid * kN;
+#pragma unroll
+  for (int j = 0; j < kN; j++) out[j] = acc[j];
+}
+
+// C[i * b + j] (row-major a x b) = sum over the CTAs of row range of the partial tiles
+__global__ void ozaki_reduce_kernel(const double* __restrict__ P, int nrb, int ny, int a, int b, double* __restrict__ C) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a * b) return;
+  const int i = e / b, j = e % b;
+  const int mz = i / kM, nyi = j / kN;
+  const int64_t base = (((int64_t)mz * ny + nyi) * nrb) * (kM * kN) + (int64_t)(i % kM) * kN + (j % kN);
+  double s = 0.0;
+  for (int k = 0; k < nrb; k++) s += P[base + (int64_t)k * (kM * kN)];
+  C[e] = s;
+}
+
+std::mutex g_attr_mu;
+bool g_attr_done[256] = {};
+
+}  // namespace
+
+int ozaki_gram_partials(int64_t n, int a, int b, int num_sms) {
+  const int tiles = ((a + kM - 1) / kM) * ((b + kN - 1) / kN);
+  const int64_t chunks = std::max<int64_t>(1, (n + kChunk - 1) / kChunk);
+  // two CTAs per SM (83 KB of shared memory and 256 TMEM columns each): one slices while the other
+  // waits on its loads or MMAs
+  const int64_t per = std::max<int64_t>(1, 2 * num_sms / tiles);
+  return (int)std::min<int64_t>(per, chunks);
+}
+
+size_t ozaki_gram_workspace(int64_t n, int a, int b, int num_sms) {
+  const int tiles = ((a + kM - 1) / kM) * ((b + kN - 1) / kN);
+  return (size_t)ozaki_gram_partials(n, a, b, num_sms) * tiles * kM * kN;
+}
+
+void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b,
+                double* C, double* work, size_t work_doubles, int* err) {
+  if (a <= 0 || b <= 0) return;
+  if (a > 4 * kM || b > 8 * kN) fail(FEM2D_E_INVALID_ARG, "ozaki_gram: block wider than 512 x 256");
+  {
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (c.device >= 0 && c.device < 256 && !g_attr_done[c.device]) {
+      FEM2D_CUDA(cudaFuncSetAttribute(ozaki_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+      g_attr_done[c.device] = true;
+    }
+  }
+  const int nrb = ozaki_gram_partials(n, a, b, c.num_sms);
+  const int mz = (a + kM - 1) / kM, ny = (b + kN - 1) / kN;
+  if (work_doubles < (size_t)nrb * mz * ny * kM * kN) fail(FEM2D_E_INVALID_ARG, "ozaki_gram: workspace too small");
+  int64_t rpc = (std::max<int64_t>(n, 1) + nrb - 1) / nrb;
+  rpc = (rpc + kChunk - 1) / kChunk * kChunk;
+  dim3 grid(nrb, ny, mz);
+  ozaki_gram_kernel<<<grid, kThreads, kSmemBytes, c.stream>>>(n, X, ldx, a, Y, ldy, b, rpc, work, err);
+  FEM2D_CUDA(cudaGetLastError());
+  ozaki_reduce_kernel<<<(a * b + 255) / 256, 256, 0, c.stream>>>(work, nrb, ny, a, b, C);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches += 2;
+}
+
+}  // namespace fem2d

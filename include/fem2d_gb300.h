@@ -159,6 +159,11 @@ int fem2d_gep_recompute(fem2d_ctx* c, fem2d_gep* g);
  * current device is restored on return. Returns after the work is queued on the context's stream;
  * synchronise before reading d_a and d_b. No cudaMalloc, cudaFree or other allocating call is made. */
 int fem2d_gep_values_noalloc(fem2d_ctx* c, const fem2d_gep* g, double* d_a, double* d_b);
+/* The FP64 contraction-table size (doubles) a GEP of this Domain needs: 2 x intervals x 5 x
+ * (max order + 1)^2, the quantity fem2d_gep_values_noalloc checks against its capacity. Runs the host
+ * symbolic phase only (no GPU needed); errors as fem2d_galerkin_sample_gep_hcurl's argument checks.
+ * No counterpart in the reference. */
+int fem2d_domain_table_doubles(const fem2d_domain* d, int basis, int nq_u, int nq_v, int64_t* doubles);
 /* galerkin_sample_gep_hcurl over many Domains at once (galerkin.rs:33-187 per Domain; the reference
  * has no batched form: a caller loops over Domains). Each Domain gets its own host symbolic phase and
  * its own GEP (out[i], freed with fem2d_gep_free); the device numeric phase of ALL of them is two
@@ -227,6 +232,15 @@ int fem2d_gep_shifted_solve(fem2d_ctx* c, const fem2d_gep* g, double c_a, double
  * d_x and d_y must not overlap. Queued on the context's stream; returns without synchronising. */
 int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c_b, const double* d_x, int64_t ldx,
                           int nb, double* d_y, int64_t ldy);
+/* C = X^T Y for device blocks X (n x a, row-major, leading dimension ldx) and Y (n x b, ldy) into the
+ * device array d_c (a x b, row-major): the block Gram product of gpu_solve_gep's B-orthogonalisation
+ * and Rayleigh-Ritz steps (no counterpart in the reference, whose eigensolve runs in an external
+ * process), exposed for checking and timing. method 0: FP64 emulated on the tensor cores (tcgen05 MMA
+ * on exact 7-bit digit slices with exact FP32 accumulation; a <= 512, b <= 256; normwise accuracy at
+ * FP64 rounding level), method 1: FP64 on the CUDA cores. Synchronises; FEM2D_E_TIMEOUT if a bounded
+ * wait inside the tensor kernel expired. */
+int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
+                            const double* d_y, int64_t ldy, int b, double* d_c);
 typedef struct fem2d_solve_opts {
   int precond;          /* reserved: the eigensolve's shifted systems are solved exactly (multifrontal LU);
                            the iterative inner solver with its preconditioners is fem2d_pcg_* */
@@ -243,6 +257,9 @@ typedef struct fem2d_solve_opts {
                            row-run blocks when the Jacobi-scaled factorizations are inaccurate),
                            1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's diagonal blocks
                            over runs of rows with one column list) */
+  int dense;            /* Gram products of the B-orthogonalisation and Rayleigh-Ritz steps: 0 = FP64
+                           emulated on the tensor cores (tcgen05, exact integer slicing; default),
+                           1 = FP64 CUDA cores */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {

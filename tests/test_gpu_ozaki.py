@@ -1,0 +1,79 @@
+"""The tensor-core FP64 Gram product (tcgen05 MMA on exact 7-bit digit slices, ozaki.cu) against
+FP64 references: numpy's X^T Y and the library's FP64 CUDA-core kernel, through the C ABI
+(fem2d_block_gram_device). The slicing error is bounded per 128-row chunk by 2^-49 times
+rows x max|x_i| x max|y_j| of the chunk; the tests hold the result to that bound (plus the reference's
+own rounding), and to 1e-13 of |X|^T |Y| for well-scaled data."""
+import numpy as np
+import pytest
+
+import fem_2d_gb300 as fg
+
+pytestmark = pytest.mark.gpu
+
+
+def _chunk_bound(X, Y, chunk=128):
+    n = X.shape[0]
+    bound = np.zeros((X.shape[1], Y.shape[1]))
+    for c0 in range(0, n, chunk):
+        xs, ys = X[c0:c0 + chunk], Y[c0:c0 + chunk]
+        bound += len(xs) * np.outer(np.max(np.abs(xs), axis=0), np.max(np.abs(ys), axis=0))
+    return 2.0 ** -49 * bound
+
+
+def _gram(ctx, method, X, Y):
+    torch = pytest.importorskip("torch")
+    dx = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    dy = torch.from_numpy(np.ascontiguousarray(Y)).cuda()
+    dc = torch.full((X.shape[1], Y.shape[1]), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    fg.block_gram_device(ctx, method, X.shape[0], dx.data_ptr(), X.shape[1], X.shape[1], dy.data_ptr(), Y.shape[1],
+                         Y.shape[1], dc.data_ptr())
+    return dc.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return fg.Context(0)
+
+
+@pytest.mark.parametrize("n,a,b", [(1, 1, 1), (129, 5, 3), (100003, 150, 30), (20000, 150, 150), (4096, 300, 40)])
+def test_tensor_gram_gaussian(ctx, n, a, b):
+    rng = np.random.default_rng(n + a + b)
+    X = rng.standard_normal((n, a))
+    Y = rng.standard_normal((n, b))
+    ref = X.T @ Y
+    absref = np.abs(X).T @ np.abs(Y)
+    C0 = _gram(ctx, fg.GRAM_TENSOR, X, Y)
+    C1 = _gram(ctx, fg.GRAM_FP64, X, Y)
+    assert np.all(np.isfinite(C0))
+    assert np.max(np.abs(C0 - ref) / absref) < 1e-13
+    assert np.max(np.abs(C1 - ref) / absref) < 1e-13
+    assert np.all(np.abs(C0 - ref) <= _chunk_bound(X, Y) + 1e-15 * n * absref)
+    # deterministic: the same call gives the same bits
+    assert np.array_equal(C0, _gram(ctx, fg.GRAM_TENSOR, X, Y))
+
+
+def test_tensor_gram_wide_dynamic_range(ctx):
+    """Rows scaled over 30 orders of magnitude, exact zeros and negative values: the per-chunk column
+    scaling keeps the error within the chunk bound."""
+    rng = np.random.default_rng(5)
+    n, a, b = 50000, 64, 24
+    X = rng.standard_normal((n, a)) * 10.0 ** rng.uniform(-15, 15, size=(n, 1))
+    Y = rng.standard_normal((n, b)) * 10.0 ** rng.uniform(-15, 15, size=(n, 1))
+    X[::7, 3] = 0.0
+    Y[:, 5] = 0.0
+    ref = X.T @ Y
+    C0 = _gram(ctx, fg.GRAM_TENSOR, X, Y)
+    bound = _chunk_bound(X, Y) + 1e-15 * n * (np.abs(X).T @ np.abs(Y))
+    assert np.all(np.abs(C0 - ref) <= bound)
+    assert np.all(C0[:, 5] == 0.0)
+
+
+def test_tensor_gram_symmetric_products(ctx):
+    """X^T X (the B-orthogonalisation Gram form) is symmetric to rounding and positive on the diagonal."""
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal((30000, 40))
+    G = _gram(ctx, fg.GRAM_TENSOR, X, X)
+    assert np.max(np.abs(G - G.T)) <= 1e-13 * np.max(np.abs(G))
+    d = np.sum(X * X, axis=0)
+    assert np.all(np.abs(np.diag(G) - d) <= np.diag(_chunk_bound(X, X)) + 1e-15 * X.shape[0] * d)

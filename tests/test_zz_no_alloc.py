@@ -67,8 +67,9 @@ def test_values_noalloc_matches_recompute():
 
 
 def _too_large_workload():
-    """Two Elems: Elem 0 at expansion order 20 (table stride 21), Elem 1 at order 2 split seven times
-    along u (254 dyadic sub-intervals): 2 x 255 x 5 x 21^2 table doubles, above the 524,288 limit."""
+    """Two Elems: Elem 0 at expansion order 20 (table stride 21), Elem 1 at order 2 refined seven times
+    with V refinements of all its leaves (1,528 DoFs): 568,890 table doubles, above the 524,288 limit
+    (checked on the host by tests/test_host_tables.py)."""
     m_json = configs.grid_mesh_json(2, 1, 0.0, 2.0, 0.0, 1.0)
     ops = [("orders", 2, 2, None), ("orders", 20, 20, [0])]
     m = configs.NativeReplay(m_json)
@@ -76,7 +77,7 @@ def _too_large_workload():
     for _ in range(7):
         info = m.elem_info()
         leaves = [int(e) for e in np.nonzero(info[:, 0] == 1)[0] if e != 0]
-        op = ("href", 1, leaves, -1)
+        op = ("hmix", leaves, [2] * len(leaves))
         m.apply([op])
         ops.append(op)
     return configs.Workload("too_large_tables", m_json, ops, basis=0, glq=(10, 10))
