@@ -585,13 +585,14 @@ def _cluster_bounds(th_sel, rb, th_all, rel_tol=1e-6):
 
 
 def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1e-6, tol=1e-13, seed=0,
-                            refine=2, reject=1e-2):
+                            refine=2, reject=1e-2, pivot=0.1):
     """Second, independent FP64 sparse oracle for large pencils: ARPACK (implicitly restarted Lanczos
     in the B inner product, through scipy ``eigsh``) on T = (A - sigma B)^-1 A (A + c B)^-1 B.
 
     T's eigenvalues mu = lambda / ((lambda - sigma)(lambda + c)) vanish on the curl null space and grow
     without bound as lambda nears sigma, so the largest |mu| are the physical modes near sigma. The
-    solves are SuperLU factorizations under ``perm``. The k + extra Lanczos vectors X are then refined
+    solves are SuperLU factorizations under ``perm`` (threshold ``pivot`` for row pivoting: a smaller one
+    keeps more diagonal pivots and less fill). The k + extra Lanczos vectors X are then refined
     ``refine`` times by one Rayleigh-Ritz step on (A, B) over span[X, T X] in FP64, and the k Ritz
     values nearest sigma with |lambda| > spurious |sigma| and relative residual below ``reject`` are
     returned with:
@@ -609,9 +610,9 @@ def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1
     n = A.shape[0]
     c = abs(sigma) if c is None else c
     extra = k if extra is None else extra
-    luM = NDLU((A - sigma * B).tocsc(), perm)
-    luP = NDLU((A + c * B).tocsc(), perm)
-    luB = NDLU(B.tocsc(), perm)
+    luM = NDLU((A - sigma * B).tocsc(), perm, pivot)
+    luP = NDLU((A + c * B).tocsc(), perm, pivot)
+    luB = NDLU(B.tocsc(), perm, pivot)
     Ac, Bc = A.tocsr(), B.tocsr()
     count = [0]
 
