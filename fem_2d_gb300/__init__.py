@@ -42,7 +42,8 @@ class _fem2d_solve_opts(ctypes.Structure):
     _fields_ = [("precond", ctypes.c_int), ("max_outer", ctypes.c_int), ("max_inner", ctypes.c_int),
                 ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("block", ctypes.c_int),
                 ("verbose", ctypes.c_int), ("krylov_steps", ctypes.c_int),
-                ("damping", ctypes.c_double), ("scaling", ctypes.c_int), ("dense", ctypes.c_int)]
+                ("damping", ctypes.c_double), ("scaling", ctypes.c_int), ("dense", ctypes.c_int),
+                ("net", ctypes.c_void_p)]
 
 
 class _fem2d_solve_stats(ctypes.Structure):
@@ -51,7 +52,8 @@ class _fem2d_solve_stats(ctypes.Structure):
                 ("max_rel_residual", ctypes.c_double), ("spmv_count", ctypes.c_int64),
                 ("refine_spd", ctypes.c_int), ("refine_indefinite", ctypes.c_int), ("dense_plan", ctypes.c_int),
                 ("floor_reached", ctypes.c_int), ("block_scaled", ctypes.c_int), ("delayed_pivots", ctypes.c_int),
-                ("max_backward_error", ctypes.c_double)]
+                ("max_backward_error", ctypes.c_double), ("inner_cg_iters", ctypes.c_int64),
+                ("inner_minres_iters", ctypes.c_int64), ("inner_max_relres", ctypes.c_double)]
 
 
 def lib():
@@ -777,7 +779,8 @@ def nalgebra_solve_gep(gep, target_eigenvalue):
     return EigenPair(val.value, vec)
 
 
-PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
+PRECOND_EXACT, PRECOND_PLAIN, PRECOND_LEARNED = 0, 1, 2
+PRECOND_BLOCK_JACOBI = PRECOND_PLAIN
 GRAM_TENSOR, GRAM_FP64 = 0, 1
 
 
@@ -788,19 +791,21 @@ def block_gram_device(ctx, method, n, d_x, ldx, a, d_y, ldy, b, d_c):
                                          ctypes.c_void_p(d_y), int(ldy), int(b), ctypes.c_void_p(d_c)))
 
 
-def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=PRECOND_BLOCK_JACOBI, tol=0.0, max_outer=0,
+def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=0, tol=0.0, max_outer=0,
                     max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0, damping=0.0, scaling=0,
-                    dense=0):
+                    dense=0, net=None):
     """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
     the context the GEP was built on). dense=1 keeps the Gram products on the FP64 CUDA cores instead of
-    the tensor-core FP64 emulation."""
+    the tensor-core FP64 emulation. precond: PRECOND_EXACT (multifrontal LU, default), PRECOND_PLAIN
+    (inner CG / MINRES with the additive-Schwarz preconditioner) or PRECOND_LEARNED (the same with the
+    two-level preconditioner of the trained PatchNet `net`)."""
     ctx = ctx or gep.ctx
     n = gep.dimension
     vals = np.zeros(n_pairs)
     vecs = np.zeros((n_pairs, n))
     res = np.zeros(n_pairs)
     o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose, krylov_steps, damping,
-                          scaling, dense)
+                          scaling, dense, net._h if net is not None else None)
     st = _fem2d_solve_stats()
     _check(lib().fem2d_gpu_solve_gep(ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
                                      _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),

@@ -833,7 +833,8 @@ int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_p
   fem2d_solve_stats st{};
   try {
     std::lock_guard<std::mutex> lk(g->plan.mu);
-    sparse_solve(c->c, g->dom, g->h, g->d, g->plan, target, n_pairs, o, values, vectors, residuals, &st);
+    sparse_solve(c->c, g->dom, g->h, g->d, g->plan, target, n_pairs, o, values, vectors, residuals, &st,
+                 o.net ? &o.net->net : nullptr);
   } catch (...) {
     if (stats) *stats = st;
     throw;

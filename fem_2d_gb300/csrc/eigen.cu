@@ -32,6 +32,7 @@
 #include "blockscale.h"
 #include "eigen.h"
 #include "ozaki.h"
+#include "precond.h"
 #include "mf.h"
 #include "mfdev.h"
 #include "symeig.h"
@@ -599,7 +600,7 @@ MFDevice& mf_plan_dense(MFPlan& p, Ctx& c, const HostGEP& h) {
 // ================================================================ sparse shift-invert eigensolver
 void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double sigma, int k,
                   const fem2d_solve_opts& o, double* values, double* vectors, double* residuals,
-                  fem2d_solve_stats* st) {
+                  fem2d_solve_stats* st, const PatchNet* net) {
   auto t0 = std::chrono::steady_clock::now();
   setup_gemm_smem(c.device);
   enable_stream_pool(c.device);
@@ -658,7 +659,12 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       c.launches++;
     }
   }
-  MFDevice* M = &mf_plan(plan, c, dom, h);
+  // precond 1 / 2: T's two shifted solves by preconditioned CG (A + c B) and MINRES (A - sigma B) with
+  // the plain additive-Schwarz preconditioner or the learned two-level one, instead of multifrontal LU
+  const bool iterative = o.precond == 1 || o.precond == 2;
+  if (o.precond == 2 && !net) fail(FEM2D_E_INVALID_ARG, "precond 2 (learned) needs a trained network");
+  if (o.precond < 0 || o.precond > 2) fail(FEM2D_E_INVALID_ARG, "precond must be 0, 1 or 2");
+  MFDevice* M = iterative ? nullptr : &mf_plan(plan, c, dom, h);
   MFFactor fm, fp;
   // A + c B (c > 0) is SPD: factored without pivoting. c = |sigma| by default from kLargeN DoFs: the null
   // space of the curl-curl operator, smeared by rounding to |lambda| <~ eps ||A|| / lambda_min(B) (which
@@ -666,7 +672,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // physical modes below sigma keep |mu| = lambda / ((lambda + c)(sigma - lambda)) above the far end of
   // a 20-pair window. Smaller GEPs keep c = 0.05 |sigma| (their smear is negligible and the modes below
   // sigma converge faster).
-  const double cshift = (o.damping > 0 ? o.damping : (large ? 1.0 : 0.05)) * std::fabs(sigma);
+  // (the iterative inner solves keep c = |sigma|: A + c B is then far from singular on the null space,
+  // and the same additive-Schwarz preconditioner of A + |sigma| B serves the MINRES solves of A - sigma B)
+  const double cshift = (o.damping > 0 ? o.damping : ((large || iterative) ? 1.0 : 0.05)) * std::fabs(sigma);
   int delayed = 0;
   auto factor_both = [&]() {
     M->factor(c, sa.p, sb.p, 1.0, -sigma, false, fm);
@@ -684,9 +692,16 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     M->factor(c, sa.p, sb.p, 1.0, cshift, true, fp);
     if (fp.flags & 2) fail(FEM2D_E_B_NOT_SPD, "A + c B is not positive definite; B is likely ill-conditioned");
   };
-  factor_both();
+  std::unique_ptr<PCGSolver> pcg;
+  if (iterative) pcg.reset(new PCGSolver(c, dom, h, d, 1.0, cshift, o.precond == 2 ? net : nullptr, nullptr, 0, sa.p,
+                                         sb.p));
+  else factor_both();
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   auto t1 = std::chrono::steady_clock::now();
+  const double inner_tol = o.inner_tol > 0 ? o.inner_tol : 1e-10;
+  const int max_inner = o.max_inner > 0 ? o.max_inner : 5000;
+  int64_t cg_iters = 0, minres_iters = 0;
+  double inner_worst = 0.0;
 
   Dev D{c, h, d, sa.p, sb.p};
   D.dense_mode = o.dense;
@@ -771,9 +786,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     return 3;
   };
   double rel_p = 0, rel_m = 0;
-  int nref_p = calibrate(fp, 1.0, cshift, rel_p);
-  int nref_m = calibrate(fm, 1.0, -sigma, rel_m);
-  if ((rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense && o.scaling == 0) {
+  int nref_p = iterative ? 0 : calibrate(fp, 1.0, cshift, rel_p);
+  int nref_m = iterative ? 0 : calibrate(fm, 1.0, -sigma, rel_m);
+  if (!iterative && (rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense && o.scaling == 0) {
     // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
     try {
       bsc.build(c, h, d, sa.p, sb.p);
@@ -793,7 +808,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // each front's fully-summed rows can grow badly on indefinite pencils of ill-conditioned bases)
   // switch to one dense front with partial pivoting over all rows; the choice is kept in the plan
   constexpr int64_t kDenseMax = 4096;
-  if ((rel_p > 1e-11 || rel_m > 1e-11) && !plan.dense && n <= kDenseMax) {
+  if (!iterative && (rel_p > 1e-11 || rel_m > 1e-11) && !plan.dense && n <= kDenseMax) {
     M = &mf_plan_dense(plan, c, h);
     factor_both();
     nref_p = calibrate(fp, 1.0, cshift, rel_p);
@@ -802,9 +817,20 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // Out (ld lo) = T In (ld li), nb columns; In and Out may not alias W1..W3
   auto apply_T = [&](const double* In, int64_t li, double* Out, int64_t lo, int nb) {
     D.spmm(0.0, 1.0, In, li, nb, W1.p, 32);
-    solve_ref(fp, 1.0, cshift, W1.p, 32, W2.p, 32, nb, nref_p);
-    D.spmm(1.0, 0.0, W2.p, 32, nb, W3.p, 32);
-    solve_ref(fm, 1.0, -sigma, W3.p, 32, Out, lo, nb, nref_m);
+    if (iterative) {
+      PCGStats s1, s2;
+      pcg->cg_device(W1.p, 32, W2.p, 32, nb, inner_tol, max_inner, &s1);
+      D.spmm(1.0, 0.0, W2.p, 32, nb, W3.p, 32);
+      pcg->minres_device(1.0, -sigma, W3.p, 32, Out, lo, nb, inner_tol, max_inner, &s2);
+      cg_iters += s1.iters;
+      minres_iters += s2.iters;
+      spmv += (int64_t)nb * (s1.iters + s2.iters);
+      inner_worst = std::max(inner_worst, std::max(s1.relres, s2.relres));
+    } else {
+      solve_ref(fp, 1.0, cshift, W1.p, 32, W2.p, 32, nb, nref_p);
+      D.spmm(1.0, 0.0, W2.p, 32, nb, W3.p, 32);
+      solve_ref(fm, 1.0, -sigma, W3.p, 32, Out, lo, nb, nref_m);
+    }
     spmv += 2 * nb;
     napply += nb;
   };
@@ -1181,6 +1207,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     st->refine_spd = nref_p;
     st->refine_indefinite = nref_m;
     st->dense_plan = plan.dense ? 1 : 0;
+    st->inner_cg_iters = cg_iters;
+    st->inner_minres_iters = minres_iters;
+    st->inner_max_relres = inner_worst;
     st->block_scaled = blocked ? 1 : 0;
     st->delayed_pivots = delayed;
     st->floor_reached = attained ? 1 : 0;
@@ -1302,6 +1331,13 @@ namespace fem2d {
 void gep_spmm(Ctx& c, const HostGEP& h, const DeviceGEP& d, double ca, double cb, const double* X, int64_t ldx, int nb,
               double* Y, int64_t ldy) {
   Dev D{c, h, d, d.a.p, d.b.p};
+  D.spmm(ca, cb, X, ldx, nb, Y, ldy);
+  FEM2D_CUDA(cudaGetLastError());
+}
+
+void gep_spmm_values(Ctx& c, const HostGEP& h, const DeviceGEP& d, const double* va, const double* vb, double ca,
+                     double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
+  Dev D{c, h, d, va, vb};
   D.spmm(ca, cb, X, ldx, nb, Y, ldy);
   FEM2D_CUDA(cudaGetLastError());
 }

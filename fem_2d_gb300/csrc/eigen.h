@@ -6,16 +6,20 @@
 namespace fem2d {
 
 struct Domain;
+struct PatchNet;
 void dense_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double target,
                  double* value, double* vector);
 void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double target,
                   int n_pairs,
                   const fem2d_solve_opts& o, double* values, double* vectors, double* residuals,
-                  fem2d_solve_stats* st);
+                  fem2d_solve_stats* st, const PatchNet* net = nullptr);
 
 // Y = ca A X + cb B X (device pointers, row-major n x nb, nb <= 32), queued on the context's stream
 void gep_spmm(Ctx& c, const HostGEP& h, const DeviceGEP& d, double ca, double cb, const double* X, int64_t ldx, int nb,
               double* Y, int64_t ldy);
+// the same on a pencil given by its own value arrays (full CSR order, the GEP's pattern)
+void gep_spmm_values(Ctx& c, const HostGEP& h, const DeviceGEP& d, const double* va, const double* vb, double ca,
+                     double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy);
 void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, MFPlan& plan, double ca,
                    double cb, bool spd,
                    int nrhs, const double* rhs, double* x);

@@ -455,6 +455,42 @@ __global__ void cg_direction_kernel(int64_t n, int nb, const double* __restrict_
   }
 }
 
+// Y (ldy) = X (ldx), n x nb
+__global__ void strided_copy_kernel(int64_t n, int nb, const double* __restrict__ X, int64_t ldx, double* __restrict__ Y,
+                                    int64_t ldy) {
+  const int64_t total = n * nb;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / nb;
+    const int j = (int)(t % nb);
+    Y[r * ldy + j] = X[r * ldx + j];
+  }
+}
+
+// Y = s0_c X0 + s1_c X1 + s2_c X2 per column c (blocks n x kNB; a null X term is skipped; Y may alias X0)
+__global__ void lincomb3_kernel(int64_t n, int nb, const double* __restrict__ s, const double* X0, const double* X1,
+                                const double* X2, double* Y) {
+  const int64_t total = n * kNB;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t % kNB);
+    if (c >= nb) continue;
+    double v = s[c] * X0[t];
+    if (X1) v += s[kNB + c] * X1[t];
+    if (X2) v += s[2 * kNB + c] * X2[t];
+    Y[t] = v;
+  }
+}
+
+// X += a_c P per column
+__global__ void axpy_cols_kernel(int64_t n, int nb, const double* __restrict__ a, const double* __restrict__ P,
+                                 double* __restrict__ X) {
+  const int64_t total = n * kNB;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t % kNB);
+    if (c >= nb) continue;
+    X[t] += a[c] * P[t];
+  }
+}
+
 uint64_t splitmix(uint64_t& s) {
   s += 0x9E3779B97F4A7C15ull;
   uint64_t z = s;
@@ -709,8 +745,12 @@ struct PCGSolver::Impl {
   const HostGEP& h;
   const DeviceGEP& d;
   double ca, cb;
+  const double* va = nullptr;   // the pencil's A and B values (full CSR order)
+  const double* vb = nullptr;
   int64_t n;
   Patches pt;
+  // MINRES blocks (n x kNB), allocated on first use
+  DBuf<double> Mv[3], Mw[3], Mz, Mz2, Maz;
   DBuf<int64_t> pptr, ioff;
   DBuf<int32_t> rdof;
   DBuf<double> inv;
@@ -725,6 +765,17 @@ struct PCGSolver::Impl {
   double setup_ms = 0;
 
   Impl(Ctx& ctx, const HostGEP& hg, const DeviceGEP& dg, double a, double b) : c(ctx), h(hg), d(dg), ca(a), cb(b) {}
+
+  void spmm(double ka, double kb, const double* X, double* Y, int nb) {
+    gep_spmm_values(c, h, d, va, vb, ka, kb, X, kNB, nb, Y, kNB);
+  }
+  void upload_scalars(const std::vector<double>& v) {
+    FEM2D_CUDA(cudaMemcpyAsync(scal.p, v.data(), std::min<size_t>(v.size(), 3 * kNB) * sizeof(double),
+                               cudaMemcpyHostToDevice, c.stream));
+  }
+  // preconditioned CG on Rb (overwritten by the residual) into Xb (zeroed first); returns iterations
+  int cg_block(int nb, double tol, int max_iter, double& rel, std::vector<double>* snaps, const double* xstar,
+               int nrhs, int c0, int every, int max_snaps, int first);
 
   void precondition(const double* R, double* Zo, int nb) {
     FEM2D_CUDA(cudaMemsetAsync(Zo, 0, (size_t)n * kNB * sizeof(double), c.stream));
@@ -756,11 +807,13 @@ struct PCGSolver::Impl {
 };
 
 PCGSolver::PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double ca, double cb,
-                     const PatchNet* net, const float* basis, int basis_k)
+                     const PatchNet* net, const float* basis, int basis_k, const double* va, const double* vb)
     : p_(new Impl(c, h, d, ca, cb)) {
   auto t0 = std::chrono::steady_clock::now();
   Impl& I = *p_;
   I.n = h.n;
+  I.va = va ? va : d.a.p;
+  I.vb = vb ? vb : d.b.p;
   if (!(ca > 0.0) || !(cb > 0.0)) fail(FEM2D_E_INVALID_ARG, "PCG needs an SPD shift: c_a > 0 and c_b > 0");
   build_patches(dom, cb / ca, I.pt);
   const int P = I.pt.npatch();
@@ -800,7 +853,7 @@ PCGSolver::PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGE
   int maxnp = 0;
   for (int p = 0; p < P; p++) maxnp = std::max<int>(maxnp, (int)(I.pt.ptr[p + 1] - I.pt.ptr[p]));
   bj_invert_kernel<<<P, 256, (size_t)maxnp * maxnp * sizeof(double), c.stream>>>(
-      I.pptr.p, I.rdof.p, sd.p, sl.p, I.ioff.p, d.row_ptr.p, d.col.p, d.a.p, d.b.p, ca, cb, I.inv.p, flag.p);
+      I.pptr.p, I.rdof.p, sd.p, sl.p, I.ioff.p, d.row_ptr.p, d.col.p, I.va, I.vb, ca, cb, I.inv.p, flag.p);
   c.launches++;
   FEM2D_CUDA(cudaGetLastError());
   int hf = 0;
@@ -809,7 +862,7 @@ PCGSolver::PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGE
   if (hf) fail(FEM2D_E_B_NOT_SPD, "an Elem block of the shifted matrix is not positive definite");
   for (DBuf<double>* b : {&I.Rb, &I.Zb, &I.Pb, &I.Qb, &I.Xb}) b->alloc((size_t)I.n * kNB);
   I.part.alloc((size_t)c.num_sms * 2 * kNB + kNB);
-  I.scal.alloc(kNB);
+  I.scal.alloc(3 * kNB);
 
   std::vector<float> Zh;
   if (net) {
@@ -873,7 +926,7 @@ PCGSolver::PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGE
       const int p0 = j0 / I.k, p1 = std::min(P, (j0 + w + I.k - 1) / I.k);
       coarse_columns_kernel<<<p1 - p0, 128, 0, c.stream>>>(I.pptr.p, I.rdof.p, I.Zw.p, I.k, j0, p0, p1, Zc.p);
       c.launches++;
-      gep_spmm(c, h, d, ca, cb, Zc.p, kNB, w, Yc.p, kNB);
+      I.spmm(ca, cb, Zc.p, Yc.p, w);
       coarse_gram_kernel<<<P, 128, 0, c.stream>>>(I.pptr.p, I.rdof.p, I.Zw.p, I.k, Yc.p, w, j0, I.m, Kc.p);
       c.launches++;
     }
@@ -914,6 +967,65 @@ PCGSolver::~PCGSolver() = default;
 int PCGSolver::coarse_dim() const { return p_->m; }
 double PCGSolver::setup_ms() const { return p_->setup_ms; }
 
+int PCGSolver::Impl::cg_block(int nb, double tol, int max_iter, double& rel, std::vector<double>* snaps,
+                               const double* xstar, int nrhs, int c0, int every, int max_snaps, int first) {
+  FEM2D_CUDA(cudaMemsetAsync(Xb.p, 0, (size_t)n * kNB * sizeof(double), c.stream));
+  const std::vector<double> bb = dots(Rb.p, Rb.p, nb);
+  precondition(Rb.p, Zb.p, nb);
+  FEM2D_CUDA(cudaMemcpyAsync(Pb.p, Zb.p, (size_t)n * kNB * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  std::vector<double> rz = dots(Rb.p, Zb.p, nb), alpha(kNB, 0.0), beta(kNB, 0.0);
+  std::vector<char> done(nb, 0);
+  std::vector<double> hx;
+  int it = 0;
+  rel = 0.0;
+  for (int j = 0; j < nb; j++)
+    if (!(bb[j] > 0.0)) done[j] = 1;   // a zero right-hand side: x = 0
+  for (; it < max_iter; it++) {
+    bool any = false;
+    for (int j = 0; j < nb; j++) any = any || !done[j];
+    if (!any) break;
+    spmm(ca, cb, Pb.p, Qb.p, nb);
+    const std::vector<double> pq = dots(Pb.p, Qb.p, nb);
+    for (int j = 0; j < nb; j++) alpha[j] = (done[j] || pq[j] <= 0.0) ? 0.0 : rz[j] / pq[j];
+    upload_scalars(alpha);
+    cg_update_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, scal.p, Pb.p, Qb.p, Xb.p, Rb.p);
+    c.launches++;
+    if (snaps && xstar && every > 0 && it + 1 >= first && (it + 1) % every == 0 &&
+        (int64_t)snaps->size() < (int64_t)max_snaps * n) {
+      hx.resize((size_t)n * kNB);
+      FEM2D_CUDA(cudaMemcpyAsync(hx.data(), Xb.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+      for (int j = 0; j < nb && (int64_t)snaps->size() < (int64_t)max_snaps * n; j++) {
+        if (done[j]) continue;
+        for (int64_t i = 0; i < n; i++) snaps->push_back(xstar[(size_t)i * nrhs + c0 + j] - hx[(size_t)i * kNB + j]);
+      }
+    }
+    const std::vector<double> rr = dots(Rb.p, Rb.p, nb);
+    rel = 0.0;
+    bool all = true;
+    for (int j = 0; j < nb; j++) {
+      const double rj = bb[j] > 0.0 ? std::sqrt(rr[j] / bb[j]) : 0.0;
+      if (rj <= tol) done[j] = 1;
+      all = all && done[j];
+      rel = std::max(rel, rj);
+    }
+    if (all) {
+      it++;
+      break;
+    }
+    precondition(Rb.p, Zb.p, nb);
+    const std::vector<double> rz2 = dots(Rb.p, Zb.p, nb);
+    for (int j = 0; j < nb; j++) {
+      beta[j] = (done[j] || rz[j] == 0.0) ? 0.0 : rz2[j] / rz[j];
+      rz[j] = rz2[j];
+    }
+    upload_scalars(beta);
+    cg_direction_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, scal.p, Zb.p, Pb.p);
+    c.launches++;
+  }
+  return it;
+}
+
 void PCGSolver::solve(int nrhs, const double* rhs, double* x, double tol, int max_iter, PCGStats* st,
                       std::vector<double>* snaps, const double* xstar, int every, int max_snaps, int first) {
   Impl& I = *p_;
@@ -929,53 +1041,8 @@ void PCGSolver::solve(int nrhs, const double* rhs, double* x, double tol, int ma
     for (int64_t i = 0; i < n; i++)
       for (int j = 0; j < nb; j++) hb[(size_t)i * kNB + j] = rhs[(size_t)i * nrhs + c0 + j];
     FEM2D_CUDA(cudaMemcpyAsync(I.Rb.p, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    FEM2D_CUDA(cudaMemsetAsync(I.Xb.p, 0, (size_t)n * kNB * sizeof(double), c.stream));
-    const std::vector<double> bb = I.dots(I.Rb.p, I.Rb.p, nb);
-    I.precondition(I.Rb.p, I.Zb.p, nb);
-    FEM2D_CUDA(cudaMemcpyAsync(I.Pb.p, I.Zb.p, (size_t)n * kNB * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
-    std::vector<double> rz = I.dots(I.Rb.p, I.Zb.p, nb), alpha(kNB, 0.0), beta(kNB, 0.0);
-    std::vector<char> done(nb, 0);
-    int it = 0;
     double rel = 0.0;
-    for (; it < max_iter; it++) {
-      gep_spmm(c, I.h, I.d, I.ca, I.cb, I.Pb.p, kNB, nb, I.Qb.p, kNB);
-      const std::vector<double> pq = I.dots(I.Pb.p, I.Qb.p, nb);
-      for (int j = 0; j < nb; j++) alpha[j] = (done[j] || pq[j] <= 0.0) ? 0.0 : rz[j] / pq[j];
-      FEM2D_CUDA(cudaMemcpyAsync(I.scal.p, alpha.data(), kNB * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-      cg_update_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, I.Pb.p, I.Qb.p, I.Xb.p, I.Rb.p);
-      c.launches++;
-      if (snaps && xstar && every > 0 && it + 1 >= first && (it + 1) % every == 0 &&
-          (int64_t)snaps->size() < (int64_t)max_snaps * n) {
-        FEM2D_CUDA(cudaMemcpyAsync(hx.data(), I.Xb.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-        FEM2D_CUDA(cudaStreamSynchronize(c.stream));
-        for (int j = 0; j < nb && (int64_t)snaps->size() < (int64_t)max_snaps * n; j++) {
-          if (done[j]) continue;
-          for (int64_t i = 0; i < n; i++) snaps->push_back(xstar[(size_t)i * nrhs + c0 + j] - hx[(size_t)i * kNB + j]);
-        }
-      }
-      const std::vector<double> rr = I.dots(I.Rb.p, I.Rb.p, nb);
-      rel = 0.0;
-      bool all = true;
-      for (int j = 0; j < nb; j++) {
-        const double rj = std::sqrt(rr[j] / std::max(bb[j], 1e-300));
-        if (rj <= tol) done[j] = 1;
-        all = all && done[j];
-        rel = std::max(rel, rj);
-      }
-      if (all) {
-        it++;
-        break;
-      }
-      I.precondition(I.Rb.p, I.Zb.p, nb);
-      const std::vector<double> rz2 = I.dots(I.Rb.p, I.Zb.p, nb);
-      for (int j = 0; j < nb; j++) {
-        beta[j] = (done[j] || rz[j] == 0.0) ? 0.0 : rz2[j] / rz[j];
-        rz[j] = rz2[j];
-      }
-      FEM2D_CUDA(cudaMemcpyAsync(I.scal.p, beta.data(), kNB * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-      cg_direction_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, I.Zb.p, I.Pb.p);
-      c.launches++;
-    }
+    const int it = I.cg_block(nb, tol, max_iter, rel, snaps, xstar, nrhs, c0, every, max_snaps, first);
     total_iters = std::max(total_iters, it);
     worst = std::max(worst, rel);
     FEM2D_CUDA(cudaMemcpyAsync(hx.data(), I.Xb.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -986,6 +1053,144 @@ void PCGSolver::solve(int nrhs, const double* rhs, double* x, double tol, int ma
   if (st) {
     st->iters = total_iters;
     st->relres = worst;
+    st->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    st->setup_ms = I.setup_ms;
+    st->coarse_dim = I.m;
+  }
+}
+
+void PCGSolver::cg_device(const double* R, int64_t ldr, double* X, int64_t ldx, int nb, double tol, int max_iter,
+                          PCGStats* st) {
+  Impl& I = *p_;
+  Ctx& c = I.c;
+  if (nb < 1 || nb > kNB) fail(FEM2D_E_INVALID_ARG, "cg_device: 1..32 right-hand sides");
+  auto t0 = std::chrono::steady_clock::now();
+  FEM2D_CUDA(cudaMemsetAsync(I.Rb.p, 0, (size_t)I.n * kNB * sizeof(double), c.stream));
+  strided_copy_kernel<<<grid_for(c, I.n * nb), 256, 0, c.stream>>>(I.n, nb, R, ldr, I.Rb.p, kNB);
+  c.launches++;
+  double rel = 0.0;
+  const int it = I.cg_block(nb, tol, max_iter, rel, nullptr, nullptr, 0, 0, 0, 0, 0);
+  strided_copy_kernel<<<grid_for(c, I.n * nb), 256, 0, c.stream>>>(I.n, nb, I.Xb.p, kNB, X, ldx);
+  c.launches++;
+  if (st) {
+    st->iters = it;
+    st->relres = rel;
+    st->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    st->setup_ms = I.setup_ms;
+    st->coarse_dim = I.m;
+  }
+}
+
+// Preconditioned MINRES (the recurrence of Elman, Silvester and Wathen, "Finite Elements and Fast
+// Iterative Solvers", Algorithm 6.1) per column, with this solver's SPD preconditioner; the stopping
+// test is on the preconditioned residual norm |eta| <= tol gamma_1.
+void PCGSolver::minres_device(double ka, double kb, const double* R, int64_t ldr, double* X, int64_t ldx, int nb,
+                              double tol, int max_iter, PCGStats* st) {
+  Impl& I = *p_;
+  Ctx& c = I.c;
+  const int64_t n = I.n;
+  if (nb < 1 || nb > kNB) fail(FEM2D_E_INVALID_ARG, "minres_device: 1..32 right-hand sides");
+  auto t0 = std::chrono::steady_clock::now();
+  for (DBuf<double>* b : {&I.Mv[0], &I.Mv[1], &I.Mv[2], &I.Mw[0], &I.Mw[1], &I.Mw[2], &I.Mz, &I.Mz2, &I.Maz})
+    if (b->n != (size_t)n * kNB) b->alloc((size_t)n * kNB);
+  const size_t bytes = (size_t)n * kNB * sizeof(double);
+  double *v0 = I.Mv[0].p, *v1 = I.Mv[1].p, *v2 = I.Mv[2].p;
+  double *w0 = I.Mw[0].p, *w1 = I.Mw[1].p, *w2 = I.Mw[2].p;
+  double *z = I.Mz.p, *z2 = I.Mz2.p, *az = I.Maz.p;
+  for (double* p : {v0, v1, w0, w1, I.Xb.p}) FEM2D_CUDA(cudaMemsetAsync(p, 0, bytes, c.stream));
+  strided_copy_kernel<<<grid_for(c, n * nb), 256, 0, c.stream>>>(n, nb, R, ldr, v1, kNB);   // x0 = 0: v1 = b
+  c.launches++;
+  I.precondition(v1, z, nb);
+  std::vector<double> g(nb), gprev(nb, 1.0), eta(nb), eta0(nb), cc0(nb, 1.0), cc1(nb, 1.0), ss0(nb, 0.0),
+      ss1(nb, 0.0);
+  std::vector<char> done(nb, 0);
+  {
+    const std::vector<double> zv = I.dots(z, v1, nb);
+    for (int j = 0; j < nb; j++) {
+      g[j] = zv[j] > 0.0 ? std::sqrt(zv[j]) : 0.0;
+      eta[j] = eta0[j] = g[j];
+      if (!(g[j] > 0.0)) done[j] = 1;
+    }
+  }
+  std::vector<double> sc(3 * kNB, 0.0);
+  int it = 0;
+  double rel = 0.0;
+  for (; it < max_iter; it++) {
+    bool any = false;
+    for (int j = 0; j < nb; j++) any = any || !done[j];
+    if (!any) break;
+    // z_j = z_j / gamma_j
+    std::fill(sc.begin(), sc.end(), 0.0);
+    for (int j = 0; j < nb; j++) sc[j] = g[j] > 0.0 ? 1.0 / g[j] : 0.0;
+    I.upload_scalars(sc);
+    lincomb3_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, z, nullptr, nullptr, z);
+    c.launches++;
+    I.spmm(ka, kb, z, az, nb);
+    const std::vector<double> delta = I.dots(az, z, nb);
+    // v2 = az - (delta / gamma) v1 - (gamma / gamma_prev) v0
+    for (int j = 0; j < nb; j++) {
+      sc[j] = 1.0;
+      sc[kNB + j] = g[j] > 0.0 ? -delta[j] / g[j] : 0.0;
+      sc[2 * kNB + j] = gprev[j] > 0.0 ? -g[j] / gprev[j] : 0.0;
+    }
+    I.upload_scalars(sc);
+    lincomb3_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, az, v1, v0, v2);
+    c.launches++;
+    I.precondition(v2, z2, nb);
+    const std::vector<double> zv = I.dots(z2, v2, nb);
+    std::vector<double> a1(nb), a2(nb), a3(nb), cnew(nb), snew(nb), gnew(nb);
+    for (int j = 0; j < nb; j++) {
+      gnew[j] = zv[j] > 0.0 ? std::sqrt(zv[j]) : 0.0;
+      const double al0 = cc1[j] * delta[j] - cc0[j] * ss1[j] * g[j];
+      const double al1 = std::sqrt(al0 * al0 + gnew[j] * gnew[j]);
+      a2[j] = ss1[j] * delta[j] + cc0[j] * cc1[j] * g[j];
+      a3[j] = ss0[j] * g[j];
+      a1[j] = al1;
+      cnew[j] = al1 > 0.0 ? al0 / al1 : 1.0;
+      snew[j] = al1 > 0.0 ? gnew[j] / al1 : 0.0;
+    }
+    // w2 = (z - a3 w0 - a2 w1) / a1
+    for (int j = 0; j < nb; j++) {
+      const double inv = (a1[j] > 0.0 && !done[j]) ? 1.0 / a1[j] : 0.0;
+      sc[j] = inv;
+      sc[kNB + j] = -a3[j] * inv;
+      sc[2 * kNB + j] = -a2[j] * inv;
+    }
+    I.upload_scalars(sc);
+    lincomb3_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, z, w0, w1, w2);
+    c.launches++;
+    // x += c_new eta w2
+    std::vector<double> step(kNB, 0.0);
+    for (int j = 0; j < nb; j++) step[j] = done[j] ? 0.0 : cnew[j] * eta[j];
+    I.upload_scalars(step);
+    axpy_cols_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, w2, I.Xb.p);
+    c.launches++;
+    rel = 0.0;
+    for (int j = 0; j < nb; j++) {
+      if (done[j]) continue;
+      eta[j] = -snew[j] * eta[j];
+      const double r = std::fabs(eta[j]) / eta0[j];
+      if (r <= tol || !(gnew[j] > 0.0)) done[j] = 1;
+      rel = std::max(rel, r);
+      ss0[j] = ss1[j];
+      ss1[j] = snew[j];
+      cc0[j] = cc1[j];
+      cc1[j] = cnew[j];
+      gprev[j] = g[j];
+      g[j] = gnew[j];
+    }
+    // rotate: v0 <- v1 <- v2, w0 <- w1 <- w2, z <- z2
+    std::swap(v0, v1);
+    std::swap(v1, v2);
+    std::swap(w0, w1);
+    std::swap(w1, w2);
+    std::swap(z, z2);
+  }
+  strided_copy_kernel<<<grid_for(c, n * nb), 256, 0, c.stream>>>(n, nb, I.Xb.p, kNB, X, ldx);
+  c.launches++;
+  if (st) {
+    st->iters = it;
+    st->relres = rel;
     st->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     st->setup_ms = I.setup_ms;
     st->coarse_dim = I.m;

@@ -60,10 +60,22 @@ struct PCGStats {
 
 class PCGSolver {
  public:
-  // net: learned coarse basis; else basis (nrows x basis_k floats, rows in patch order) when given; else plain
+  // net: learned coarse basis; else basis (nrows x basis_k floats, rows in patch order) when given; else plain.
+  // va, vb: the pencil's values (full CSR order, the GEP's pattern) when not the GEP's own A and B (the
+  // eigensolver passes its scaled pencil)
   PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& d, double ca, double cb,
-            const PatchNet* net, const float* basis = nullptr, int basis_k = 0);
+            const PatchNet* net, const float* basis = nullptr, int basis_k = 0, const double* va = nullptr,
+            const double* vb = nullptr);
   ~PCGSolver();
+  // device-resident solves of nb <= 32 right-hand sides (row-major n x nb blocks, leading dimensions
+  // ldr and ldx), zero start, per column to ||r|| <= tol ||b|| (CG) or ||r||_P <= tol ||b||_P (MINRES):
+  //  cg_device:     K = ca A + cb B (the solver's SPD shift) by preconditioned CG
+  //  minres_device: ka A + kb B (symmetric, possibly indefinite) by MINRES with this solver's SPD
+  //                 preconditioner
+  void cg_device(const double* R, int64_t ldr, double* X, int64_t ldx, int nb, double tol, int max_iter,
+                 PCGStats* st);
+  void minres_device(double ka, double kb, const double* R, int64_t ldr, double* X, int64_t ldx, int nb, double tol,
+                     int max_iter, PCGStats* st);
   // x = K^-1 rhs (n x nrhs row-major, host) by preconditioned CG, per column to ||r|| <= tol ||b||
   void solve(int nrhs, const double* rhs, double* x, double tol, int max_iter, PCGStats* st,
              std::vector<double>* snaps = nullptr, const double* xstar = nullptr, int every = 0, int max_snaps = 0,

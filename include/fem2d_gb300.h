@@ -241,13 +241,18 @@ int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c
  * wait inside the tensor kernel expired. */
 int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
                             const double* d_y, int64_t ldy, int b, double* d_c);
+typedef struct fem2d_patchnet fem2d_patchnet;
 typedef struct fem2d_solve_opts {
-  int precond;          /* reserved: the eigensolve's shifted systems are solved exactly (multifrontal LU);
-                           the iterative inner solver with its preconditioners is fem2d_pcg_* */
+  int precond;          /* how T = (A - s B)^-1 A (A + c B)^-1 B solves its two shifted systems (the KSP
+                           solves of the external SLEPc process, slepc_solve.rs:26-36):
+                           0 = exact multifrontal LU (default);
+                           1 = preconditioned CG on A + c B and preconditioned MINRES on A - s B, with
+                               the plain additive-Schwarz (per-Elem block-Jacobi) preconditioner;
+                           2 = the same with the learned two-level preconditioner of `net` */
   int max_outer;        /* outer (restart) cycles, 0 = default 40 */
-  int max_inner;        /* reserved */
+  int max_inner;        /* iterations per inner CG / MINRES solve (precond 1, 2), 0 = default 5000 */
   double tol;           /* relative residual ||Ax - lambda Bx|| / (|lambda| ||Bx||), 0 = default 1e-10 */
-  double inner_tol;     /* reserved */
+  double inner_tol;     /* relative residual of each inner solve (precond 1, 2), 0 = default 1e-10 */
   int block;            /* block size, 0 = default (n_pairs + guard) */
   int verbose;
   int krylov_steps;     /* block Krylov steps per restart cycle (at most 8), 0 = default 4 */
@@ -260,6 +265,7 @@ typedef struct fem2d_solve_opts {
   int dense;            /* Gram products of the B-orthogonalisation and Rayleigh-Ritz steps: 0 = FP64
                            emulated on the tensor cores (tcgen05, exact integer slicing; default),
                            1 = FP64 CUDA cores */
+  const fem2d_patchnet* net;   /* trained patch network (precond 2), else NULL */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {
@@ -276,6 +282,9 @@ typedef struct fem2d_solve_stats {
   int block_scaled;    /* 1: the pencil was scaled by Cholesky factors of B's row-run diagonal blocks */
   int delayed_pivots;  /* DoFs whose elimination moved to a parent front (no stable pivot in their own) */
   double max_backward_error;  /* max over the pairs of ||Ax - lambda Bx|| / ((||A|| + |lambda| ||B||) ||x||) */
+  int64_t inner_cg_iters;      /* precond 1, 2: CG iterations summed over the inner block solves */
+  int64_t inner_minres_iters;  /* precond 1, 2: MINRES iterations summed over the inner block solves */
+  double inner_max_relres;     /* precond 1, 2: largest final relative residual of an inner solve */
 } fem2d_solve_stats;
 
 /* gpu_solve_gep: the n_pairs eigenpairs of (A, B) nearest target, by a shift-invert block
@@ -337,7 +346,6 @@ int fem2d_fields_xy_device(fem2d_fields* f, const double* d_solution, int64_t n_
  *                operator Z^T K Z inverted densely, at most 16384 coarse vectors).
  * The network (an MLP 16 -> hidden -> hidden -> k, tanh, FP32) is trained on the GPU by its own
  * forward/backward/Adam kernels on error vectors of the plain solver. */
-typedef struct fem2d_patchnet fem2d_patchnet;
 typedef struct fem2d_pcg fem2d_pcg;
 int fem2d_patchnet_create(int k, int hidden, uint64_t seed, fem2d_patchnet** out);
 void fem2d_patchnet_free(fem2d_patchnet* p);
