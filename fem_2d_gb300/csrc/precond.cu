@@ -322,22 +322,6 @@ __global__ void coarse_restrict_kernel(const int64_t* __restrict__ pptr, const i
   }
 }
 
-// w = Kinv y (m x m times m x nb, FP64); one warp per coarse row, lanes split the row
-__global__ void coarse_apply_kernel(int m, const double* __restrict__ Kinv, const double* __restrict__ y, int nb,
-                                    double* __restrict__ w) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < m;
-       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const double* row = Kinv + i * m;
-    for (int c = 0; c < nb; c++) {
-      double s = 0.0;
-      for (int j = lane; j < m; j += 32) s += row[j] * y[(int64_t)j * kNB + c];
-      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-      if (lane == 0) w[i * kNB + c] = s;
-    }
-  }
-}
-
 // Zo[dof_i][c] += w_i sum_a Zn[i][a] w[(p k + a)][c]
 __global__ void coarse_prolong_kernel(const int64_t* __restrict__ pptr, const int32_t* __restrict__ rdof,
                                       const float* __restrict__ Zw, int k, const double* __restrict__ w, int nb,
@@ -453,6 +437,15 @@ __global__ void cg_direction_kernel(int64_t n, int nb, const double* __restrict_
     if (c >= nb) continue;
     P[t] = Zs[t] + beta[c] * P[t];
   }
+}
+
+__global__ void to_f32_kernel(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    y[t] = (float)x[t];
+}
+__global__ void to_f64_kernel(int64_t n, const float* __restrict__ x, double* __restrict__ y) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    y[t] = (double)x[t];
 }
 
 // Y (ldy) = X (ldx), n x nb
@@ -758,8 +751,8 @@ struct PCGSolver::Impl {
   bool learned = false;
   int k = 0, m = 0;
   DBuf<float> Zw;
-  DBuf<double> Kinv;
   DBuf<double> ycoarse, wcoarse;
+  DBuf<float> KinvF, yF, wF;   // the coarse inverse and its operands in FP32 (a preconditioner needs no more)
   // CG blocks (n x kNB)
   DBuf<double> Rb, Zb, Pb, Qb, Xb, part, scal;
   double setup_ms = 0;
@@ -784,9 +777,13 @@ struct PCGSolver::Impl {
     c.launches++;
     if (learned) {
       coarse_restrict_kernel<<<P, 128, 0, c.stream>>>(pptr.p, rdof.p, Zw.p, k, R, kNB, nb, ycoarse.p);
-      coarse_apply_kernel<<<grid_for(c, (int64_t)m * 32), 256, 0, c.stream>>>(m, Kinv.p, ycoarse.p, nb, wcoarse.p);
+      // w = Kinv y as one FP32 tiled GEMM (m x m times m x nb)
+      to_f32_kernel<<<grid_for(c, (int64_t)m * kNB), 256, 0, c.stream>>>((int64_t)m * kNB, ycoarse.p, yF.p);
+      dim3 gg((nb + 63) / 64, (m + 63) / 64);
+      sgemm_kernel<false, false><<<gg, 256, 0, c.stream>>>(m, nb, m, KinvF.p, m, yF.p, kNB, wF.p, kNB, 0.f);
+      to_f64_kernel<<<grid_for(c, (int64_t)m * kNB), 256, 0, c.stream>>>((int64_t)m * kNB, wF.p, wcoarse.p);
       coarse_prolong_kernel<<<P, 128, 0, c.stream>>>(pptr.p, rdof.p, Zw.p, k, wcoarse.p, nb, Zo, kNB);
-      c.launches += 3;
+      c.launches += 5;
     }
   }
 
@@ -885,7 +882,7 @@ PCGSolver::PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGE
   if (!Zh.empty()) {
     I.learned = true;
     I.m = P * I.k;
-    if (I.m > 16384) fail(FEM2D_E_TOO_LARGE, "coarse space above 16384 vectors (dense coarse inverse)");
+    if (I.m > 20480) fail(FEM2D_E_TOO_LARGE, "coarse space above 20480 vectors (dense coarse inverse)");
     // per Elem: weight rows by the partition of unity of shared functions, then orthonormalise the k
     // vectors (modified Gram-Schmidt, FP64); nearly dependent vectors are zeroed, not kept
     for (int p = 0; p < P; p++) {
@@ -953,11 +950,14 @@ PCGSolver::PCGSolver(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGE
       c.launches += 3;
     }
     FEM2D_CUDA(cudaGetLastError());
-    I.Kinv.alloc((size_t)I.m * I.m);
-    FEM2D_CUDA(cudaMemcpyAsync(I.Kinv.p, Kc.p, (size_t)I.m * I.m * sizeof(double), cudaMemcpyDeviceToDevice,
-                               c.stream));
+    I.KinvF.alloc((size_t)I.m * I.m);
+    to_f32_kernel<<<grid_for(c, (int64_t)I.m * I.m), 256, 0, c.stream>>>((int64_t)I.m * I.m, Kc.p, I.KinvF.p);
+    c.launches++;
     I.ycoarse.alloc((size_t)I.m * kNB);
     I.wcoarse.alloc((size_t)I.m * kNB);
+    I.yF.alloc((size_t)I.m * kNB);
+    I.wF.alloc((size_t)I.m * kNB);
+    FEM2D_CUDA(cudaMemsetAsync(I.ycoarse.p, 0, (size_t)I.m * kNB * sizeof(double), c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   }
   I.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

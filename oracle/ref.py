@@ -585,14 +585,15 @@ def _cluster_bounds(th_sel, rb, th_all, rel_tol=1e-6):
 
 
 def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1e-6, tol=1e-13, seed=0,
-                            refine=2, reject=1e-2, pivot=0.1):
+                            refine=2, reject=1e-2, pivot=0.1, schur=None):
     """Second, independent FP64 sparse oracle for large pencils: ARPACK (implicitly restarted Lanczos
     in the B inner product, through scipy ``eigsh``) on T = (A - sigma B)^-1 A (A + c B)^-1 B.
 
     T's eigenvalues mu = lambda / ((lambda - sigma)(lambda + c)) vanish on the curl null space and grow
     without bound as lambda nears sigma, so the largest |mu| are the physical modes near sigma. The
     solves are SuperLU factorizations under ``perm`` (threshold ``pivot`` for row pivoting: a smaller one
-    keeps more diagonal pivots and less fill). The k + extra Lanczos vectors X are then refined
+    keeps more diagonal pivots and less fill), or ``SchurLU`` substructuring when ``schur`` = (box, parts,
+    sep) is given. The k + extra Lanczos vectors X are then refined
     ``refine`` times by one Rayleigh-Ritz step on (A, B) over span[X, T X] in FP64, and the k Ritz
     values nearest sigma with |lambda| > spurious |sigma| and relative residual below ``reject`` are
     returned with:
@@ -610,9 +611,15 @@ def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1
     n = A.shape[0]
     c = abs(sigma) if c is None else c
     extra = k if extra is None else extra
-    luM = NDLU((A - sigma * B).tocsc(), perm, pivot)
-    luP = NDLU((A + c * B).tocsc(), perm, pivot)
-    luB = NDLU(B.tocsc(), perm, pivot)
+    if schur is None:
+        luM = NDLU((A - sigma * B).tocsc(), perm, pivot)
+        luP = NDLU((A + c * B).tocsc(), perm, pivot)
+        luB = NDLU(B.tocsc(), perm, pivot)
+    else:   # (box, parts, sep): two-level substructuring for very large pencils
+        box, parts, sep = schur
+        luM = SchurLU(A - sigma * B, box, parts, sep, pivot)
+        luP = SchurLU(A + c * B, box, parts, sep, pivot)
+        luB = SchurLU(B, box, parts, sep, pivot)
     Ac, Bc = A.tocsr(), B.tocsr()
     count = [0]
 
@@ -665,3 +672,100 @@ def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1
     return {"values": th[idx], "vectors": X[:, idx], "rel_residual": rel[idx], "backward_error": bwd[idx],
             "resid_binv": rb, "err_bound": _cluster_bounds(th[idx], rb, phys), "mu_min": mu_min,
             "applications": count[0]}
+
+
+def nd_parts(box, levels=4):
+    """The top `levels` levels of ``nd_order``'s geometric dissection: returns (parts, sep), the 2^levels
+    subdomains (index arrays) and the union of their separators (index array)."""
+    parts, seps = [], []
+
+    def cut(idx):
+        best = None
+        for ax in (0, 1):
+            lo, hi = box[idx, ax], box[idx, ax + 2]
+            c = np.sort(0.5 * (lo + hi))
+            q0, q1 = c[int(0.3 * (len(c) - 1))], c[int(0.7 * (len(c) - 1))]
+            cand = np.unique(np.concatenate([lo, hi]))
+            cand = cand[(cand >= q0) & (cand <= q1)]
+            if len(cand) == 0:
+                continue
+            slo, shi = np.sort(lo), np.sort(hi)
+            left = np.searchsorted(shi, cand, side="right")
+            right = len(idx) - np.searchsorted(slo, cand, side="left")
+            score = (len(idx) - left - right) * len(idx) + np.abs(left - right)
+            k = int(np.argmin(score))
+            if best is None or score[k] < best[0]:
+                best = (score[k], ax, cand[k])
+        return best
+
+    def rec(idx, level):
+        b = cut(idx) if level < levels else None
+        if b is None:
+            parts.append(idx)
+            return
+        _, ax, s = b
+        lo, hi = box[idx, ax], box[idx, ax + 2]
+        rec(idx[hi <= s], level + 1)
+        rec(idx[lo >= s], level + 1)
+        seps.append(idx[(lo < s) & (hi > s)])
+
+    rec(np.arange(len(box)), 0)
+    return [p for p in parts if len(p)], (np.concatenate(seps) if seps else np.zeros(0, np.int64))
+
+
+class SchurLU:
+    """K x = b by two-level substructuring, for matrices beyond SuperLU's 32-bit size limits (its first
+    fill estimate, about 20 x nnz, overflows near 1e8 nonzeros): each subdomain block K_ii (``nd_parts``)
+    is factored by SuperLU under its own nested-dissection ordering; the separator unknowns are solved
+    through the dense Schur complement S = K_SS - sum_i K_Si K_ii^-1 K_iS (LAPACK LU with partial
+    pivoting). Subdomains of about a quarter of the waveguide's width keep their blocks of A - 10 B far
+    from singular (their own PEC eigenvalues start near 39)."""
+
+    def __init__(self, K, box, parts, sep, pivot=0.1):
+        import scipy.linalg as sl
+        import scipy.sparse.linalg as sla
+
+        K = K.tocsr()
+        self.n = K.shape[0]
+        self.parts, self.sep = parts, sep
+        self.lus, self.KiS, self.KSi = [], [], []
+        KS = K[sep]
+        S = KS[:, sep].toarray()
+        for idx in parts:
+            perm = nd_order(box[idx])
+            inv = np.empty_like(perm)
+            inv[perm] = np.arange(len(perm))
+            Kii = K[idx][:, idx]
+            lu = sla.splu(Kii[perm][:, perm].tocsc(), permc_spec="NATURAL", diag_pivot_thresh=pivot,
+                          options={"SymmetricMode": True})
+            KiS = K[idx][:, sep].tocsc()
+            KSi = KS[:, idx].tocsr()
+            nzc = np.nonzero(np.diff(KiS.indptr))[0]   # the separator columns this subdomain touches
+            if len(nzc):
+                rhs = KiS[:, nzc].toarray()[perm]
+                Y = np.empty_like(rhs)
+                for c0 in range(0, len(nzc), 512):
+                    Y[:, c0:c0 + 512] = lu.solve(np.ascontiguousarray(rhs[:, c0:c0 + 512]))
+                Y = Y[inv]
+                S[:, nzc] -= KSi @ Y
+            self.lus.append((lu, perm, inv))
+            self.KiS.append(KiS.tocsr())
+            self.KSi.append(KSi)
+        self.Slu = sl.lu_factor(S) if len(sep) else None
+
+    def _part_solve(self, i, b):
+        lu, perm, inv = self.lus[i]
+        return lu.solve(np.ascontiguousarray(b[perm]))[inv]
+
+    def solve(self, b):
+        import scipy.linalg as sl
+
+        x = np.zeros_like(b)
+        rS = b[self.sep].copy()
+        for i, idx in enumerate(self.parts):
+            rS -= self.KSi[i] @ self._part_solve(i, b[idx])
+        xS = sl.lu_solve(self.Slu, rS) if self.Slu is not None else rS
+        x[self.sep] = xS
+        for i, idx in enumerate(self.parts):
+            x[idx] = self._part_solve(i, b[idx] - self.KiS[i] @ xS)
+        return x

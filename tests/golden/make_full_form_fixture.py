@@ -8,7 +8,8 @@ For each workload this runs, once, on the host:
   its values entrywise without re-running the assembly;
 * the 20 eigenvalues nearest 10.0 (non-spurious) by the ARPACK oracle ``arpack_nearest_physical``
   (Lanczos on T = (A - s B)^-1 A (A + s B)^-1 B with SuperLU solves under the oracle's own nested
-  dissection ordering), with their residuals and error bounds;
+  dissection ordering; above 500k DoFs, SuperLU on 16 subdomains plus a dense Schur complement), with
+  their residuals and error bounds;
 * with ``--cross-check``, the same 20 by the second oracle method ``sparse_nearest_physical`` (block
   Krylov with CGS2 and Rayleigh-Ritz), and the largest relative difference of the two.
 
@@ -69,11 +70,18 @@ def make(name, cross_check=False, samples=4096, threads=None):
     A = ref.full_sym(n, r, c, a)
     B = ref.full_sym(n, r, c, b)
     del r, c, a, b
-    perm = ref.nd_order(ref.dof_boxes(om))
+    box = ref.dof_boxes(om)
     t0 = time.time()
-    # at 1M DoFs SuperLU runs out of its index range with the default pivot threshold (0.1); 0.01 keeps
-    # the fill below it (the solves stay backward stable: checked against 0.1 at 106k DoFs)
-    res = ref.arpack_nearest_physical(A, B, w.target, w.n_pairs, perm, refine=0, pivot=0.01 if n > 500000 else 0.1)
+    if n > 500000:
+        # SuperLU's first fill estimate (about 20 x nnz) overflows its 32-bit sizes at this nnz: two-level
+        # substructuring over 16 subdomains (SuperLU each) and a dense Schur complement instead (checked
+        # against the direct SuperLU fixture at 160k DoFs: eigenvalues within 6.2e-12)
+        parts, sep = ref.nd_parts(box, 4)
+        res = ref.arpack_nearest_physical(A, B, w.target, w.n_pairs, None, refine=0, schur=(box, parts, sep))
+        solver = "SchurLU: 16 SuperLU subdomains + dense Schur complement of %d separator DoFs" % len(sep)
+    else:
+        res = ref.arpack_nearest_physical(A, B, w.target, w.n_pairs, ref.nd_order(box), refine=0)
+        solver = "SuperLU under the oracle's nested-dissection ordering"
     t_eig = time.time() - t0
     o = np.argsort(res["values"])
     out["eigenvalues"] = res["values"][o].tolist()
@@ -84,11 +92,12 @@ def make(name, cross_check=False, samples=4096, threads=None):
     out["mu_min"] = res["mu_min"]
     out["arpack_applications"] = res["applications"]
     out["t_oracle_eigensolve_s"] = t_eig
-    out["superlu_pivot_threshold"] = 0.01 if n > 500000 else 0.1
+    out["sparse_solver"] = solver
     print("ARPACK: %.1f s, %d applications of T" % (t_eig, res["applications"]), flush=True)
     if cross_check:
         t0 = time.time()
-        ws, _, rel = ref.sparse_nearest_physical(A, B, w.target, w.n_pairs, perm=perm, tol=1e-12, max_cycles=25)
+        ws, _, rel = ref.sparse_nearest_physical(A, B, w.target, w.n_pairs, perm=ref.nd_order(box), tol=1e-12,
+                                                 max_cycles=25)
         ws = np.sort(ws)
         out["cross_check"] = {"method": "block Krylov (sparse_nearest_physical)", "eigenvalues": ws.tolist(),
                               "max_rel_diff": float(np.max(np.abs(ws - res["values"][o]) / np.abs(ws))),
