@@ -459,7 +459,8 @@ def run_native(args, ws, rank, local):
     ms_prof = 1e3 * (time.perf_counter() - tp0)
     ctx.set_profiling(False)
     regions = {}
-    for reg in ("assembly_values", "spmm", "mf_factor", "mf_solve", "dense_block", "gram_tc"):
+    for reg in ("assembly_values", "spmm", "mf_factor", "mf_solve", "dense_block", "gram_tc", "vector_ops",
+                "block_scale"):
         regions[reg] = ctx.profile(reg)
     dom_name = max(regions, key=lambda k: regions[k]["ms"])
     hbm, peak_kind = peaks()

@@ -100,6 +100,8 @@ def lib():
         "fem2d_gep_recompute": (ctypes.c_int, [P, P]),
         "fem2d_gep_values_noalloc": (ctypes.c_int, [P, P, ctypes.c_void_p, ctypes.c_void_p]),
         "fem2d_gep_set_upper_values": (ctypes.c_int, [P, dp, dp]),
+        "fem2d_block_gemm_device": (ctypes.c_int, [P, ctypes.c_int, i64, ctypes.c_void_p, i64, ctypes.c_int,
+                                                   ctypes.c_void_p, ctypes.c_int, d, d, ctypes.c_void_p, i64]),
         "fem2d_domain_table_doubles": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]),
         "fem2d_block_gram_device": (ctypes.c_int, [P, ctypes.c_int, i64, ctypes.c_void_p, i64, ctypes.c_int,
                                                    ctypes.c_void_p, i64, ctypes.c_int, ctypes.c_void_p]),
@@ -789,6 +791,14 @@ def block_gram_device(ctx, method, n, d_x, ldx, a, d_y, ldy, b, d_c):
     or GRAM_FP64 (CUDA cores). Synchronises."""
     _check(lib().fem2d_block_gram_device(ctx._h, int(method), int(n), ctypes.c_void_p(d_x), int(ldx), int(a),
                                          ctypes.c_void_p(d_y), int(ldy), int(b), ctypes.c_void_p(d_c)))
+
+
+def block_gemm_device(ctx, method, n, d_x, ldx, a, d_c, b, alpha, beta, d_z, ldz):
+    """Z = beta Z + alpha X C on device blocks (raw pointers, row-major; C is a x b): method GRAM_TENSOR
+    (tcgen05 FP64 emulation) or GRAM_FP64 (CUDA cores). Synchronises."""
+    _check(lib().fem2d_block_gemm_device(ctx._h, int(method), int(n), ctypes.c_void_p(d_x), int(ldx), int(a),
+                                         ctypes.c_void_p(d_c), int(b), float(alpha), float(beta), ctypes.c_void_p(d_z),
+                                         int(ldz)))
 
 
 def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=0, tol=0.0, max_outer=0,

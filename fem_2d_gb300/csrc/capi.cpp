@@ -822,6 +822,17 @@ int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d
   API_END
 }
 
+int fem2d_block_gemm_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
+                            const double* d_c, int b, double alpha, double beta, double* d_z, int64_t ldz) {
+  API_BEGIN
+  if (!c || !d_x || !d_c || !d_z) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (n < 0 || a < 1 || b < 1 || ldx < a || ldz < b) fail(FEM2D_E_INVALID_ARG, "bad block sizes");
+  if (method != 0 && method != 1) fail(FEM2D_E_INVALID_ARG, "method must be 0 (tensor) or 1 (FP64)");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  block_gemm(c->c, method, n, d_x, ldx, a, d_c, b, alpha, beta, d_z, ldz);
+  API_END
+}
+
 int fem2d_gpu_solve_gep(fem2d_ctx* c, const fem2d_gep* g, double target, int n_pairs, const fem2d_solve_opts* opts,
                         double* values, double* vectors, double* residuals, fem2d_solve_stats* stats) {
   API_BEGIN

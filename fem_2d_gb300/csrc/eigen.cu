@@ -416,6 +416,18 @@ struct Dev {
     ozaki_gram(c, h.n, X, ldx, a, Y, ldy, b, Cd, ozw.p, ozw.n, ozerr.p);
     return true;
   }
+  // Z = beta Z + alpha X C (C device, a x b) on the tensor cores; false when the FP64 kernel must be used
+  bool tensor_gemm(const double* X, int64_t ldx, int a, const double* Cd, int b, double alpha, double beta, double* Z,
+                   int64_t ldz) {
+    if (dense_mode != 0 || a > 256 || b > 32 || a <= 0 || b <= 0) return false;
+    ProfScope ps(c, "gemm_tc", 8.0 * h.n * (a + (beta != 0.0 ? 2.0 : 1.0) * b), 2.0 * h.n * a * b);
+    if (ozerr.n == 0) {
+      ozerr.alloc_on(1, c.stream);
+      FEM2D_CUDA(cudaMemsetAsync(ozerr.p, 0, sizeof(int), c.stream));
+    }
+    ozaki_gemm(c, h.n, X, ldx, a, Cd, b, alpha, beta, Z, ldz, ozerr.p);
+    return true;
+  }
   // the tensor Gram kernel's error flag (synchronises the stream)
   void check_tensor() {
     if (ozerr.n == 0) return;
@@ -480,6 +492,21 @@ struct Dev {
   void gemm(const double* X, int64_t ldx, int a, const std::vector<double>& C, int b, double beta, double* Z,
             int64_t ldz) {
     if (a <= 0 || b <= 0) return;
+    if (dense_mode == 0 && a <= 256) {
+      // 32 columns of C at a time through the tensor-core kernel
+      std::vector<double> Ct;
+      for (int j0 = 0; j0 < b; j0 += 32) {
+        const int w = std::min(32, b - j0);
+        Ct.resize((size_t)a * w);
+        for (int i = 0; i < a; i++)
+          for (int j = 0; j < w; j++) Ct[(size_t)i * w + j] = C[(size_t)i * b + j0 + j];
+        if (small.n < Ct.size()) small.alloc_on(std::max<size_t>(Ct.size(), 16384), c.stream);
+        FEM2D_CUDA(cudaMemcpyAsync(small.p, Ct.data(), Ct.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        tensor_gemm(X, ldx, a, small.p, w, 1.0, beta, Z + j0, ldz);
+        // (pageable copies are staged before cudaMemcpyAsync returns: Ct may be reused)
+      }
+      return;
+    }
     ProfScope ps(c, "dense_block", 8.0 * h.n * (a + (beta != 0.0 ? 2.0 : 1.0) * b), 2.0 * h.n * a * b);
     const int chunk = std::max(1, std::min(b, (int)((96 * 1024) / (sizeof(double) * a))));
     std::vector<double> Ct;
@@ -498,6 +525,7 @@ struct Dev {
     }
   }
   void axpby(double alpha, const double* X, int64_t ldx, int b, double beta, double* Y, int64_t ldy) {
+    ProfScope ps(c, "vector_ops", 8.0 * h.n * b * (beta != 0.0 ? 3.0 : 2.0));
     const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
     axpby_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, b, alpha, X, ldx, beta, Y, ldy);
     c.launches++;
@@ -522,6 +550,7 @@ struct Dev {
   void gemm_dev(const double* X, int64_t ldx, int a, const double* Cd, int b, double alpha, double beta, double* Z,
                 int64_t ldz) {
     if (a <= 0 || b <= 0) return;
+    if (tensor_gemm(X, ldx, a, Cd, b, alpha, beta, Z, ldz)) return;
     ProfScope ps(c, "dense_block", 8.0 * h.n * (a + (beta != 0.0 ? 2.0 : 1.0) * b), 2.0 * h.n * a * b);
     const size_t smem = (size_t)a * b * sizeof(double);
     if (smem > 96 * 1024) fail(FEM2D_E_INVALID_ARG, "device-resident projection block too large");
@@ -531,6 +560,7 @@ struct Dev {
     c.launches++;
   }
   void copy(const double* X, int64_t ldx, int b, double* Y, int64_t ldy) {
+    ProfScope ps(c, "vector_ops", 16.0 * h.n * b);
     const int64_t blocks = std::min<int64_t>((h.n * b + 255) / 256, (int64_t)c.num_sms * 8);
     copy_block_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(h.n, b, X, ldx, Y, ldy);
     c.launches++;
@@ -651,7 +681,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   bool blocked = false;
   if (o.scaling == 2 || (o.scaling == 0 && large)) {
     try {
-      bsc.build(c, h, d, sa.p, sb.p);
+      {
+        ProfScope ps_bs(c, "block_scale", 0.0);
+        bsc.build(c, h, d, sa.p, sb.p);
+      }
       blocked = true;
     } catch (const Error&) {
       if (o.scaling == 2) throw;
@@ -791,7 +824,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   if (!iterative && (rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense && o.scaling == 0) {
     // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
     try {
-      bsc.build(c, h, d, sa.p, sb.p);
+      {
+        ProfScope ps_bs(c, "block_scale", 0.0);
+        bsc.build(c, h, d, sa.p, sb.p);
+      }
       blocked = true;
       factor_both();
       nref_p = calibrate(fp, 1.0, cshift, rel_p);
@@ -1050,8 +1086,11 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     const int nblk = std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
     const int64_t rpb = (n + nblk - 1) / nblk;
     P.alloc_on((size_t)nblk * 3 * nc, c.stream);
-    resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AY.p, BY.p, XY.p, nc, nc, th_d.p, rpb, P.p);
-    c.launches++;
+    {
+      ProfScope ps_r(c, "vector_ops", 24.0 * n * nc);
+      resid_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, AY.p, BY.p, XY.p, nc, nc, th_d.p, rpb, P.p);
+      c.launches++;
+    }
     std::vector<double> Ph((size_t)nblk * 3 * nc);
     FEM2D_CUDA(cudaMemcpyAsync(Ph.data(), P.p, Ph.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     FEM2D_CUDA(cudaStreamSynchronize(c.stream));
@@ -1415,6 +1454,25 @@ void block_gram(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int
   D.dense_mode = method == 0 ? 0 : 1;
   if (method == 0 && (a > 512 || b > 256)) fail(FEM2D_E_INVALID_ARG, "tensor Gram: a <= 512 and b <= 256");
   D.gram_dev(X, ldx, a, Y, ldy, b, Cd);
+  D.check_tensor();
+  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+}  // namespace fem2d
+
+namespace fem2d {
+
+// Z = beta Z + alpha X C (device blocks; C row-major a x b): method 0 tensor cores, 1 FP64 CUDA cores
+void block_gemm(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Cd, int b,
+                double alpha, double beta, double* Z, int64_t ldz) {
+  setup_gemm_smem(c.device);
+  HostGEP hg;
+  hg.n = n;
+  DeviceGEP dg;
+  Dev D{c, hg, dg, nullptr, nullptr};
+  D.dense_mode = method == 0 ? 0 : 1;
+  if (method == 0 && (a > 256 || b > 32)) fail(FEM2D_E_INVALID_ARG, "tensor update: a <= 256 and b <= 32");
+  D.gemm_dev(X, ldx, a, Cd, b, alpha, beta, Z, ldz);
   D.check_tensor();
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
 }

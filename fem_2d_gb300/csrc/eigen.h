@@ -24,6 +24,9 @@ void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP&
                    double cb, bool spd,
                    int nrhs, const double* rhs, double* x);
 // C (device, row-major a x b) = X^T Y: method 0 on the tensor cores (ozaki.cu), 1 on the FP64 CUDA cores
+// Z = beta Z + alpha X C (device, C row-major a x b): method 0 tensor cores, 1 FP64 CUDA cores
+void block_gemm(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Cd, int b,
+                double alpha, double beta, double* Z, int64_t ldz);
 void block_gram(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Y, int64_t ldy,
                 int b, double* Cd);
 

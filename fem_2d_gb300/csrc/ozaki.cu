@@ -376,6 +376,190 @@ __global__ void ozaki_reduce_kernel(const double* __restrict__ P, int nrb, int n
   C[e] = s;
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Z = beta Z + alpha X C for a tall X (n x a, a <= 256) and a small C (a x b, b <= 32): the block
+// updates of the B-orthogonalisation and the Ritz-vector products. Each CTA owns 128-row tiles of X
+// and Z (one row per thread). X is sliced with one exponent per row (over its a entries) and C with one
+// per column (over its a entries), so every K sub-block's digit sums share one scale: they are read
+// from TMEM after each 128 columns of K (the exact-accumulation limit) and summed exactly in int64,
+// and converted to FP64 once per output element. C's digit planes stay in shared memory for all tiles.
+constexpr int kGemmKMax = 256;
+constexpr int kPlaneC = kN * kGemmKMax * 2;          // one digit plane of C (32 x 256 bf16, K-major)
+constexpr int kGemmSmem = kDigits * kPlaneA + kDigits * kPlaneC + 1024;
+
+// byte offset of core matrix (row group rg, k group kg) in a K-major tile with kc columns
+__device__ __forceinline__ int core_off_k(int rg, int kg, int kc) { return (rg * (kc / 8) + kg) * 128; }
+
+__global__ void __launch_bounds__(kThreads, 1)
+    ozaki_gemm_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ C, int b,
+                      double alpha, double beta, double* __restrict__ Z, int64_t ldz, int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;                              // kDigits planes of kM x kSub (X sub-block)
+  uint8_t* sC = smem + kDigits * kPlaneA;          // kDigits planes of kN x kGemmKMax (all of C)
+  int* eC = reinterpret_cast<int*>(sC + kDigits * kPlaneC);   // kN column exponents of C
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(eC + kN);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int kc = (a + kSub - 1) / kSub * kSub;     // K padded to whole sub-blocks
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // C's column exponents, then its digit planes (row j of the B operand = column j of C)
+  if (tid < kN) {
+    int e = 0;
+    if (tid < b)
+      for (int k = 0; k < a; k++) e = max(e, biased_exp(C[(int64_t)k * b + tid]));
+    eC[tid] = e;
+  }
+  __syncthreads();
+  for (int t = tid; t < kN * (kc / 8); t += kThreads) {
+    const int j = t % kN, kg = t / kN;
+    uint32_t pk[kDigits][4];
+#pragma unroll
+    for (int r8 = 0; r8 < 8; r8 += 2) {
+      float d0[kDigits], d1[kDigits];
+      const int k0 = kg * 8 + r8;
+      digits8((j < b && k0 < a) ? C[(int64_t)k0 * b + j] : 0.0, eC[j], d0);
+      digits8((j < b && k0 + 1 < a) ? C[(int64_t)(k0 + 1) * b + j] : 0.0, eC[j], d1);
+#pragma unroll
+      for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
+    }
+    const int off = core_off_k(j >> 3, kg, kGemmKMax) + (j & 7) * 16;
+#pragma unroll
+    for (int s2 = 0; s2 < kDigits; s2++)
+      *reinterpret_cast<uint4*>(sC + s2 * kPlaneC + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t mb = smem_addr(mbar);
+  uint32_t phase = 0;
+  bool failed = false;
+  constexpr uint32_t idesc = instr_desc(kM, kN);
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+
+  const int64_t ntiles = (n + kM - 1) / kM;
+  for (int64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+    const int64_t row = tile * kM + tid;
+    const bool row_ok = row < n;
+    const double* xr = X + row * ldx;
+    int Ex = 0;
+    if (row_ok) {
+      int k = 0;
+      for (; k + 16 <= a; k += 16) {
+        double v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) v[q] = __ldg(xr + k + q);
+#pragma unroll
+        for (int q = 0; q < 16; q++) Ex = max(Ex, biased_exp(v[q]));
+      }
+      for (; k < a; k++) Ex = max(Ex, biased_exp(__ldg(xr + k)));
+    }
+    long long Th[kN], Tl[kN];
+#pragma unroll
+    for (int j = 0; j < kN; j++) Th[j] = Tl[j] = 0;
+    for (int k0 = 0; k0 < kc && !failed; k0 += kSub) {
+      // this thread's row of the X sub-block (32 columns) as digit planes
+      double xv[kSub];
+#pragma unroll
+      for (int q = 0; q < kSub; q++) xv[q] = (row_ok && k0 + q < a) ? __ldg(xr + k0 + q) : 0.0;
+#pragma unroll
+      for (int kg = 0; kg < kSub / 8; kg++) {
+        uint32_t pk[kDigits][4];
+#pragma unroll
+        for (int r8 = 0; r8 < 8; r8 += 2) {
+          float d0[kDigits], d1[kDigits];
+          digits8(xv[kg * 8 + r8], Ex, d0);
+          digits8(xv[kg * 8 + r8 + 1], Ex, d1);
+#pragma unroll
+          for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
+        }
+        const int off = core_off(tid >> 3, kg) + (tid & 7) * 16;
+#pragma unroll
+        for (int s2 = 0; s2 < kDigits; s2++)
+          *reinterpret_cast<uint4*>(sA + s2 * kPlaneA + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const bool first = (k0 % kChunk) == 0;   // the accumulators restart every 128 columns of K
+      if (tid == 0) {
+        const uint32_t aBase = smem_addr(sA), cBase = smem_addr(sC);
+#pragma unroll 1
+        for (int g = 0; g < kDigits; g++)
+          for (int s2 = 0; s2 <= g; s2++) {
+            const int t = g - s2;
+#pragma unroll
+            for (int kk = 0; kk < kSub / 16; kk++) {
+              const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
+              const uint64_t dc =
+                  smem_desc(cBase + t * kPlaneC + ((k0 / 8) + 2 * kk) * 128, 128, (kGemmKMax / 8) * 128);
+              const uint32_t accum = (!first || s2 > 0 || kk > 0) ? 1u : 0u;
+              mma_bf16(tmem + (uint32_t)(g * kN), da, dc, idesc, accum);
+            }
+          }
+        mma_commit(mb);
+      }
+      if (!mbar_wait(mb, phase)) failed = true;
+      phase ^= 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const bool last = (k0 + kSub) % kChunk == 0 || k0 + kSub >= kc;
+      if (last && !failed) {
+        // exact digit sums of these (at most 128) columns of K into the int64 accumulators
+#pragma unroll
+        for (int cb = 0; cb < kN; cb += 8) {
+#pragma unroll
+          for (int g = 0; g < kDigits; g++) {
+            float v[8];
+            tmem_ld8(lane_base + (uint32_t)(g * kN + cb), v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+              const long long iv = (long long)__float2int_rn(v[q]);
+              if (g < 4) Th[cb + q] += iv << (7 * (3 - g));
+              else Tl[cb + q] += iv << (7 * (7 - g));
+            }
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      }
+      // the digit planes (and after `last`, the accumulators) are free for the next sub-block
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (failed) break;
+    if (row_ok) {
+      double* zr = Z + row * ldz;
+#pragma unroll
+      for (int j = 0; j < kN; j++) {
+        if (j >= b) break;
+        const double t = fma((double)Tl[j], 0x1p-28, (double)Th[j]);
+        const double v = alpha * (t * pow2(Ex + eC[j] - 2044 - 35));
+        zr[j] = beta == 0.0 ? v : fma(beta, zr[j], v);
+      }
+    }
+  }
+  if (failed) {
+    atomicOr(err, 1);
+    mbar_wait(mb, phase ^ 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
 std::mutex g_attr_mu;
 bool g_attr_done[256] = {};
 
@@ -393,6 +577,26 @@ int ozaki_gram_partials(int64_t n, int a, int b, int num_sms) {
 size_t ozaki_gram_workspace(int64_t n, int a, int b, int num_sms) {
   const int tiles = ((a + kM - 1) / kM) * ((b + kN - 1) / kN);
   return (size_t)ozaki_gram_partials(n, a, b, num_sms) * tiles * kM * kN;
+}
+
+void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* C, int b, double alpha,
+                double beta, double* Z, int64_t ldz, int* err) {
+  if (n <= 0 || b <= 0) return;
+  if (a < 1 || a > kGemmKMax || b > kN) fail(FEM2D_E_INVALID_ARG, "ozaki_gemm: a <= 256 and b <= 32");
+  static std::mutex mu;
+  static bool done[256] = {};
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (c.device >= 0 && c.device < 256 && !done[c.device]) {
+      FEM2D_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
+      done[c.device] = true;
+    }
+  }
+  const int64_t ntiles = (n + kM - 1) / kM;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)c.num_sms));
+  ozaki_gemm_kernel<<<grid, kThreads, kGemmSmem, c.stream>>>(n, X, ldx, a, C, b, alpha, beta, Z, ldz, err);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
 }
 
 void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* Y, int64_t ldy, int b,

@@ -241,6 +241,12 @@ int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c
  * wait inside the tensor kernel expired. */
 int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
                             const double* d_y, int64_t ldy, int b, double* d_c);
+/* Z = beta Z + alpha X C for device blocks X (n x a, ldx), C (a x b, row-major) and Z (n x b, ldz): the
+ * block updates of gpu_solve_gep's B-orthogonalisation and its Ritz-vector products (no counterpart in
+ * the reference), exposed for checking and timing. method 0: FP64 emulated on the tensor cores (a <= 256,
+ * b <= 32), 1: FP64 CUDA cores. Synchronises; FEM2D_E_TIMEOUT as fem2d_block_gram_device. */
+int fem2d_block_gemm_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
+                            const double* d_c, int b, double alpha, double beta, double* d_z, int64_t ldz);
 typedef struct fem2d_patchnet fem2d_patchnet;
 typedef struct fem2d_solve_opts {
   int precond;          /* how T = (A - s B)^-1 A (A + c B)^-1 B solves its two shifted systems (the KSP

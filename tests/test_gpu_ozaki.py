@@ -77,3 +77,33 @@ def test_tensor_gram_symmetric_products(ctx):
     assert np.max(np.abs(G - G.T)) <= 1e-13 * np.max(np.abs(G))
     d = np.sum(X * X, axis=0)
     assert np.all(np.abs(np.diag(G) - d) <= np.diag(_chunk_bound(X, X)) + 1e-15 * X.shape[0] * d)
+
+
+def _gemm(ctx, method, X, C, Z0, alpha, beta):
+    torch = pytest.importorskip("torch")
+    dx = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    dc = torch.from_numpy(np.ascontiguousarray(C)).cuda()
+    dz = torch.from_numpy(np.ascontiguousarray(Z0)).cuda()
+    torch.cuda.synchronize()
+    n, a = X.shape
+    b = C.shape[1]
+    fg.block_gemm_device(ctx, method, n, dx.data_ptr(), a, a, dc.data_ptr(), b, alpha, beta, dz.data_ptr(), b)
+    return dz.cpu().numpy()
+
+
+@pytest.mark.parametrize("n,a,b,beta", [(1, 1, 1, 0.0), (300, 7, 5, 1.0), (100003, 150, 30, 1.0),
+                                        (20000, 256, 32, 0.0), (50000, 129, 17, -0.5)])
+def test_tensor_block_update(ctx, n, a, b, beta):
+    """Z = beta Z + alpha X C: the per-row / per-column slicing bound is 2^-49 a max|x_i| max|c_j|."""
+    rng = np.random.default_rng(n + 3 * a + b)
+    X = rng.standard_normal((n, a)) * 10.0 ** rng.uniform(-3, 3, size=(n, 1))
+    C = rng.standard_normal((a, b))
+    Z0 = rng.standard_normal((n, b))
+    alpha = -1.0
+    ref = beta * Z0 + alpha * (X @ C)
+    Zt = _gemm(ctx, fg.GRAM_TENSOR, X, C, Z0, alpha, beta)
+    Zf = _gemm(ctx, fg.GRAM_FP64, X, C, Z0, alpha, beta)
+    bound = 2.0 ** -49 * a * np.outer(np.max(np.abs(X), axis=1), np.max(np.abs(C), axis=0)) \
+        + 1e-15 * (abs(beta) * np.abs(Z0) + a * (np.abs(X) @ np.abs(C)))
+    assert np.all(np.abs(Zt - ref) <= bound)
+    assert np.all(np.abs(Zf - ref) <= bound)
