@@ -316,12 +316,14 @@ def run_reference(args, ws, rank):
     print(json.dumps(out), flush=True)
 
 
-def learned_vs_plain(ctx, eval_nx=32, eval_ny=16, train_nx=16, train_ny=8, shift=10.0, k=4, hidden=64,
+def learned_vs_plain(ctx, eval_nx=16, eval_ny=8, train_nx=8, train_ny=4, shift=10.0, k=4, hidden=64,
                      epochs=300, n_pairs=10):
     """The metric's learned-vs-plain comparison on the learned-preconditioner family (KOLeg, orders (5,7),
     two rounds of U/V refinement): gpu_solve_gep for the 10 pairs nearest 10.0 with iterative inner solves
     (CG on A + 10 B, MINRES on A - 10 B), once with the plain additive-Schwarz preconditioner and once
-    with the learned two-level preconditioner, on the held-out seed 4 at eval_nx x eval_ny base Elems;
+    with the learned two-level preconditioner, on the held-out seed 4 at eval_nx x eval_ny base Elems
+    (16 x 8 by default, 34,570 DoFs, about two minutes for both arms; `--learned-full` runs the family's
+    full 32 x 16 size, 138,861 DoFs);
     both to the same outer tolerance, each timed end to end (preconditioner set-up included) and checked
     against the exact multifrontal path's eigenvalues. The per-Elem-patch network is trained on the GPU
     by the library's own kernels on error vectors of the plain solver (harvest_errors) on seeds 1..3 at
@@ -504,8 +506,8 @@ def run_native(args, ws, rank, local):
            "config": {"workload": w.name, "ndofs": n, "nnz_upper": nnz_u, "nnz_full": nnz_f,
                       "visits": gep.num_visits, "basis": "KOLeg" if w.basis == 1 else "HierPoly",
                       "glq": list(w.glq), "n_pairs": w.n_pairs, "target": w.target, "seed": w.seed,
-                      "precond": "exact multifrontal shift-invert (inner PCG with plain and learned "
-                                 "preconditioners measured separately: learned_vs_plain)",
+                      "precond": "exact multifrontal shift-invert solves (the eigensolve with iterative inner "
+                                 "solves, plain vs learned preconditioner, is measured in learned_vs_plain)",
                       "l2": "256 MiB device write between timed steps", "parallelism": "replicas" if ws > 1 else "1 GPU"},
            "t_assembly_s": t_asm / args.steps / 1e3, "t_eigensolve_s": t_eig / args.steps / 1e3,
            "wall_s_timed": wall, "gpu_launches": launches,
@@ -522,7 +524,7 @@ def run_native(args, ws, rank, local):
     if rank == 0 and not args.no_check:
         out["accuracy"] = accuracy_check(w, mesh, ctx, res)
     if rank == 0 and ws == 1 and not args.no_learned:
-        out["learned_vs_plain"] = learned_vs_plain(ctx)
+        out["learned_vs_plain"] = (learned_vs_plain(ctx, 32, 16, 16, 8) if args.learned_full else learned_vs_plain(ctx))
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 4
         sw, what = cpu_sample(args.workload)
@@ -648,6 +650,7 @@ def main():
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-full", action="store_true")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--workers", type=int, default=8)
     args = ap.parse_args()

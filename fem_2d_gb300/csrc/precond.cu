@@ -1120,8 +1120,10 @@ void PCGSolver::minres_device(double ka, double kb, const double* R, int64_t ldr
     for (int j = 0; j < nb; j++) any = any || !done[j];
     if (!any) break;
     // z_j = z_j / gamma_j
+    // a finished column gets zero coefficients everywhere: its vectors become and stay exactly zero
+    // (frozen recurrences would otherwise grow without bound, and 0 * inf poisons x)
     std::fill(sc.begin(), sc.end(), 0.0);
-    for (int j = 0; j < nb; j++) sc[j] = g[j] > 0.0 ? 1.0 / g[j] : 0.0;
+    for (int j = 0; j < nb; j++) sc[j] = (!done[j] && g[j] > 0.0) ? 1.0 / g[j] : 0.0;
     I.upload_scalars(sc);
     lincomb3_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, z, nullptr, nullptr, z);
     c.launches++;
@@ -1129,9 +1131,9 @@ void PCGSolver::minres_device(double ka, double kb, const double* R, int64_t ldr
     const std::vector<double> delta = I.dots(az, z, nb);
     // v2 = az - (delta / gamma) v1 - (gamma / gamma_prev) v0
     for (int j = 0; j < nb; j++) {
-      sc[j] = 1.0;
-      sc[kNB + j] = g[j] > 0.0 ? -delta[j] / g[j] : 0.0;
-      sc[2 * kNB + j] = gprev[j] > 0.0 ? -g[j] / gprev[j] : 0.0;
+      sc[j] = done[j] ? 0.0 : 1.0;
+      sc[kNB + j] = (!done[j] && g[j] > 0.0) ? -delta[j] / g[j] : 0.0;
+      sc[2 * kNB + j] = (!done[j] && gprev[j] > 0.0) ? -g[j] / gprev[j] : 0.0;
     }
     I.upload_scalars(sc);
     lincomb3_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, az, v1, v0, v2);
