@@ -194,14 +194,16 @@ def oracle_check(w, key, gep, res):
         del gr, gc, ga, gb, key_g
         ov = np.asarray(fx["eigenvalues"])
         gv = np.sort(res.values)
-        rel = np.abs(gv - ov) / np.abs(ov)
+        m = min(len(ov), len(gv))
+        # each oracle eigenvalue against the nearest GPU eigenvalue (equal counts when both found all pairs)
+        rel = np.array([np.min(np.abs(gv - t)) / abs(t) for t in ov[:m]])
         out = {"oracle": "committed FP64 oracle fixture (tests/golden/full_form_%s.json): literal 2-D assembly + "
                          "ARPACK shift-invert Lanczos with SuperLU solves" % key,
                "ndofs_match": gep.dimension == fx["ndofs"], "nnz_upper_match": gep.dims()[1] == fx["nnz_upper"],
                "pattern_bit_exact": h.hexdigest() == fx["pattern_sha256"], "sample_keys_found": found,
                "sample_entries": len(key_s), "entry_err_A": ea, "entry_err_B": eb,
-               "eig_rel_err_max": float(np.max(rel)), "eig_rel_err": rel.tolist(),
-               "oracle_eig_err_bound_rel_max": float(np.max(np.asarray(fx["err_bound"]) / np.abs(ov)))}
+               "eig_rel_err_max": float(np.max(rel)), "eig_rel_err": rel.tolist(), "pairs_compared": int(m),
+               "oracle_rr_vs_mu_max_rel_diff": fx.get("rr_vs_mu_max_rel_diff")}
         if "cross_check" in fx:
             out["oracle_methods_max_rel_diff"] = fx["cross_check"]["max_rel_diff"]
         return out
@@ -461,8 +463,8 @@ def run_native(args, ws, rank, local):
     ms_prof = 1e3 * (time.perf_counter() - tp0)
     ctx.set_profiling(False)
     regions = {}
-    for reg in ("assembly_values", "spmm", "mf_factor", "mf_solve", "dense_block", "gram_tc", "vector_ops",
-                "block_scale"):
+    for reg in ("assembly_values", "spmm", "spmm_tc", "spmm_slice", "mf_factor", "mf_solve", "dense_block", "gram_tc",
+                "gemm_tc", "vector_ops", "block_scale"):
         regions[reg] = ctx.profile(reg)
     dom_name = max(regions, key=lambda k: regions[k]["ms"])
     hbm, peak_kind = peaks()
@@ -483,7 +485,7 @@ def run_native(args, ws, rank, local):
                 "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": f_hbm, "peak_source": peak_kind},
                 "fp64": {"achieved": tfl, "peak": fp64, "unit": "TFLOP/s", "frac": f_fp,
                          "peak_source": "measured (library FP64 FMA microbenchmark, this run)"}}
-        if reg == "gram_tc":
+        if reg in ("gram_tc", "gemm_tc", "spmm_tc"):
             # FP64 emulated on the tensor cores: its FP64-equivalent rate is not bounded by the FP64 pipe;
             # the kernel streams its operands once, so HBM is its roofline (tensor-pipe use from ncu)
             base["fp64"]["note"] = "FP64-equivalent rate of the tensor-core emulation (may exceed the FP64 peak)"

@@ -102,6 +102,8 @@ def lib():
         "fem2d_gep_set_upper_values": (ctypes.c_int, [P, dp, dp]),
         "fem2d_block_gemm_device": (ctypes.c_int, [P, ctypes.c_int, i64, ctypes.c_void_p, i64, ctypes.c_int,
                                                    ctypes.c_void_p, ctypes.c_int, d, d, ctypes.c_void_p, i64]),
+        "fem2d_gep_spmm_tensor_device": (ctypes.c_int, [P, P, ctypes.c_int, d, ctypes.c_void_p, i64, ctypes.c_int,
+                                                        ctypes.c_void_p, i64]),
         "fem2d_domain_table_doubles": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p]),
         "fem2d_block_gram_device": (ctypes.c_int, [P, ctypes.c_int, i64, ctypes.c_void_p, i64, ctypes.c_int,
                                                    ctypes.c_void_p, i64, ctypes.c_int, ctypes.c_void_p]),
@@ -579,6 +581,12 @@ class GEP:
         ctx = ctx or self.ctx
         _check(lib().fem2d_gep_spmm_device(ctx._h, self._h, float(c_a), float(c_b), ctypes.c_void_p(d_x), int(ldx),
                                            int(nb), ctypes.c_void_p(d_y), int(ldy)))
+
+    def spmm_tensor_device(self, which, coef, d_x, ldx, nb, d_y, ldy, ctx=None):
+        """Y = coef M X with M = A (which 0) or B (1) through the tensor-core product (synchronises)."""
+        ctx = ctx or self.ctx
+        _check(lib().fem2d_gep_spmm_tensor_device(ctx._h, self._h, int(which), float(coef), ctypes.c_void_p(d_x),
+                                                  int(ldx), int(nb), ctypes.c_void_p(d_y), int(ldy)))
 
     def print_to_petsc_binary_files(self, dir, prefix):
         """GEP::print_to_petsc_binary_files (linalg.rs:44-52): {dir}/tmp/{prefix}_a.dat and _b.dat."""

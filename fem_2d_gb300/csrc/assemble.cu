@@ -43,6 +43,21 @@ __global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const in
 
 }  // namespace
 
+std::vector<int32_t> row_runs(const HostGEP& g) {
+  std::vector<int32_t> grp{0};
+  for (int64_t i = 1; i <= g.n; i++) {
+    const int64_t h = grp.back();
+    bool brk = i == g.n || i - h >= 64;
+    if (!brk) {
+      const int64_t li = g.row_ptr[i + 1] - g.row_ptr[i], lh = g.row_ptr[h + 1] - g.row_ptr[h];
+      brk = li != lh || std::memcmp(g.col.data() + g.row_ptr[i], g.col.data() + g.row_ptr[h], li * sizeof(int32_t)) != 0;
+    }
+    if (brk) grp.push_back((int32_t)i);
+  }
+  if (g.n == 0) grp.assign(1, 0);
+  return grp;
+}
+
 void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
   cudaStream_t s = c.stream;
   d.row_ptr.upload(g.row_ptr, s);
@@ -69,18 +84,8 @@ void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
   d.a.alloc(g.nnz_full);
   d.b.alloc(g.nnz_full);
   // rows of one Elem's interior functions share their column list; the operator products stage each
-  // run's gathered X rows once (eigen.cu spmm_group_kernel)
-  std::vector<int32_t> grp{0};
-  for (int64_t i = 1; i <= g.n; i++) {
-    const int64_t h = grp.back();
-    bool brk = i == g.n || i - h >= 64;
-    if (!brk) {
-      const int64_t li = g.row_ptr[i + 1] - g.row_ptr[i], lh = g.row_ptr[h + 1] - g.row_ptr[h];
-      brk = li != lh || std::memcmp(g.col.data() + g.row_ptr[i], g.col.data() + g.row_ptr[h], li * sizeof(int32_t)) != 0;
-    }
-    if (brk) grp.push_back((int32_t)i);
-  }
-  if (g.n == 0) grp.assign(1, 0);
+  // run's gathered X rows once (eigen.cu spmm_group_kernel, ozaki.cu spmm_tc_kernel)
+  std::vector<int32_t> grp = row_runs(g);
   std::vector<int2> work;
   for (size_t q = 0; q + 1 < grp.size(); q++) {
     const int64_t len = g.row_ptr[grp[q] + 1] - g.row_ptr[grp[q]];

@@ -811,6 +811,17 @@ int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c
   API_END
 }
 
+int fem2d_gep_spmm_tensor_device(fem2d_ctx* c, const fem2d_gep* g, int which, double coef, const double* d_x,
+                                 int64_t ldx, int nb, double* d_y, int64_t ldy) {
+  API_BEGIN
+  if (!c || !g || !d_x || !d_y) fail(FEM2D_E_INVALID_ARG, "null argument");
+  if (nb < 1 || nb > 32 || ldx < nb || ldy < nb) fail(FEM2D_E_INVALID_ARG, "block width must be 1..32 and fit both leading dimensions");
+  if (g->ctx->device != c->c.device) fail(FEM2D_E_INVALID_ARG, "the GEP lives on another device");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  gep_spmm_tensor(c->c, g->h, g->d, which, coef, d_x, ldx, nb, d_y, ldy);
+  API_END
+}
+
 int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
                             const double* d_y, int64_t ldy, int b, double* d_c) {
   API_BEGIN

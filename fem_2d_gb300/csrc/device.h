@@ -130,6 +130,8 @@ struct DeviceGEP {
 };
 
 // assemble.cu
+// runs of at most 64 consecutive rows with one column list: run starts, then n (the GEP's pattern)
+std::vector<int32_t> row_runs(const HostGEP& g);
 void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d);
 // launches the table kernel and the value kernel; returns device times in ms (tables, values)
 void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, float* ms_values);

@@ -399,6 +399,7 @@ struct Dev {
   DBuf<double> part;
   DBuf<double> small;
   int dense_mode = 0;    // Gram products: 0 FP64 emulated on the tensor cores (ozaki.cu), 1 FP64 CUDA cores
+  TcSpmm* tcs = nullptr;  // products with A or B alone on the tensor cores when set (slices of va, vb)
   DBuf<double> ozw;      // tensor Gram workspace (partial tiles)
   DBuf<int> ozerr;       // set by the tensor Gram kernel when a bounded wait expired
   int grid_rows() const { return std::max(1, c.num_sms * 2); }
@@ -439,6 +440,20 @@ struct Dev {
 
   void spmm(double ca, double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
     const double nv = (ca != 0.0) + (cb != 0.0);
+    if (tcs && nb <= 32 && nv == 1.0) {
+      ProfScope ps(c, "spmm_tc", (double)tcs->plane_units * 16.0 + 4.0 * h.nnz_full + 16.0 * h.n * nb,
+                   2.0 * (double)h.nnz_full * nb);
+      const int64_t zb = std::min<int64_t>((h.n * nb + 255) / 256, (int64_t)c.num_sms * 8);
+      zero_block_kernel<<<(int)std::max<int64_t>(zb, 1), 256, 0, c.stream>>>(h.n, nb, Y, ldy);
+      c.launches++;
+      if (ozerr.n == 0) {
+        ozerr.alloc_on(1, c.stream);
+        FEM2D_CUDA(cudaMemsetAsync(ozerr.p, 0, sizeof(int), c.stream));
+      }
+      tcs->apply(c, ca != 0.0 ? 0 : 1, ca != 0.0 ? ca : cb, d.grp.p, d.row_ptr.p, d.col.p, X, ldx, nb, Y, ldy,
+                 ozerr.p);
+      return;
+    }
     ProfScope ps(c, "spmm", (double)h.nnz_full * (4.0 + 8.0 * nv) + 8.0 * (h.n + 1) + 16.0 * h.n * nb,
                  2.0 * (double)h.nnz_full * nb);
     if (d.nwork > 0 && nb <= 32) {
@@ -930,6 +945,16 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   };
 
   const double norm_a = pencil_norm(1.0, 0.0), norm_b = pencil_norm(0.0, 1.0);
+  // products with A or B alone (the T applications, the basis products) on the tensor cores from here
+  // on: the scaled pencil is final, so its values are sliced once
+  TcSpmm tcs;
+  if (o.dense == 0 && d.nwork > 0) {
+    ProfScope ps(c, "spmm_slice", 16.0 * h.nnz_full, 0.0);
+    tcs.build(c, n, row_runs(h), h.row_ptr);
+    tcs.slice(c, d.grp.p, d.row_ptr.p, sa.p, 0);
+    tcs.slice(c, d.grp.p, d.row_ptr.p, sb.p, 1);
+    D.tcs = &tcs;
+  }
   // start block: T applied to a fixed pseudo-random block
   {
     std::vector<double> R0;
@@ -1262,6 +1287,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       scale_rows_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, kout, sc.p, XO.p, 32);
       c.launches++;
     }
+    D.tcs = nullptr;   // the final residuals use the unscaled pencil (and FP64 products)
     D.va = d.a.p;
     D.vb = d.b.p;
     D.spmm(1.0, 0.0, XO.p, 32, kout, AX.p, 32);
@@ -1473,6 +1499,26 @@ void block_gemm(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int
   D.dense_mode = method == 0 ? 0 : 1;
   if (method == 0 && (a > 256 || b > 32)) fail(FEM2D_E_INVALID_ARG, "tensor update: a <= 256 and b <= 32");
   D.gemm_dev(X, ldx, a, Cd, b, alpha, beta, Z, ldz);
+  D.check_tensor();
+  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+}  // namespace fem2d
+
+namespace fem2d {
+
+// Y = coef M X for M = A (which 0) or B (which 1) of the GEP through the tensor-core product (the GEP's
+// values sliced for this call); synchronises
+void gep_spmm_tensor(Ctx& c, const HostGEP& h, const DeviceGEP& d, int which, double coef, const double* X,
+                     int64_t ldx, int nb, double* Y, int64_t ldy) {
+  if (which != 0 && which != 1) fail(FEM2D_E_INVALID_ARG, "which must be 0 (A) or 1 (B)");
+  if (nb < 1 || nb > 32) fail(FEM2D_E_INVALID_ARG, "1..32 columns");
+  TcSpmm tcs;
+  tcs.build(c, h.n, row_runs(h), h.row_ptr);
+  tcs.slice(c, d.grp.p, d.row_ptr.p, which == 0 ? d.a.p : d.b.p, which);
+  Dev D{c, h, d, d.a.p, d.b.p};
+  D.tcs = &tcs;
+  D.spmm(which == 0 ? coef : 0.0, which == 1 ? coef : 0.0, X, ldx, nb, Y, ldy);
   D.check_tensor();
   FEM2D_CUDA(cudaStreamSynchronize(c.stream));
 }

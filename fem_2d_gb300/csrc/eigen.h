@@ -27,6 +27,9 @@ void shifted_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP&
 // Z = beta Z + alpha X C (device, C row-major a x b): method 0 tensor cores, 1 FP64 CUDA cores
 void block_gemm(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Cd, int b,
                 double alpha, double beta, double* Z, int64_t ldz);
+// Y = coef M X, M = A (which 0) or B (1), through the tensor-core product; synchronises
+void gep_spmm_tensor(Ctx& c, const HostGEP& h, const DeviceGEP& d, int which, double coef, const double* X,
+                     int64_t ldx, int nb, double* Y, int64_t ldy);
 void block_gram(Ctx& c, int method, int64_t n, const double* X, int64_t ldx, int a, const double* Y, int64_t ldy,
                 int b, double* Cd);
 

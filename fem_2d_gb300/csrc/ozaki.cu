@@ -560,6 +560,219 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Operator products Y = coef M X for one matrix M (A or B) of the pencil, nb <= 32 columns.
+// Rows of one Elem's interior functions share a column list (a run, at most 64 rows); a chunk item is
+// (run, 128 consecutive columns of that list). M's values are sliced once per solve (spmm_slice_kernel)
+// into digit planes per (item, 32-column sub-block) in the core-matrix layout the MMA reads, with one
+// exponent per (item, row). The product (spmm_tc_kernel) gathers the item's 128 rows of X, slices them
+// with one exponent per column, runs the 36 digit-pair MMAs per sub-block (M = 128 with the run's rows
+// first; rows past the run are never read back) and adds the exactly recombined chunk into Y.
+constexpr int kPlaneB128 = kN * kChunk * 2;          // one digit plane of the gathered X (32 x 128 bf16)
+constexpr int kSpmmSmem = kDigits * kPlaneA + kDigits * kPlaneB128 + 1024;
+
+__global__ void __launch_bounds__(kThreads) spmm_slice_kernel(int nitems, const int4* __restrict__ items,
+                                                               const int32_t* __restrict__ grp,
+                                                               const int64_t* __restrict__ rp,
+                                                               const int64_t* __restrict__ poff,
+                                                               const int64_t* __restrict__ eoff,
+                                                               const double* __restrict__ v, uint4* __restrict__ planes,
+                                                               int* __restrict__ ex) {
+  __shared__ int erow[64];
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 w = items[it];   // x: run, y: first column, z: rows R, w: columns Lc
+    const int r0 = grp[w.x], R = w.z, R8 = (R + 7) & ~7, Lc = w.w;
+    __syncthreads();
+    if (threadIdx.x < 64) erow[threadIdx.x] = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < R * 16; t += blockDim.x) {   // row r, 8-column group
+      const int r = t / 16, q8 = (t % 16) * 8;
+      const double* vr = v + rp[r0 + r] + w.y;
+      int e = 0;
+      for (int q = q8; q < min(q8 + 8, Lc); q++) e = max(e, biased_exp(vr[q]));
+      atomicMax(&erow[r], e);
+    }
+    __syncthreads();
+    if (threadIdx.x < R) ex[eoff[it] + threadIdx.x] = erow[threadIdx.x];
+    // digit planes: sub-block s (32 columns), plane t, core (rg, kg): 16 bytes per (row, k group)
+    uint4* pl = planes + poff[it];
+    const int per_sub = kDigits * R8 * 4;   // uint4 units per sub-block (R8 rows x 4 k groups per plane)
+    for (int t = threadIdx.x; t < R8 * 16; t += blockDim.x) {
+      const int r = t / 16, kg16 = t % 16, sb = kg16 / 4, kg = kg16 % 4;
+      uint32_t pk[kDigits][4];
+      const double* vr = r < R ? v + rp[r0 + r] + w.y : nullptr;
+      const int E = r < R ? erow[r] : 0;
+#pragma unroll
+      for (int r8 = 0; r8 < 8; r8 += 2) {
+        const int q = sb * 32 + kg * 8 + r8;
+        float d0[kDigits], d1[kDigits];
+        digits8((vr && q < Lc) ? vr[q] : 0.0, E, d0);
+        digits8((vr && q + 1 < Lc) ? vr[q + 1] : 0.0, E, d1);
+#pragma unroll
+        for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
+      }
+      // core matrix (r / 8, kg) of plane s2: 16 bytes at row r % 8
+      const int64_t cm = (int64_t)((r >> 3) * 4 + kg) * 8 + (r & 7);   // uint4 index within a plane
+#pragma unroll
+      for (int s2 = 0; s2 < kDigits; s2++)
+        pl[(int64_t)sb * per_sub + (int64_t)s2 * R8 * 4 + cm] = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    spmm_tc_kernel(int nitems, const int4* __restrict__ items, const int32_t* __restrict__ grp,
+                   const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const int64_t* __restrict__ poff,
+                   const int64_t* __restrict__ eoff, const uint4* __restrict__ planes, const int* __restrict__ ex,
+                   double coef, const double* __restrict__ X, int64_t ldx, int nb, double* __restrict__ Y, int64_t ldy,
+                   int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;                               // kDigits planes of kM x kSub (the item's sub-block of M)
+  uint8_t* sB = smem + kDigits * kPlaneA;           // kDigits planes of kN x kChunk (gathered X)
+  int* eY = reinterpret_cast<int*>(sB + kDigits * kPlaneB128);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(eY + kN);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t mb = smem_addr(mbar);
+  uint32_t phase = 0;
+  bool failed = false;
+  constexpr uint32_t idesc = instr_desc(kM, kN);
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+
+  for (int it = blockIdx.x; it < nitems && !failed; it += gridDim.x) {
+    const int4 w = items[it];
+    const int r0 = grp[w.x], R = w.z, R8 = (R + 7) & ~7, Lc = w.w;
+    const int32_t* cols = col + rp[r0] + w.y;
+    // gathered X rows: column exponents (4 threads per column, 32 rows each), then digit planes
+    if (tid < kN) eY[tid] = 0;
+    __syncthreads();
+    {
+      const int j = tid % kN, part = tid / kN;
+      int e = 0;
+      if (j < nb) {
+        const int q1 = min(Lc, part * 32 + 32);
+        for (int q = part * 32; q < q1; q++) e = max(e, biased_exp(__ldg(X + (int64_t)__ldg(cols + q) * ldx + j)));
+      }
+      atomicMax(&eY[j], e);
+    }
+    __syncthreads();
+    for (int t = tid; t < kN * (kChunk / 8); t += kThreads) {
+      const int j = t % kN, kg = t / kN;
+      uint32_t pk[kDigits][4];
+      double xv[8];
+#pragma unroll
+      for (int r8 = 0; r8 < 8; r8++) {
+        const int q = kg * 8 + r8;
+        xv[r8] = (j < nb && q < Lc) ? __ldg(X + (int64_t)__ldg(cols + q) * ldx + j) : 0.0;
+      }
+#pragma unroll
+      for (int r8 = 0; r8 < 8; r8 += 2) {
+        float d0[kDigits], d1[kDigits];
+        digits8(xv[r8], eY[j], d0);
+        digits8(xv[r8 + 1], eY[j], d1);
+#pragma unroll
+        for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
+      }
+      const int off = core_off_k(j >> 3, kg, kChunk) + (j & 7) * 16;
+#pragma unroll
+      for (int s2 = 0; s2 < kDigits; s2++)
+        *reinterpret_cast<uint4*>(sB + s2 * kPlaneB128 + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+    }
+    const uint4* pl = planes + poff[it];
+    const int per_sub = kDigits * R8 * 4;
+    for (int sb = 0; sb < kChunk / kSub && !failed; sb++) {
+      // the item's digit planes of this sub-block: plane s2 (R8 rows) to the start of smem plane s2
+      for (int t = tid; t < per_sub; t += kThreads) {
+        const int s2 = t / (R8 * 4), rem = t % (R8 * 4);
+        *reinterpret_cast<uint4*>(sA + s2 * kPlaneA + rem * 16) = __ldg(pl + (int64_t)sb * per_sub + t);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        const uint32_t aBase = smem_addr(sA), bBase = smem_addr(sB);
+#pragma unroll 1
+        for (int g = 0; g < kDigits; g++)
+          for (int s2 = 0; s2 <= g; s2++) {
+            const int t = g - s2;
+#pragma unroll
+            for (int kk = 0; kk < kSub / 16; kk++) {
+              const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
+              const uint64_t db =
+                  smem_desc(bBase + t * kPlaneB128 + (sb * 4 + 2 * kk) * 128, 128, (kChunk / 8) * 128);
+              const uint32_t accum = (sb > 0 || s2 > 0 || kk > 0) ? 1u : 0u;
+              mma_bf16(tmem + (uint32_t)(g * kN), da, db, idesc, accum);
+            }
+          }
+        mma_commit(mb);
+      }
+      if (!mbar_wait(mb, phase)) failed = true;
+      phase ^= 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      __syncthreads();   // the sub-block's planes are free for the next one
+    }
+    if (failed) break;
+    if (warp * 32 < R) {   // warps holding rows of the run read their lanes back
+      const int Er = tid < R ? ex[eoff[it] + tid] : 0;
+#pragma unroll
+      for (int cb = 0; cb < kN; cb += 8) {
+        long long Th[8], Tl[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) Th[q] = Tl[q] = 0;
+#pragma unroll
+        for (int g = 0; g < kDigits; g++) {
+          float v[8];
+          tmem_ld8(lane_base + (uint32_t)(g * kN + cb), v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const long long iv = (long long)__float2int_rn(v[q]);
+            if (g < 4) Th[q] += iv << (7 * (3 - g));
+            else Tl[q] += iv << (7 * (7 - g));
+          }
+        }
+        if (tid < R) {
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const int j = cb + q;
+            if (j < nb) {
+              const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
+              atomicAdd(Y + (int64_t)(r0 + tid) * ldy + j, coef * (t * pow2(Er + eY[j] - 2044 - 35)));
+            }
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (failed) {
+    atomicOr(err, 1);
+    mbar_wait(mb, phase ^ 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
 std::mutex g_attr_mu;
 bool g_attr_done[256] = {};
 
@@ -595,6 +808,68 @@ void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
   const int64_t ntiles = (n + kM - 1) / kM;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)c.num_sms));
   ozaki_gemm_kernel<<<grid, kThreads, kGemmSmem, c.stream>>>(n, X, ldx, a, C, b, alpha, beta, Z, ldz, err);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
+}
+
+void TcSpmm::build(Ctx& c, int64_t n, const std::vector<int32_t>& grp_h, const std::vector<int64_t>& row_ptr) {
+  std::vector<int4> it;
+  std::vector<int64_t> po, eo;
+  int64_t pcur = 0, ecur = 0;
+  for (size_t g = 0; g + 1 < grp_h.size(); g++) {
+    const int r0 = grp_h[g], R = grp_h[g + 1] - r0;
+    if (R <= 0) continue;
+    if (R > 64) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: a row run longer than 64 rows");
+    const int64_t len = row_ptr[r0 + 1] - row_ptr[r0];
+    const int R8 = (R + 7) & ~7;
+    for (int64_t q0 = 0; q0 < len; q0 += kChunk) {
+      it.push_back(make_int4((int)g, (int)q0, R, (int)std::min<int64_t>(kChunk, len - q0)));
+      po.push_back(pcur);
+      eo.push_back(ecur);
+      pcur += (int64_t)(kChunk / kSub) * kDigits * R8 * 4;   // uint4 units
+      ecur += R;
+    }
+  }
+  nitems = (int)it.size();
+  plane_units = pcur;
+  exp_count = ecur;
+  items.upload(it, c.stream);
+  poff.upload(po, c.stream);
+  eoff.upload(eo, c.stream);
+  (void)n;
+}
+
+void TcSpmm::slice(Ctx& c, const int32_t* grp, const int64_t* rp, const double* v, int which) {
+  DBuf<uint4>& pl = which == 0 ? planesA : planesB;
+  DBuf<int>& ex = which == 0 ? expA : expB;
+  if (pl.n != (size_t)std::max<int64_t>(plane_units, 1)) pl.alloc_on(std::max<int64_t>(plane_units, 1), c.stream);
+  if (ex.n != (size_t)std::max<int64_t>(exp_count, 1)) ex.alloc_on(std::max<int64_t>(exp_count, 1), c.stream);
+  if (nitems == 0) return;
+  const int grid = std::max(1, std::min(nitems, c.num_sms * 8));
+  spmm_slice_kernel<<<grid, kThreads, 0, c.stream>>>(nitems, items.p, grp, rp, poff.p, eoff.p, v, pl.p, ex.p);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
+  (which == 0 ? readyA : readyB) = true;
+}
+
+void TcSpmm::apply(Ctx& c, int which, double coef, const int32_t* grp, const int64_t* rp, const int32_t* col,
+                   const double* X, int64_t ldx, int nb, double* Y, int64_t ldy, int* err) {
+  if (nb < 1 || nb > kN) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: 1..32 columns");
+  if (!(which == 0 ? readyA : readyB)) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: matrix not sliced");
+  static std::mutex mu;
+  static bool done[256] = {};
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (c.device >= 0 && c.device < 256 && !done[c.device]) {
+      FEM2D_CUDA(cudaFuncSetAttribute(spmm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmmSmem));
+      done[c.device] = true;
+    }
+  }
+  if (nitems == 0) return;
+  const int grid = std::max(1, std::min(nitems, c.num_sms));
+  spmm_tc_kernel<<<grid, kThreads, kSpmmSmem, c.stream>>>(nitems, items.p, grp, rp, col, poff.p, eoff.p,
+                                                         which == 0 ? planesA.p : planesB.p,
+                                                         which == 0 ? expA.p : expB.p, coef, X, ldx, nb, Y, ldy, err);
   FEM2D_CUDA(cudaGetLastError());
   c.launches++;
 }

@@ -2,10 +2,12 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <vector>
+
+#include "device.h"
 
 namespace fem2d {
 
-struct Ctx;
 
 // number of row-range partial tiles the Gram kernel writes for an (n, a, b) product
 int ozaki_gram_partials(int64_t n, int a, int b, int num_sms);
@@ -22,5 +24,22 @@ void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
 // normwise accuracy at FP64 rounding level). Queued on c.stream; *err as ozaki_gram.
 void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* C, int b, double alpha,
                 double beta, double* Z, int64_t ldz, int* err);
+
+// Y = coef M X for one matrix M of a pencil (its values sliced once into digit planes), X and Y
+// row-major n x nb (nb <= 32), Y accumulated (zero it first). Built per pattern (row runs of at most
+// 64 rows with one column list), sliced per value array: which = 0 (A) or 1 (B).
+struct TcSpmm {
+  int nitems = 0;
+  int64_t plane_units = 0, exp_count = 0;
+  DBuf<int4> items;
+  DBuf<int64_t> poff, eoff;
+  DBuf<uint4> planesA, planesB;
+  DBuf<int> expA, expB;
+  bool readyA = false, readyB = false;
+  void build(Ctx& c, int64_t n, const std::vector<int32_t>& grp, const std::vector<int64_t>& row_ptr);
+  void slice(Ctx& c, const int32_t* grp, const int64_t* rp, const double* v, int which);
+  void apply(Ctx& c, int which, double coef, const int32_t* grp, const int64_t* rp, const int32_t* col,
+             const double* X, int64_t ldx, int nb, double* Y, int64_t ldy, int* err);
+};
 
 }  // namespace fem2d

@@ -239,6 +239,14 @@ int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c
  * on exact 7-bit digit slices with exact FP32 accumulation; a <= 512, b <= 256; normwise accuracy at
  * FP64 rounding level), method 1: FP64 on the CUDA cores. Synchronises; FEM2D_E_TIMEOUT if a bounded
  * wait inside the tensor kernel expired. */
+/* Y = coef M X with M = A (which 0) or B (which 1) of the GEP, on the tensor cores: FP64 emulated by
+ * exact 7-bit digit slices of M's values (one exponent per row and 128-column chunk of each row run)
+ * and of X (one exponent per column and chunk), FP32-exact digit sums in TMEM, exact int64 recombination.
+ * The operator product gpu_solve_gep uses for its T applications and basis products (no counterpart in the
+ * reference), exposed for checking and timing; the values are sliced on every call here. Device row-major
+ * n x nb blocks, 1 <= nb <= 32. Synchronises. */
+int fem2d_gep_spmm_tensor_device(fem2d_ctx* c, const fem2d_gep* g, int which, double coef, const double* d_x,
+                                 int64_t ldx, int nb, double* d_y, int64_t ldy);
 int fem2d_block_gram_device(fem2d_ctx* c, int method, int64_t n, const double* d_x, int64_t ldx, int a,
                             const double* d_y, int64_t ldy, int b, double* d_c);
 /* Z = beta Z + alpha X C for device blocks X (n x a, ldx), C (a x b, row-major) and Z (n x b, ldz): the

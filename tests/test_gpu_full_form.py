@@ -55,5 +55,6 @@ def test_eigenvalues_against_oracle_fixture(gep, fixture, dense):
     res = fg.gpu_solve_gep_n(gep, 10.0, 20, dense=dense)
     ov = np.asarray(fixture["eigenvalues"])
     gv = np.sort(res.values)
+    assert len(ov) == len(gv) == 20
     assert np.max(np.abs(gv - ov) / np.abs(ov)) <= 1e-9
     assert res.stats["max_backward_error"] <= 1e-9
