@@ -752,7 +752,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   double inner_worst = 0.0;
 
   Dev D{c, h, d, sa.p, sb.p};
-  D.dense_mode = o.dense;
+  D.dense_mode = o.dense == 1 ? 1 : 0;
   DBuf<double> V, AV, BV, X, AX, BX, G0, W1, W2, W3;
   V.alloc_on((size_t)n * mmax, c.stream);
   AV.alloc_on((size_t)n * mmax, c.stream);
@@ -948,7 +948,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // products with A or B alone (the T applications, the basis products) on the tensor cores from here
   // on: the scaled pencil is final, so its values are sliced once
   TcSpmm tcs;
-  if (o.dense == 0 && d.nwork > 0) {
+  if (o.dense == 2 && d.nwork > 0) {
     ProfScope ps(c, "spmm_slice", 16.0 * h.nnz_full, 0.0);
     tcs.build(c, n, row_runs(h), h.row_ptr);
     tcs.slice(c, d.grp.p, d.row_ptr.p, sa.p, 0);

@@ -276,9 +276,12 @@ typedef struct fem2d_solve_opts {
                            row-run blocks when the Jacobi-scaled factorizations are inaccurate),
                            1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's diagonal blocks
                            over runs of rows with one column list) */
-  int dense;            /* Gram products of the B-orthogonalisation and Rayleigh-Ritz steps: 0 = FP64
-                           emulated on the tensor cores (tcgen05, exact integer slicing; default),
-                           1 = FP64 CUDA cores */
+  int dense;            /* the eigensolver's FP64 contractions: 0 = Gram products and block updates of
+                           the B-orthogonalisation and Rayleigh-Ritz steps emulated on the tensor cores
+                           (tcgen05, exact integer slicing; default), operator products on the FP64
+                           CUDA cores; 1 = everything on the FP64 CUDA cores; 2 = as 0 plus the operator
+                           products with A or B alone on the tensor cores (slower than the CUDA-core
+                           kernel at present: Elem row runs of a few rows fill 128-row MMA tiles poorly) */
   const fem2d_patchnet* net;   /* trained patch network (precond 2), else NULL */
 } fem2d_solve_opts;
 

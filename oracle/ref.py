@@ -669,9 +669,22 @@ def arpack_nearest_physical(A, B, sigma, k, perm, c=None, extra=None, spurious=1
     Z = luB.solve(Rs)
     rb = np.sqrt(np.abs(np.einsum("ij,ij->j", Rs, Z)))
     phys = th[ok]
+    # the eigenvalues from ARPACK's converged mu directly: mu (lambda - sigma)(lambda + c) = lambda, the
+    # root of the sign of lambda's side of sigma. Relative conditioning |d lambda / lambda| / |d mu / mu|
+    # = |(lambda - sigma)(lambda + c)| / (lambda^2 + sigma c) <= 1, and rounding noise in the solves (high-
+    # frequency directions, where T's eigenvalues are ~0) barely moves the wanted mu, whereas a Rayleigh-
+    # Ritz step on (A, B) can turn that noise into spurious or inaccurate Ritz pairs on ill-conditioned
+    # (monomial) pencils
+    qa, qb, qc = mu, mu * (c - sigma) - 1.0, -mu * sigma * c
+    disc = np.sqrt(qb * qb - 4.0 * qa * qc)
+    r1 = (-qb + disc) / (2.0 * qa)
+    r2 = (-qb - disc) / (2.0 * qa)
+    lam_mu = np.where(mu > 0, np.maximum(r1, r2), np.where((r1 > 0) & (r1 < sigma), r1, r2))
+    okm = np.nonzero(np.abs(lam_mu) > spurious * abs(sigma))[0]
+    sel = okm[np.argsort(np.abs(lam_mu[okm] - sigma), kind="stable")][:k]
     return {"values": th[idx], "vectors": X[:, idx], "rel_residual": rel[idx], "backward_error": bwd[idx],
             "resid_binv": rb, "err_bound": _cluster_bounds(th[idx], rb, phys), "mu_min": mu_min,
-            "applications": count[0]}
+            "applications": count[0], "values_from_mu": lam_mu[sel], "mu": mu[sel]}
 
 
 def nd_parts(box, levels=4):
