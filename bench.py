@@ -464,7 +464,7 @@ def run_native(args, ws, rank, local):
     ctx.set_profiling(False)
     regions = {}
     for reg in ("assembly_values", "spmm", "spmm_tc", "spmm_slice", "mf_factor", "mf_solve", "dense_block", "gram_tc",
-                "gemm_tc", "vector_ops", "block_scale"):
+                "gemm_tc", "vector_ops", "block_scale", "rr_host"):
         regions[reg] = ctx.profile(reg)
     dom_name = max(regions, key=lambda k: regions[k]["ms"])
     hbm, peak_kind = peaks()

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -60,6 +61,24 @@ struct ProfScope {
     r.count++;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+  }
+};
+
+// Times host work (wall clock, after draining the stream) when profiling is enabled, under a region name.
+struct HostScope {
+  Ctx& c;
+  const char* name;
+  std::chrono::steady_clock::time_point t0;
+  HostScope(Ctx& ctx, const char* n) : c(ctx), name(n) {
+    if (!c.profile) return;
+    cudaStreamSynchronize(c.stream);
+    t0 = std::chrono::steady_clock::now();
+  }
+  ~HostScope() {
+    if (!c.profile) return;
+    ProfRec& r = c.prof[name];
+    r.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    r.count++;
   }
 };
 

@@ -30,6 +30,8 @@
 #include <numeric>
 
 #include "blockscale.h"
+#include <memory>
+
 #include "eigen.h"
 #include "ozaki.h"
 #include "precond.h"
@@ -402,6 +404,7 @@ struct Dev {
   TcSpmm* tcs = nullptr;  // products with A or B alone on the tensor cores when set (slices of va, vb)
   DBuf<double> ozw;      // tensor Gram workspace (partial tiles)
   DBuf<int> ozerr;       // set by the tensor Gram kernel when a bounded wait expired
+  DBuf<int> ozrow;       // row exponents of the tensor block update
   int grid_rows() const { return std::max(1, c.num_sms * 2); }
 
   // C (device, a x b) = X^T Y on the tensor cores; false when the FP64 CUDA-core kernels must be used
@@ -426,7 +429,8 @@ struct Dev {
       ozerr.alloc_on(1, c.stream);
       FEM2D_CUDA(cudaMemsetAsync(ozerr.p, 0, sizeof(int), c.stream));
     }
-    ozaki_gemm(c, h.n, X, ldx, a, Cd, b, alpha, beta, Z, ldz, ozerr.p);
+    if (ozrow.n < (size_t)std::max<int64_t>(h.n, 1)) ozrow.alloc_on(std::max<int64_t>(h.n, 1), c.stream);
+    ozaki_gemm(c, h.n, X, ldx, a, Cd, b, alpha, beta, Z, ldz, ozrow.p, ozerr.p);
     return true;
   }
   // the tensor Gram kernel's error flag (synchronises the stream)
@@ -1056,6 +1060,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
         GA[(size_t)i * ma + j] = GA[(size_t)j * ma + i] = 0.5 * (GA[(size_t)i * ma + j] + GA[(size_t)j * ma + i]);
         GB[(size_t)i * ma + j] = GB[(size_t)j * ma + i] = 0.5 * (GB[(size_t)i * ma + j] + GB[(size_t)j * ma + i]);
       }
+    auto hs_rr = std::make_unique<HostScope>(c, "rr_host");
     if (!symeig(ma, GB, wb, zb)) fail(FEM2D_E_NOT_CONVERGED, "Gram eigen-decomposition failed");
     const double wbmax = *std::max_element(wb.begin(), wb.end());
     std::vector<int> kb;
@@ -1100,6 +1105,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     for (int i = 0; i < ma; i++)
       for (int q = 0; q < nc; q++) Ysub[(size_t)i * nc + q] = Y[(size_t)i * m2 + order[q]];
     for (int q = 0; q < nc; q++) thc[q] = th[order[q]];
+    hs_rr.reset();
     DBuf<double> AY, BY, XY, th_d, P;
     AY.alloc_on((size_t)n * nc, c.stream);
     BY.alloc_on((size_t)n * nc, c.stream);

@@ -19,11 +19,12 @@
 // output element and chunk: 36 digit-pair MMAs on the tensor pipe, and on the FP64 pipe two
 // conversions and two FMAs instead of 128 FMAs.
 //
-// One CTA (4 warps, one row of C per thread) owns a 128 x 32 tile of C and a range of rows of X and
-// Y. Per 128-row chunk: a pass over the chunk finds each column's exponent; then four 32-row
-// sub-blocks are sliced into shared memory (8 digit planes per operand, K-major core-matrix layout
-// without swizzle) and thread 0 issues the 72 MMAs of the sub-block; their completion is tracked by
-// an mbarrier. Partial tiles of all CTAs are summed by a second, deterministic kernel.
+// A first, coalesced pass (chunk_exp_kernel) finds each column's exponent per 128-row chunk. Then one
+// CTA (4 warps, one row of C per thread) owns a 128 x 32 tile of C and a range of rows of X and Y:
+// per chunk, four 32-row sub-blocks are sliced into shared memory (8 digit planes per operand,
+// K-major core-matrix layout without swizzle) and thread 0 issues the 72 MMAs of the sub-block,
+// tracked by an mbarrier; the loads of a sub-block are issued before waiting on the previous
+// sub-block's MMAs, so they overlap. Partial tiles of all CTAs are summed by a deterministic kernel.
 //
 // Every wait on the mbarrier is bounded (about one second of GPU time): on expiry the kernel raises
 // an error flag, waits once more (bounded) for its MMAs in flight, frees its TMEM and returns.
@@ -148,14 +149,34 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 // byte offset of core matrix (row group rg, k group kg) in a K-major tile with kSub columns
 __device__ __forceinline__ int core_off(int rg, int kg) { return (rg * (kSub / 8) + kg) * 128; }
 
+// E[c * a + j] = biased exponent of max |X[r][j]| over the 128-row chunk c (one pass, coalesced)
+__global__ void __launch_bounds__(128) chunk_exp_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a,
+                                                         int* __restrict__ E) {
+  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
+  const int col = blockIdx.y * 128 + threadIdx.x;
+  if (col >= a) return;
+  const int rows = (int)min((int64_t)kChunk, n - c0);
+  const double* xp = X + c0 * ldx + col;
+  int e = 0, r = 0;
+  for (; r + 16 <= rows; r += 16) {
+    double v[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) v[q] = __ldg(xp + (int64_t)(r + q) * ldx);
+#pragma unroll
+    for (int q = 0; q < 16; q++) e = max(e, biased_exp(v[q]));
+  }
+  for (; r < rows; r++) e = max(e, biased_exp(__ldg(xp + (int64_t)r * ldx)));
+  E[(int64_t)blockIdx.x * a + col] = e;
+}
+
 __global__ void __launch_bounds__(kThreads, 2)
     ozaki_gram_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ Y,
-                      int64_t ldy, int b, int64_t rows_per_cta, double* __restrict__ P, int* __restrict__ err) {
+                      int64_t ldy, int b, int64_t rows_per_cta, const int* __restrict__ EX, const int* __restrict__ EY,
+                      double* __restrict__ P, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;                                   // kDigits planes of kM x kSub bf16
   uint8_t* sB = smem + kDigits * kPlaneA;               // kDigits planes of kN x kSub bf16
-  int* eX = reinterpret_cast<int*>(sB + kDigits * kPlaneB);   // kM column exponents of the chunk
-  int* eY = eX + kM;                                    // kN
+  int* eY = reinterpret_cast<int*>(sB + kDigits * kPlaneB);   // kN column exponents of Y in the chunk
   uint64_t* mbar = reinterpret_cast<uint64_t*>(eY + kN);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
 
@@ -181,7 +202,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   const uint32_t tmem = *tmem_slot;
   const uint32_t mb = smem_addr(mbar);
   uint32_t phase = 0;
-  bool failed = false;
+  bool failed = false, pending = false;
 
   double acc[kN];
 #pragma unroll
@@ -189,103 +210,67 @@ __global__ void __launch_bounds__(kThreads, 2)
 
   const int my_col = col0 + tid;   // this thread's column of X (its row of C)
   const bool col_ok = my_col < a;
+  const int yj = tid % kN, ykg = tid / kN;   // this thread's column of Y and its 8-row group of a sub-block
+  const bool y_ok = cy0 + yj < b;
   constexpr uint32_t idesc = instr_desc(kM, kN);
 
   for (int64_t c0 = r0; c0 < r1 && !failed; c0 += kChunk) {
-    const int rows = (int)min((int64_t)kChunk, r1 - c0);
-    // column exponents of the chunk
-    // (loads issued 16 at a time so that many are in flight: this pass is latency-bound otherwise)
-    {
-      int e = 0;
-      if (col_ok) {
-        const double* xp = X + c0 * ldx + my_col;
-        int r = 0;
-        for (; r + 16 <= rows; r += 16) {
-          double v[16];
-#pragma unroll
-          for (int q = 0; q < 16; q++) v[q] = __ldg(xp + (int64_t)(r + q) * ldx);
-#pragma unroll
-          for (int q = 0; q < 16; q++) e = max(e, biased_exp(v[q]));
-        }
-        for (; r < rows; r++) e = max(e, biased_exp(__ldg(xp + (int64_t)r * ldx)));
-      }
-      eX[tid] = e;
-      if (tid < kN) eY[tid] = 0;
-    }
+    const int64_t chunk = c0 / kChunk;
+    const int Ex = col_ok ? EX[chunk * a + my_col] : 0;
+    if (tid < kN) eY[tid] = (cy0 + tid < b) ? EY[chunk * b + cy0 + tid] : 0;
     __syncthreads();
-    {
-      const int j = tid % kN, part = tid / kN;   // 4 threads per column of Y, 32 rows each
-      int e = 0;
-      if (cy0 + j < b) {
-        const double* yp = Y + c0 * ldy + cy0 + j;
-        const int rb = part * 32, re = min(rows, part * 32 + 32);
-        int r = rb;
-        for (; r + 16 <= re; r += 16) {
-          double v[16];
-#pragma unroll
-          for (int q = 0; q < 16; q++) v[q] = __ldg(yp + (int64_t)(r + q) * ldy);
-#pragma unroll
-          for (int q = 0; q < 16; q++) e = max(e, biased_exp(v[q]));
-        }
-        for (; r < re; r++) e = max(e, biased_exp(__ldg(yp + (int64_t)r * ldy)));
-      }
-      atomicMax(&eY[j], e);
-    }
-    __syncthreads();
-    const int Ex = eX[tid];
-    for (int sb = 0; sb < kChunk / kSub && !failed; sb++) {
+    const int Ey = eY[yj];
+    for (int sb = 0; sb < kChunk / kSub; sb++) {
       const int64_t s0 = c0 + sb * kSub;
-      // X digits: this thread's column, 32 rows = 4 core matrices along K per digit plane
-      double xv[kSub];   // this thread's 32 values of the sub-block, all loads issued before use
+      // this sub-block's values: the loads are issued before waiting on the previous sub-block's MMAs
+      double xv[kSub], yv[8];
 #pragma unroll
       for (int r = 0; r < kSub; r++) {
         const int64_t ra = s0 + r;
         xv[r] = (col_ok && ra < r1) ? __ldg(X + ra * ldx + my_col) : 0.0;
       }
 #pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const int64_t ra = s0 + ykg * 8 + r;
+        yv[r] = (y_ok && ra < r1) ? __ldg(Y + ra * ldy + cy0 + yj) : 0.0;
+      }
+      if (pending) {   // the digit planes are free once the previous sub-block's MMAs have completed
+        if (!mbar_wait(mb, phase)) failed = true;
+        phase ^= 1;
+        pending = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      }
+      if (failed) break;
+#pragma unroll
       for (int kg = 0; kg < kSub / 8; kg++) {
         uint32_t pk[kDigits][4];
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
           float d0[kDigits], d1[kDigits];
-          const double va = xv[kg * 8 + r8];
-          const double vb = xv[kg * 8 + r8 + 1];
-          digits8(va, Ex, d0);
-          digits8(vb, Ex, d1);
+          digits8(xv[kg * 8 + r8], Ex, d0);
+          digits8(xv[kg * 8 + r8 + 1], Ex, d1);
 #pragma unroll
-          for (int s = 0; s < kDigits; s++) pk[s][r8 >> 1] = pack_bf16(d0[s], d1[s]);
+          for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
         }
         const int off = core_off(tid >> 3, kg) + (tid & 7) * 16;
 #pragma unroll
-        for (int s = 0; s < kDigits; s++)
-          *reinterpret_cast<uint4*>(sA + s * kPlaneA + off) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+        for (int s2 = 0; s2 < kDigits; s2++)
+          *reinterpret_cast<uint4*>(sA + s2 * kPlaneA + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
       }
-      // Y digits: column j, one k group of 8 rows per thread
       {
-        const int j = tid % kN, kg = tid / kN;
-        const int Ey = eY[j];
-        const bool ok = cy0 + j < b;
         uint32_t pk[kDigits][4];
-        double yv[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          const int64_t ra = s0 + kg * 8 + r;
-          yv[r] = (ok && ra < r1) ? __ldg(Y + ra * ldy + cy0 + j) : 0.0;
-        }
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
           float d0[kDigits], d1[kDigits];
-          const double va = yv[r8];
-          const double vb = yv[r8 + 1];
-          digits8(va, Ey, d0);
-          digits8(vb, Ey, d1);
+          digits8(yv[r8], Ey, d0);
+          digits8(yv[r8 + 1], Ey, d1);
 #pragma unroll
-          for (int s = 0; s < kDigits; s++) pk[s][r8 >> 1] = pack_bf16(d0[s], d1[s]);
+          for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
         }
-        const int off = core_off(j >> 3, kg) + (j & 7) * 16;
+        const int off = core_off(yj >> 3, ykg) + (yj & 7) * 16;
 #pragma unroll
-        for (int s = 0; s < kDigits; s++)
-          *reinterpret_cast<uint4*>(sB + s * kPlaneB + off) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+        for (int s2 = 0; s2 < kDigits; s2++)
+          *reinterpret_cast<uint4*>(sB + s2 * kPlaneB + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
       }
       // the generic-proxy stores above must be visible to the tensor core's (async) proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -296,21 +281,25 @@ __global__ void __launch_bounds__(kThreads, 2)
         const uint32_t aBase = smem_addr(sA), bBase = smem_addr(sB);
 #pragma unroll 1
         for (int g = 0; g < kDigits; g++)
-          for (int s = 0; s <= g; s++) {
-            const int t = g - s;
+          for (int s2 = 0; s2 <= g; s2++) {
+            const int t = g - s2;
 #pragma unroll
             for (int kk = 0; kk < kSub / 16; kk++) {
-              const uint64_t da = smem_desc(aBase + s * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
+              const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
               const uint64_t db = smem_desc(bBase + t * kPlaneB + kk * 256, 128, (kSub / 8) * 128);
-              const uint32_t accum = (sb > 0 || s > 0 || kk > 0) ? 1u : 0u;
+              const uint32_t accum = (sb > 0 || s2 > 0 || kk > 0) ? 1u : 0u;
               mma_bf16(tmem + (uint32_t)(g * kN), da, db, idesc, accum);
             }
           }
         mma_commit(mb);
       }
-      // the MMAs read the digit planes: wait before the next sub-block overwrites them
+      pending = true;
+    }
+    if (failed) break;
+    if (pending) {   // the chunk's last MMAs, before its accumulators are read
       if (!mbar_wait(mb, phase)) failed = true;
       phase ^= 1;
+      pending = false;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
     if (failed) break;
@@ -383,6 +372,8 @@ __global__ void ozaki_reduce_kernel(const double* __restrict__ P, int nrb, int n
 // per column (over its a entries), so every K sub-block's digit sums share one scale: they are read
 // from TMEM after each 128 columns of K (the exact-accumulation limit) and summed exactly in int64,
 // and converted to FP64 once per output element. C's digit planes stay in shared memory for all tiles.
+// The row exponents come from a coalesced pre-pass (row_exp_kernel), and each sub-block's loads are
+// issued before waiting on the previous sub-block's MMAs.
 constexpr int kGemmKMax = 256;
 constexpr int kPlaneC = kN * kGemmKMax * 2;          // one digit plane of C (32 x 256 bf16, K-major)
 constexpr int kGemmSmem = kDigits * kPlaneA + kDigits * kPlaneC + 1024;
@@ -390,9 +381,24 @@ constexpr int kGemmSmem = kDigits * kPlaneA + kDigits * kPlaneC + 1024;
 // byte offset of core matrix (row group rg, k group kg) in a K-major tile with kc columns
 __device__ __forceinline__ int core_off_k(int rg, int kg, int kc) { return (rg * (kc / 8) + kg) * 128; }
 
+// E[r] = biased exponent of max |X[r][k]| over k < a: one warp per row, lanes across the row
+__global__ void __launch_bounds__(256) row_exp_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a,
+                                                       int* __restrict__ E) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    int e = 0;
+    for (int k = lane; k < a; k += 32) e = max(e, biased_exp(__ldg(X + r * ldx + k)));
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, off));
+    if (lane == 0) E[r] = e;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki_gemm_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ C, int b,
-                      double alpha, double beta, double* __restrict__ Z, int64_t ldz, int* __restrict__ err) {
+                      double alpha, double beta, double* __restrict__ Z, int64_t ldz, const int* __restrict__ EXr,
+                      int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;                              // kDigits planes of kM x kSub (X sub-block)
   uint8_t* sC = smem + kDigits * kPlaneA;          // kDigits planes of kN x kGemmKMax (all of C)
@@ -448,30 +454,27 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
 
   const int64_t ntiles = (n + kM - 1) / kM;
+  bool pending = false;
   for (int64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
     const int64_t row = tile * kM + tid;
     const bool row_ok = row < n;
     const double* xr = X + row * ldx;
-    int Ex = 0;
-    if (row_ok) {
-      int k = 0;
-      for (; k + 16 <= a; k += 16) {
-        double v[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++) v[q] = __ldg(xr + k + q);
-#pragma unroll
-        for (int q = 0; q < 16; q++) Ex = max(Ex, biased_exp(v[q]));
-      }
-      for (; k < a; k++) Ex = max(Ex, biased_exp(__ldg(xr + k)));
-    }
+    const int Ex = row_ok ? EXr[row] : 0;
     long long Th[kN], Tl[kN];
 #pragma unroll
     for (int j = 0; j < kN; j++) Th[j] = Tl[j] = 0;
     for (int k0 = 0; k0 < kc && !failed; k0 += kSub) {
-      // this thread's row of the X sub-block (32 columns) as digit planes
+      // this thread's row of the X sub-block (32 columns), loaded before waiting on the previous MMAs
       double xv[kSub];
 #pragma unroll
       for (int q = 0; q < kSub; q++) xv[q] = (row_ok && k0 + q < a) ? __ldg(xr + k0 + q) : 0.0;
+      if (pending) {
+        if (!mbar_wait(mb, phase)) failed = true;
+        phase ^= 1;
+        pending = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      }
+      if (failed) break;
 #pragma unroll
       for (int kg = 0; kg < kSub / 8; kg++) {
         uint32_t pk[kDigits][4];
@@ -510,10 +513,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         mma_commit(mb);
       }
-      if (!mbar_wait(mb, phase)) failed = true;
-      phase ^= 1;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      pending = true;
       const bool last = (k0 + kSub) % kChunk == 0 || k0 + kSub >= kc;
+      if (last) {   // the accumulators are read back: wait for these MMAs now
+        if (!mbar_wait(mb, phase)) failed = true;
+        phase ^= 1;
+        pending = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      }
       if (last && !failed) {
         // exact digit sums of these (at most 128) columns of K into the int64 accumulators
 #pragma unroll
@@ -533,9 +540,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       }
-      // the digit planes (and after `last`, the accumulators) are free for the next sub-block
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // after `last`, every thread's reads of the accumulators precede the next MMAs
+      if (last) {
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      }
     }
     if (failed) break;
     if (row_ok) {
@@ -552,6 +561,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (failed) {
     atomicOr(err, 1);
     mbar_wait(mb, phase ^ 1);
+  } else if (pending) {
+    if (!mbar_wait(mb, phase)) atomicOr(err, 1);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -789,11 +800,13 @@ int ozaki_gram_partials(int64_t n, int a, int b, int num_sms) {
 
 size_t ozaki_gram_workspace(int64_t n, int a, int b, int num_sms) {
   const int tiles = ((a + kM - 1) / kM) * ((b + kN - 1) / kN);
-  return (size_t)ozaki_gram_partials(n, a, b, num_sms) * tiles * kM * kN;
+  const int64_t chunks = std::max<int64_t>(1, (n + kChunk - 1) / kChunk);
+  // partial tiles, then the chunk exponents of X and Y (ints, two per double)
+  return (size_t)ozaki_gram_partials(n, a, b, num_sms) * tiles * kM * kN + (size_t)(chunks * (a + b) + 1) / 2 + 1;
 }
 
 void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* C, int b, double alpha,
-                double beta, double* Z, int64_t ldz, int* err) {
+                double beta, double* Z, int64_t ldz, int* rowexp, int* err) {
   if (n <= 0 || b <= 0) return;
   if (a < 1 || a > kGemmKMax || b > kN) fail(FEM2D_E_INVALID_ARG, "ozaki_gemm: a <= 256 and b <= 32");
   static std::mutex mu;
@@ -807,9 +820,11 @@ void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
   }
   const int64_t ntiles = (n + kM - 1) / kM;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)c.num_sms));
-  ozaki_gemm_kernel<<<grid, kThreads, kGemmSmem, c.stream>>>(n, X, ldx, a, C, b, alpha, beta, Z, ldz, err);
+  row_exp_kernel<<<(int)std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 16), 256, 0, c.stream>>>(
+      n, X, ldx, a, rowexp);
+  ozaki_gemm_kernel<<<grid, kThreads, kGemmSmem, c.stream>>>(n, X, ldx, a, C, b, alpha, beta, Z, ldz, rowexp, err);
   FEM2D_CUDA(cudaGetLastError());
-  c.launches++;
+  c.launches += 2;
 }
 
 void TcSpmm::build(Ctx& c, int64_t n, const std::vector<int32_t>& grp_h, const std::vector<int64_t>& row_ptr) {
@@ -887,11 +902,20 @@ void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
   }
   const int nrb = ozaki_gram_partials(n, a, b, c.num_sms);
   const int mz = (a + kM - 1) / kM, ny = (b + kN - 1) / kN;
-  if (work_doubles < (size_t)nrb * mz * ny * kM * kN) fail(FEM2D_E_INVALID_ARG, "ozaki_gram: workspace too small");
+  if (work_doubles < ozaki_gram_workspace(n, a, b, c.num_sms)) fail(FEM2D_E_INVALID_ARG, "ozaki_gram: workspace too small");
+  const int64_t chunks = std::max<int64_t>(1, (n + kChunk - 1) / kChunk);
+  int* EX = reinterpret_cast<int*>(work + (size_t)nrb * mz * ny * kM * kN);
+  int* EY = EX + chunks * a;
+  if (n > 0) {
+    chunk_exp_kernel<<<dim3((unsigned)chunks, (a + 127) / 128), 128, 0, c.stream>>>(n, X, ldx, a, EX);
+    chunk_exp_kernel<<<dim3((unsigned)chunks, (b + 127) / 128), 128, 0, c.stream>>>(n, Y, ldy, b, EY);
+    FEM2D_CUDA(cudaGetLastError());
+    c.launches += 2;
+  }
   int64_t rpc = (std::max<int64_t>(n, 1) + nrb - 1) / nrb;
   rpc = (rpc + kChunk - 1) / kChunk * kChunk;
   dim3 grid(nrb, ny, mz);
-  ozaki_gram_kernel<<<grid, kThreads, kSmemBytes, c.stream>>>(n, X, ldx, a, Y, ldy, b, rpc, work, err);
+  ozaki_gram_kernel<<<grid, kThreads, kSmemBytes, c.stream>>>(n, X, ldx, a, Y, ldy, b, rpc, EX, EY, work, err);
   FEM2D_CUDA(cudaGetLastError());
   ozaki_reduce_kernel<<<(a * b + 255) / 256, 256, 0, c.stream>>>(work, nrb, ny, a, b, C);
   FEM2D_CUDA(cudaGetLastError());

@@ -23,7 +23,7 @@ void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
 // a <= 256, b <= 32; FP64 emulated on the tensor cores (one exponent per row of X and per column of C,
 // normwise accuracy at FP64 rounding level). Queued on c.stream; *err as ozaki_gram.
 void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* C, int b, double alpha,
-                double beta, double* Z, int64_t ldz, int* err);
+                double beta, double* Z, int64_t ldz, int* rowexp /* n ints of scratch */, int* err);
 
 // Y = coef M X for one matrix M of a pencil (its values sliced once into digit planes), X and Y
 // row-major n x nb (nb <= 32), Y accumulated (zero it first). Built per pattern (row runs of at most
