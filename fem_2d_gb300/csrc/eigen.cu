@@ -598,23 +598,36 @@ void setup_gemm_smem(int device) {
 }
 
 // splitmix64 -> standard normal (Box-Muller), deterministic start blocks
-void random_block(int64_t n, int b, uint64_t seed, std::vector<double>& out) {
-  out.resize((size_t)n * b);
-  uint64_t s = seed * 0x9E3779B97F4A7C15ull + 0x2545F4914F6CDD1Dull;
-  auto next = [&]() {
-    s += 0x9E3779B97F4A7C15ull;
-    uint64_t z = s;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-  };
-  for (size_t k = 0; k < out.size(); k += 2) {
-    double u1 = ((next() >> 11) + 0.5) / 9007199254740992.0, u2 = ((next() >> 11) + 0.5) / 9007199254740992.0;
-    double r = std::sqrt(-2.0 * std::log(u1));
-    out[k] = r * std::cos(2.0 * M_PI * u2);
-    if (k + 1 < out.size()) out[k + 1] = r * std::sin(2.0 * M_PI * u2);
+// deterministic pseudo-random start blocks: a splitmix64 sequence turned into standard normals by
+// Box-Muller, generated on the device (element k of the row-major n x b block uses the generator's
+// calls 2 floor(k/2) + 1 and + 2, so every element is independent); written with leading dimension ld
+__global__ void random_block_kernel(int64_t n, int b, uint64_t seed, double* __restrict__ out, int64_t ld) {
+  const uint64_t s0 = seed * 0x9E3779B97F4A7C15ull + 0x2545F4914F6CDD1Dull;
+  const int64_t total = n * b;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t pair = (uint64_t)(k >> 1);
+    auto mix = [](uint64_t z) {
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      return z ^ (z >> 31);
+    };
+    const uint64_t z1 = mix(s0 + (2 * pair + 1) * 0x9E3779B97F4A7C15ull);
+    const uint64_t z2 = mix(s0 + (2 * pair + 2) * 0x9E3779B97F4A7C15ull);
+    const double u1 = ((double)(z1 >> 11) + 0.5) / 9007199254740992.0;
+    const double u2 = ((double)(z2 >> 11) + 0.5) / 9007199254740992.0;
+    const double r = sqrt(-2.0 * log(u1));
+    const double v = (k & 1) ? r * sinpi(2.0 * u2) : r * cospi(2.0 * u2);
+    out[(k / b) * ld + (k % b)] = v;
   }
 }
+
+void random_block_device(Ctx& c, int64_t n, int b, uint64_t seed, double* out, int64_t ld) {
+  const int64_t blocks = std::min<int64_t>((n * b + 255) / 256, (int64_t)c.num_sms * 16);
+  random_block_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, c.stream>>>(n, b, seed, out, ld);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
+}
+
 
 }  // namespace
 
@@ -805,13 +818,11 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   auto calibrate = [&](const MFFactor& fac, double ka, double kb, double& rel_out) -> int {
     const int nb = 4;
     const double knorm = pencil_norm(ka, kb);
-    std::vector<double> R0;
-    random_block(n, nb, 777, R0);
     DBuf<double> Rb, Xb, Tb;
     Rb.alloc_on((size_t)n * nb, c.stream);
     Xb.alloc_on((size_t)n * nb, c.stream);
     Tb.alloc_on((size_t)n * nb, c.stream);
-    FEM2D_CUDA(cudaMemcpyAsync(Rb.p, R0.data(), R0.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    random_block_device(c, n, nb, 777, Rb.p, nb);
     std::vector<double> G;
     D.gram(Rb.p, nb, nb, Rb.p, nb, nb, G);
     std::vector<double> bn(nb);
@@ -961,11 +972,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   }
   // start block: T applied to a fixed pseudo-random block
   {
-    std::vector<double> R0;
-    random_block(n, b, 12345, R0);
     DBuf<double> R;
     R.alloc_on((size_t)n * b, c.stream);
-    FEM2D_CUDA(cudaMemcpyAsync(R.p, R0.data(), R0.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    random_block_device(c, n, b, 12345, R.p, b);
     apply_T(R.p, b, X.p, 32, b);
   }
   // A pair is converged when its relative residual is below tol or its normwise backward error
