@@ -43,7 +43,7 @@ class _fem2d_solve_opts(ctypes.Structure):
                 ("tol", ctypes.c_double), ("inner_tol", ctypes.c_double), ("block", ctypes.c_int),
                 ("verbose", ctypes.c_int), ("krylov_steps", ctypes.c_int),
                 ("damping", ctypes.c_double), ("scaling", ctypes.c_int), ("dense", ctypes.c_int),
-                ("net", ctypes.c_void_p)]
+                ("net", ctypes.c_void_p), ("refine", ctypes.c_int)]
 
 
 class _fem2d_solve_stats(ctypes.Structure):
@@ -811,7 +811,7 @@ def block_gemm_device(ctx, method, n, d_x, ldx, a, d_c, b, alpha, beta, d_z, ldz
 
 def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=0, tol=0.0, max_outer=0,
                     max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0, damping=0.0, scaling=0,
-                    dense=0, net=None):
+                    dense=0, net=None, refine=0):
     """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
     the context the GEP was built on). dense=1 keeps the Gram products and block updates on the FP64 CUDA
     cores instead of the tensor-core FP64 emulation; dense=2 adds the tensor-core operator products. precond: PRECOND_EXACT (multifrontal LU, default), PRECOND_PLAIN
@@ -823,7 +823,7 @@ def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=0, tol=0.0, max_out
     vecs = np.zeros((n_pairs, n))
     res = np.zeros(n_pairs)
     o = _fem2d_solve_opts(precond, max_outer, max_inner, tol, inner_tol, block, verbose, krylov_steps, damping,
-                          scaling, dense, net._h if net is not None else None)
+                          scaling, dense, net._h if net is not None else None, refine)
     st = _fem2d_solve_stats()
     _check(lib().fem2d_gpu_solve_gep(ctx._h, gep._h, float(target_eigenvalue), int(n_pairs), ctypes.byref(o),
                                      _ptr(vals, ctypes.c_double), _ptr(vecs, ctypes.c_double),

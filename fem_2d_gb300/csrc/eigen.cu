@@ -851,6 +851,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   double rel_p = 0, rel_m = 0;
   int nref_p = iterative ? 0 : calibrate(fp, 1.0, cshift, rel_p);
   int nref_m = iterative ? 0 : calibrate(fm, 1.0, -sigma, rel_m);
+  // a caller-fixed refinement count replaces the calibrated one after the checks below
   if (!iterative && (rel_p > 1e-11 || rel_m > 1e-11) && !blocked && !plan.dense && o.scaling == 0) {
     // the Jacobi-scaled factorizations lose too many digits: scale by row-run blocks of B instead
     try {
@@ -880,6 +881,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     nref_p = calibrate(fp, 1.0, cshift, rel_p);
     nref_m = calibrate(fm, 1.0, -sigma, rel_m);
   }
+  if (o.refine > 0) nref_p = nref_m = std::min(o.refine, 3);
+  if (o.refine < 0) nref_p = nref_m = 0;
   // Out (ld lo) = T In (ld li), nb columns; In and Out may not alias W1..W3
   auto apply_T = [&](const double* In, int64_t li, double* Out, int64_t lo, int nb) {
     D.spmm(0.0, 1.0, In, li, nb, W1.p, 32);
@@ -887,7 +890,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       PCGStats s1, s2;
       pcg->cg_device(W1.p, 32, W2.p, 32, nb, inner_tol, max_inner, &s1);
       D.spmm(1.0, 0.0, W2.p, 32, nb, W3.p, 32);
-      pcg->minres_device(1.0, -sigma, W3.p, 32, Out, lo, nb, inner_tol, max_inner, &s2);
+      // the learned coarse space is trained on, and corrects, the SPD system's errors: the MINRES solves
+      // of the indefinite system keep the additive-Schwarz preconditioner alone
+      pcg->minres_device(1.0, -sigma, W3.p, 32, Out, lo, nb, inner_tol, max_inner, &s2, false);
       cg_iters += s1.iters;
       minres_iters += s2.iters;
       spmv += (int64_t)nb * (s1.iters + s2.iters);

@@ -770,12 +770,12 @@ struct PCGSolver::Impl {
   int cg_block(int nb, double tol, int max_iter, double& rel, std::vector<double>* snaps, const double* xstar,
                int nrhs, int c0, int every, int max_snaps, int first);
 
-  void precondition(const double* R, double* Zo, int nb) {
+  void precondition(const double* R, double* Zo, int nb, bool coarse = true) {
     FEM2D_CUDA(cudaMemsetAsync(Zo, 0, (size_t)n * kNB * sizeof(double), c.stream));
     const int P = pt.npatch();
     bj_apply_kernel<<<P, 256, 0, c.stream>>>(pptr.p, rdof.p, ioff.p, inv.p, R, nb, Zo);
     c.launches++;
-    if (learned) {
+    if (learned && coarse) {
       coarse_restrict_kernel<<<P, 128, 0, c.stream>>>(pptr.p, rdof.p, Zw.p, k, R, kNB, nb, ycoarse.p);
       // w = Kinv y as one FP32 tiled GEMM (m x m times m x nb)
       to_f32_kernel<<<grid_for(c, (int64_t)m * kNB), 256, 0, c.stream>>>((int64_t)m * kNB, ycoarse.p, yF.p);
@@ -1085,7 +1085,7 @@ void PCGSolver::cg_device(const double* R, int64_t ldr, double* X, int64_t ldx, 
 // Iterative Solvers", Algorithm 6.1) per column, with this solver's SPD preconditioner; the stopping
 // test is on the preconditioned residual norm |eta| <= tol gamma_1.
 void PCGSolver::minres_device(double ka, double kb, const double* R, int64_t ldr, double* X, int64_t ldx, int nb,
-                              double tol, int max_iter, PCGStats* st) {
+                              double tol, int max_iter, PCGStats* st, bool coarse) {
   Impl& I = *p_;
   Ctx& c = I.c;
   const int64_t n = I.n;
@@ -1100,7 +1100,7 @@ void PCGSolver::minres_device(double ka, double kb, const double* R, int64_t ldr
   for (double* p : {v0, v1, w0, w1, I.Xb.p}) FEM2D_CUDA(cudaMemsetAsync(p, 0, bytes, c.stream));
   strided_copy_kernel<<<grid_for(c, n * nb), 256, 0, c.stream>>>(n, nb, R, ldr, v1, kNB);   // x0 = 0: v1 = b
   c.launches++;
-  I.precondition(v1, z, nb);
+  I.precondition(v1, z, nb, coarse);
   std::vector<double> g(nb), gprev(nb, 1.0), eta(nb), eta0(nb), cc0(nb, 1.0), cc1(nb, 1.0), ss0(nb, 0.0),
       ss1(nb, 0.0);
   std::vector<char> done(nb, 0);
@@ -1138,7 +1138,7 @@ void PCGSolver::minres_device(double ka, double kb, const double* R, int64_t ldr
     I.upload_scalars(sc);
     lincomb3_kernel<<<grid_for(c, n * kNB), 256, 0, c.stream>>>(n, nb, I.scal.p, az, v1, v0, v2);
     c.launches++;
-    I.precondition(v2, z2, nb);
+    I.precondition(v2, z2, nb, coarse);
     const std::vector<double> zv = I.dots(z2, v2, nb);
     std::vector<double> a1(nb), a2(nb), a3(nb), cnew(nb), snew(nb), gnew(nb);
     for (int j = 0; j < nb; j++) {

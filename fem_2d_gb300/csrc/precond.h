@@ -74,8 +74,9 @@ class PCGSolver {
   //                 preconditioner
   void cg_device(const double* R, int64_t ldr, double* X, int64_t ldx, int nb, double tol, int max_iter,
                  PCGStats* st);
+  // (coarse = false: the additive-Schwarz part of the preconditioner only)
   void minres_device(double ka, double kb, const double* R, int64_t ldr, double* X, int64_t ldx, int nb, double tol,
-                     int max_iter, PCGStats* st);
+                     int max_iter, PCGStats* st, bool coarse = true);
   // x = K^-1 rhs (n x nrhs row-major, host) by preconditioned CG, per column to ||r|| <= tol ||b||
   void solve(int nrhs, const double* rhs, double* x, double tol, int max_iter, PCGStats* st,
              std::vector<double>* snaps = nullptr, const double* xstar = nullptr, int every = 0, int max_snaps = 0,

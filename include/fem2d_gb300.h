@@ -283,6 +283,9 @@ typedef struct fem2d_solve_opts {
                            products with A or B alone on the tensor cores (slower than the CUDA-core
                            kernel at present: Elem row runs of a few rows fill 128-row MMA tiles poorly) */
   const fem2d_patchnet* net;   /* trained patch network (precond 2), else NULL */
+  int refine;           /* FP64 iterative-refinement steps per exact shifted solve: 0 = calibrated on a random
+                           block (default; up to 3 while they reduce the residual), k > 0 = k steps
+                           (at most 3), -1 = none */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {
