@@ -20,7 +20,7 @@
 // conversions and two FMAs instead of 128 FMAs.
 //
 // A first, coalesced pass (chunk_exp_kernel) finds each column's exponent per 128-row chunk. Then one
-// CTA (4 warps, one row of C per thread) owns a 128 x 32 tile of C and a range of rows of X and Y:
+// CTA (8 warps, two threads per row of C) owns a 128 x 32 tile of C and a range of rows of X and Y:
 // per chunk, four 32-row sub-blocks are sliced into shared memory (8 digit planes per operand,
 // K-major core-matrix layout without swizzle) and thread 0 issues the 72 MMAs of the sub-block,
 // tracked by an mbarrier; the loads of a sub-block are issued before waiting on the previous
@@ -169,7 +169,12 @@ __global__ void __launch_bounds__(128) chunk_exp_kernel(int64_t n, const double*
   E[(int64_t)blockIdx.x * a + col] = e;
 }
 
-__global__ void __launch_bounds__(kThreads, 2)
+// 8 warps per CTA: thread t owns row t % 128 of the C tile (the TMEM lane) and column half t / 128
+// (16 FP64 accumulators), slices 16 of each sub-block's 32 rows of its column of X, and warps w and
+// w + 4 read the two column halves of the same TMEM lanes back
+constexpr int kGramThreads = 256;
+
+__global__ void __launch_bounds__(kGramThreads, 2)
     ozaki_gram_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ Y,
                       int64_t ldy, int b, int64_t rows_per_cta, const int* __restrict__ EX, const int* __restrict__ EY,
                       double* __restrict__ P, int* __restrict__ err) {
@@ -181,6 +186,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (kM - 1), half = tid >> 7;   // row of the C tile (TMEM lane), column half
   const int col0 = blockIdx.z * kM;    // first column of X in this tile
   const int cy0 = blockIdx.y * kN;     // first column of Y
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
@@ -204,14 +210,15 @@ __global__ void __launch_bounds__(kThreads, 2)
   uint32_t phase = 0;
   bool failed = false, pending = false;
 
-  double acc[kN];
+  constexpr int kHalf = kN / 2;
+  double acc[kHalf];
 #pragma unroll
-  for (int j = 0; j < kN; j++) acc[j] = 0.0;
+  for (int j = 0; j < kHalf; j++) acc[j] = 0.0;
 
-  const int my_col = col0 + tid;   // this thread's column of X (its row of C)
+  const int my_col = col0 + row;   // this thread's column of X (its row of C)
   const bool col_ok = my_col < a;
-  const int yj = tid % kN, ykg = tid / kN;   // this thread's column of Y and its 8-row group of a sub-block
-  const bool y_ok = cy0 + yj < b;
+  const int yj = tid % kN, ykg = tid / kN;   // threads 0..127: a column of Y and its 8-row group
+  const bool y_ok = tid < kN * (kSub / 8) && cy0 + yj < b;
   constexpr uint32_t idesc = instr_desc(kM, kN);
 
   for (int64_t c0 = r0; c0 < r1 && !failed; c0 += kChunk) {
@@ -221,17 +228,17 @@ __global__ void __launch_bounds__(kThreads, 2)
     __syncthreads();
     const int Ey = eY[yj];
     for (int sb = 0; sb < kChunk / kSub; sb++) {
-      const int64_t s0 = c0 + sb * kSub;
-      // this sub-block's values: the loads are issued before waiting on the previous sub-block's MMAs
-      double xv[kSub], yv[8];
+      const int64_t s0 = c0 + sb * kSub + half * (kSub / 2);
+      // this thread's 16 rows of the sub-block, loaded before waiting on the previous MMAs
+      double xv[kSub / 2], yv[8];
 #pragma unroll
-      for (int r = 0; r < kSub; r++) {
+      for (int r = 0; r < kSub / 2; r++) {
         const int64_t ra = s0 + r;
         xv[r] = (col_ok && ra < r1) ? __ldg(X + ra * ldx + my_col) : 0.0;
       }
 #pragma unroll
       for (int r = 0; r < 8; r++) {
-        const int64_t ra = s0 + ykg * 8 + r;
+        const int64_t ra = c0 + sb * kSub + ykg * 8 + r;
         yv[r] = (y_ok && ra < r1) ? __ldg(Y + ra * ldy + cy0 + yj) : 0.0;
       }
       if (pending) {   // the digit planes are free once the previous sub-block's MMAs have completed
@@ -242,22 +249,23 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
       if (failed) break;
 #pragma unroll
-      for (int kg = 0; kg < kSub / 8; kg++) {
+      for (int kh = 0; kh < kSub / 16; kh++) {
+        const int kg = half * (kSub / 16) + kh;
         uint32_t pk[kDigits][4];
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
           float d0[kDigits], d1[kDigits];
-          digits8(xv[kg * 8 + r8], Ex, d0);
-          digits8(xv[kg * 8 + r8 + 1], Ex, d1);
+          digits8(xv[kh * 8 + r8], Ex, d0);
+          digits8(xv[kh * 8 + r8 + 1], Ex, d1);
 #pragma unroll
           for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
         }
-        const int off = core_off(tid >> 3, kg) + (tid & 7) * 16;
+        const int off = core_off(row >> 3, kg) + (row & 7) * 16;
 #pragma unroll
         for (int s2 = 0; s2 < kDigits; s2++)
           *reinterpret_cast<uint4*>(sA + s2 * kPlaneA + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
       }
-      {
+      if (tid < kN * (kSub / 8)) {
         uint32_t pk[kDigits][4];
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
@@ -303,20 +311,21 @@ __global__ void __launch_bounds__(kThreads, 2)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
     if (failed) break;
-    // combine the eight exact digit-sum accumulators of this chunk (this thread's row, 8 columns at
-    // a time). acc_g <= (g + 1) 128 127^2 < 2^24; in int64, exactly,
+    // combine the eight exact digit-sum accumulators of this chunk (this thread's row and column half,
+    // 8 columns at a time). acc_g <= (g + 1) 128 127^2 < 2^24; in int64, exactly,
     //   T_hi = sum_{g<4} acc_g 2^(7 (3 - g)) < 2^43,   T_lo = sum_{g>=4} acc_g 2^(7 (7 - g)) < 2^47,
     // and the chunk's contribution is (T_hi + T_lo 2^-28) 2^-35 2^(Ex - 1022) 2^(Ey - 1022)
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
 #pragma unroll
-    for (int cb = 0; cb < kN; cb += 8) {
+    for (int cb = 0; cb < kHalf; cb += 8) {
+      const int jc = half * kHalf + cb;   // first column of this group in the C tile
       long long Th[8], Tl[8];
 #pragma unroll
       for (int q = 0; q < 8; q++) Th[q] = Tl[q] = 0;
 #pragma unroll
       for (int g = 0; g < kDigits; g++) {
         float v[8];
-        tmem_ld8(lane_base + (uint32_t)(g * kN + cb), v);
+        tmem_ld8(lane_base + (uint32_t)(g * kN + jc), v);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int q = 0; q < 8; q++) {
@@ -327,9 +336,8 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
 #pragma unroll
       for (int q = 0; q < 8; q++) {
-        const int j = cb + q;
         const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
-        acc[j] = fma(t, pow2(Ex + eY[j] - 2044 - 35), acc[j]);
+        acc[cb + q] = fma(t, pow2(Ex + eY[jc + q] - 2044 - 35), acc[cb + q]);
       }
     }
     // every thread's TMEM reads are complete before the next chunk's MMAs overwrite the accumulators
@@ -348,9 +356,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   // this CTA's partial tile (kM x kN, row-major)
   const int64_t tile = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-  double* out = P + tile * (kM * kN) + (int64_t)tid * kN;
+  double* out = P + tile * (kM * kN) + (int64_t)row * kN + half * kHalf;
 #pragma unroll
-  for (int j = 0; j < kN; j++) out[j] = acc[j];
+  for (int j = 0; j < kHalf; j++) out[j] = acc[j];
 }
 
 // C[i * b + j] (row-major a x b) = sum over the CTAs of row range of the partial tiles
@@ -915,7 +923,7 @@ void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
   int64_t rpc = (std::max<int64_t>(n, 1) + nrb - 1) / nrb;
   rpc = (rpc + kChunk - 1) / kChunk * kChunk;
   dim3 grid(nrb, ny, mz);
-  ozaki_gram_kernel<<<grid, kThreads, kSmemBytes, c.stream>>>(n, X, ldx, a, Y, ldy, b, rpc, EX, EY, work, err);
+  ozaki_gram_kernel<<<grid, kGramThreads, kSmemBytes, c.stream>>>(n, X, ldx, a, Y, ldy, b, rpc, EX, EY, work, err);
   FEM2D_CUDA(cudaGetLastError());
   ozaki_reduce_kernel<<<(a * b + 255) / 256, 256, 0, c.stream>>>(work, nrb, ny, a, b, C);
   FEM2D_CUDA(cudaGetLastError());

@@ -37,8 +37,10 @@ class PatchNet:
         self.k, self.hidden = k, hidden
 
     def __del__(self):
-        from . import _lib
-
+        try:
+            from . import _lib
+        except ImportError:   # interpreter shutdown: the library goes away with the process
+            return
         if getattr(self, "_h", None) and _lib is not None:
             _lib.fem2d_patchnet_free(self._h)
             self._h = None
@@ -117,8 +119,10 @@ class PCG:
         self._h = h
 
     def __del__(self):
-        from . import _lib
-
+        try:
+            from . import _lib
+        except ImportError:   # interpreter shutdown
+            return
         if getattr(self, "_h", None) and _lib is not None:
             _lib.fem2d_pcg_free(self._h)
             self._h = None
