@@ -198,12 +198,15 @@ def oracle_check(w, key, gep, res):
         # each oracle eigenvalue against the nearest GPU eigenvalue (equal counts when both found all pairs)
         rel = np.array([np.min(np.abs(gv - t)) / abs(t) for t in ov[:m]])
         out = {"oracle": "committed FP64 oracle fixture (tests/golden/full_form_%s.json): literal 2-D assembly + "
-                         "ARPACK shift-invert Lanczos with SuperLU solves" % key,
+                         "ARPACK shift-invert Lanczos with SuperLU solves; eigenvalues from the %s pencil"
+                         % (key, fx.get("eig_pencil", "HierPoly").split(" ")[0]),
                "ndofs_match": gep.dimension == fx["ndofs"], "nnz_upper_match": gep.dims()[1] == fx["nnz_upper"],
                "pattern_bit_exact": h.hexdigest() == fx["pattern_sha256"], "sample_keys_found": found,
                "sample_entries": len(key_s), "entry_err_A": ea, "entry_err_B": eb,
                "eig_rel_err_max": float(np.max(rel)), "eig_rel_err": rel.tolist(), "pairs_compared": int(m),
-               "oracle_rr_vs_mu_max_rel_diff": fx.get("rr_vs_mu_max_rel_diff")}
+               "oracle_rr_vs_mu_max_rel_diff": fx.get("rr_vs_mu_max_rel_diff"),
+               "oracle_err_bound_rel_max": (float(np.max(np.asarray(fx["rr_err_bound"]) / np.abs(np.asarray(fx["rr_eigenvalues"]))))
+                                            if fx.get("rr_err_bound") else None)}
         if "cross_check" in fx:
             out["oracle_methods_max_rel_diff"] = fx["cross_check"]["max_rel_diff"]
         return out
