@@ -293,12 +293,13 @@ def run_reference(args, ws, rank):
                 "impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True,
                 "config": dict(reference_config(w, fx["ndofs"]), nnz_upper=fx["nnz_upper"]),
-                "unavailable": "one step of the CPU restatement of the path at %d DoFs took %.0f s on %d host threads "
-                               "(literal assembly %.0f s + FP64 ARPACK/SuperLU shift-invert %.0f s); %d steps would take "
-                               "about %.0f s, beyond the %d s limit; the native line's cpu_baseline times a bounded "
-                               "sample" % (fx["ndofs"], one, fx["threads"], fx["t_oracle_assembly_s"],
-                                           fx["t_oracle_eigensolve_s"], args.steps + args.warmup,
-                                           one * (args.steps + args.warmup), args.reference_limit_s)}), flush=True)
+                "unavailable": "one step of the CPU restatement of the path at %d DoFs takes at least %.0f s on %d host "
+                               "threads (literal assembly %.0f s + FP64 ARPACK shift-invert with substructured SuperLU "
+                               "solves %.0f s on the %s pencil); %d steps would take about %.0f s, beyond the %d s limit; "
+                               "the native line's cpu_baseline times a bounded sample"
+                               % (fx["ndofs"], one, fx["threads"], fx["t_oracle_assembly_s"], fx["t_oracle_eigensolve_s"],
+                                  fx.get("eig_pencil", "HierPoly").split(" ")[0], args.steps + args.warmup,
+                                  one * (args.steps + args.warmup), args.reference_limit_s)}), flush=True)
             return
     for _ in range(args.warmup):
         cpu_port_step(w, threads)
