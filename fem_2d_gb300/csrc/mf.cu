@@ -31,6 +31,8 @@ struct FrontDesc {   // device copy of the per-front scalars
   int32_t f, p, parent;
   int32_t kid[MAXKIDS];
   int64_t off, dptr, aptr, aend, eptr;
+  int64_t prow;   // tiled fronts: offset of the front's f + 1 pull-list row pointers
+  int64_t aux;    // tiled fronts with p > kSmallP: offset of the p x p scratch copy of the LU square
 };
 
 __global__ void mf_assemble_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
@@ -729,6 +731,214 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
   }
 }
 
+// ------------------------------------------------------------------ tiled solves (partitioned inverse)
+// The narrow upper levels of the tree hold a few fronts each, some far too large for one CTA, and
+// GB300's FP64 rate per SM (under two FMA per clock) makes any solve confined to a few SMs the
+// bottleneck. After the factorization, every front of such a level is turned into its partitioned
+// inverse:
+//   diagonal square: unit lower L11^-1 and upper U11^-1      (mf_invdiag_kernel / _wide_kernel)
+//   L21 -> L21' = -L21 L11^-1,  U12 -> U12' = -U11^-1 U12    (mf_partinv_kernel)
+// so that each solve direction is one dense product with no dependency between rows:
+//   forward:  out[r] = v[r] + sum_{k < min(r, p)} F(r, k) v[k]            every row r < f
+//   backward: x[r]   = sum_{k = r}^{f - 1} F(r, k) z[k],  z = [y; x_s]    every pivot row r < p
+// (v: the gathered right-hand side in pivot order; out[0:p] = y, out[p:f] the update for the parent).
+// A level's rows are cut into tiles of kTileRows (one warp per row, lane c owns right-hand side c),
+// so a level of a few large fronts spreads over hundreds of CTAs. v is pulled without atomics from
+// the B rows and the children's update vectors through a per-front source list, chunk by chunk, into
+// shared memory by every CTA of the front.
+constexpr int kTileRows = 8;
+constexpr int kChunkK = 128;
+constexpr int kTiledMaxP = 768;   // the wide inversion keeps one column per thread in shared memory
+
+struct TiledArgs {
+  const FrontDesc* fd;
+  const int32_t* dofs;
+  const int32_t* perm;
+  const int64_t* piv_off;
+  const int64_t* woff;
+  const int64_t* prow;      // per tiled front (at FrontDesc::prow): f + 1 offsets into the sources
+  const int64_t* src_off;   // source: W[src_off + c * src_str] (a child's update row)
+  const int32_t* src_str;
+  const double* F;
+  const double* B;
+  int64_t ldb;
+  double* W;
+  double* X;
+  int64_t ldx;
+  int nb;
+};
+
+// row k (pivot order) of front d's gathered right-hand side, column c
+__device__ __forceinline__ double pull_row(const TiledArgs& a, const FrontDesc& d, const int32_t* D, const int32_t* pm,
+                                           int k, int c) {
+  const int u = k < d.p ? pm[k] : k;
+  double s = k < d.p ? a.B[(int64_t)D[u] * a.ldb + c] : 0.0;
+  const int64_t* pr = a.prow + d.prow;
+  const int64_t q1 = pr[u + 1];
+  for (int64_t q = pr[u]; q < q1; q++) s += a.W[a.src_off[q] + (int64_t)c * a.src_str[q]];
+  return s;
+}
+
+// items: (front, first row) pairs
+__global__ void __launch_bounds__(256) mf_forward_tiled_kernel(const int2* __restrict__ items, TiledArgs a) {
+  __shared__ double vs[kChunkK * 33];   // vs[kk * 33 + c]: row k0 + kk of v
+  const int2 it = items[blockIdx.x];
+  const FrontDesc d = a.fd[it.x];
+  const int f = d.f, p = d.p, nb = a.nb;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = it.y + warp;
+  const bool live = r < f && lane < nb;
+  const int32_t* D = a.dofs + d.dptr;
+  const int32_t* pm = a.perm + a.piv_off[it.x];
+  const double* Ar = a.F + d.off + r;
+  const int kend = min(p, it.y + kTileRows);   // rows r < p need k < r, rows r >= p need k < p
+  const int klim = min(r, p);
+  double acc0 = 0.0, acc1 = 0.0;
+  for (int k0 = 0; k0 < kend; k0 += kChunkK) {
+    const int kc = min(kChunkK, kend - k0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kc * nb; t += blockDim.x) {
+      const int kk = t % kc, c = t / kc;
+      vs[kk * 33 + c] = pull_row(a, d, D, pm, k0 + kk, c);
+    }
+    __syncthreads();
+    if (live) {
+      const int k1 = min(k0 + kc, klim);
+      int k = k0;
+      for (; k + 2 <= k1; k += 2) {
+        acc0 += Ar[(int64_t)k * f] * vs[(k - k0) * 33 + lane];
+        acc1 += Ar[(int64_t)(k + 1) * f] * vs[(k + 1 - k0) * 33 + lane];
+      }
+      if (k < k1) acc0 += Ar[(int64_t)k * f] * vs[(k - k0) * 33 + lane];
+    }
+  }
+  if (live) a.W[a.woff[it.x] + (int64_t)lane * f + r] = pull_row(a, d, D, pm, r, lane) + (acc0 + acc1);
+}
+
+__global__ void __launch_bounds__(256) mf_backward_tiled_kernel(const int2* __restrict__ items, TiledArgs a) {
+  __shared__ double zs[kChunkK * 33];   // zs[kk * 33 + c]: row k0 + kk of z = [y; x_s]
+  const int2 it = items[blockIdx.x];
+  const FrontDesc d = a.fd[it.x];
+  const int f = d.f, p = d.p, nb = a.nb;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = it.y + warp;
+  const bool live = r < p && lane < nb;
+  const int32_t* D = a.dofs + d.dptr;
+  const double* Ar = a.F + d.off + r;
+  const double* y = a.W + a.woff[it.x];
+  double acc0 = 0.0, acc1 = 0.0;
+  for (int k0 = it.y; k0 < f; k0 += kChunkK) {
+    const int kc = min(kChunkK, f - k0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kc * nb; t += blockDim.x) {
+      const int kk = t % kc, c = t / kc, k = k0 + kk;
+      zs[kk * 33 + c] = k < p ? y[(int64_t)c * f + k] : a.X[(int64_t)D[k] * a.ldx + c];
+    }
+    __syncthreads();
+    if (live) {
+      const int k1 = k0 + kc;
+      int k = max(k0, r);
+      for (; k + 2 <= k1; k += 2) {
+        acc0 += Ar[(int64_t)k * f] * zs[(k - k0) * 33 + lane];
+        acc1 += Ar[(int64_t)(k + 1) * f] * zs[(k + 1 - k0) * 33 + lane];
+      }
+      if (k < k1) acc0 += Ar[(int64_t)k * f] * zs[(k - k0) * 33 + lane];
+    }
+  }
+  if (live) a.X[(int64_t)D[r] * a.ldx + lane] = acc0 + acc1;
+}
+
+// the p x p LU square of each listed front, copied (column-major) to scratch at FrontDesc::aux
+__global__ void mf_square_copy_kernel(const int32_t* __restrict__ lf, const FrontDesc* __restrict__ fd,
+                                      const double* __restrict__ F, double* __restrict__ S) {
+  const FrontDesc d = fd[lf[blockIdx.y]];
+  const int64_t pp = (int64_t)d.p * d.p;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < pp; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % d.p), k = (int)(t / d.p);
+    S[d.aux + t] = F[d.off + (int64_t)k * d.f + i];
+  }
+}
+
+// columns j0 .. j0 + 31 of (L11^-1, U11^-1) of a front with p > kSmallP, one thread per column, from
+// the scratch copy of its LU square; the column being built stays in shared memory (o[i * 32])
+__global__ void __launch_bounds__(32) mf_invdiag_wide_kernel(const int2* __restrict__ items,
+                                                             const FrontDesc* __restrict__ fd,
+                                                             const double* __restrict__ S, double* __restrict__ F) {
+  extern __shared__ double ob[];
+  const int2 it = items[blockIdx.x];
+  const FrontDesc d = fd[it.x];
+  const int p = d.p, f = d.f;
+  const int lane = threadIdx.x, j = it.y + lane;
+  if (j >= p) return;
+  const double* Sp = S + d.aux;   // Sp[k * p + i] = LU(i, k)
+  double* o = ob + lane;
+  // L11 x = e_j (unit diagonal): x_i = -L(i, j) - sum_{k = j+1}^{i-1} L(i, k) x_k for i > j
+  for (int i = j + 1; i < p; i++) {
+    double a0 = -Sp[(int64_t)j * p + i], a1 = 0.0;
+    int k = j + 1;
+    for (; k + 2 <= i; k += 2) {
+      a0 -= Sp[(int64_t)k * p + i] * o[k * 32];
+      a1 -= Sp[(int64_t)(k + 1) * p + i] * o[(k + 1) * 32];
+    }
+    if (k < i) a0 -= Sp[(int64_t)k * p + i] * o[k * 32];
+    o[i * 32] = a0 + a1;
+  }
+  // U11 y = e_j: y_j = 1 / U(j, j), y_i = -(sum_{k = i+1}^{j} U(i, k) y_k) / U(i, i) for i < j
+  o[j * 32] = 1.0 / Sp[(int64_t)j * p + j];
+  for (int i = j - 1; i >= 0; i--) {
+    double a0 = 0.0, a1 = 0.0;
+    int k = i + 1;
+    for (; k + 2 <= j + 1; k += 2) {
+      a0 += Sp[(int64_t)k * p + i] * o[k * 32];
+      a1 += Sp[(int64_t)(k + 1) * p + i] * o[(k + 1) * 32];
+    }
+    if (k <= j) a0 += Sp[(int64_t)k * p + i] * o[k * 32];
+    o[i * 32] = -(a0 + a1) / Sp[(int64_t)i * p + i];
+  }
+  double* out = F + d.off + (int64_t)j * f;
+  for (int i = 0; i < p; i++) out[i] = o[i * 32];
+}
+
+// L21' = -L21 L11^-1 (kind 0: rows t0 .. t0 + 7 of L21) and U12' = -U11^-1 U12 (kind 1: columns
+// t0 .. t0 + 7 of U12), one warp per row / column, from the inverted diagonal square; items are
+// (front, kind, t0, 0). Each warp reads only the square and writes only its own row / column.
+__global__ void __launch_bounds__(256) mf_partinv_kernel(const int4* __restrict__ items,
+                                                         const FrontDesc* __restrict__ fd, double* __restrict__ F) {
+  extern __shared__ double pb[];   // kTileRows x p: the warp's original row / column
+  const int4 it = items[blockIdx.x];
+  const FrontDesc d = fd[it.x];
+  const int f = d.f, p = d.p;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = p + it.z + warp;   // row (kind 0) or column (kind 1) of the front
+  double* A = F + d.off;
+  double* b = pb + (size_t)warp * p;
+  if (q >= f) return;   // no block-wide barrier below
+  if (it.y == 0) {
+    for (int i = lane; i < p; i += 32) b[i] = A[(int64_t)i * f + q];
+    __syncwarp();
+    for (int k = 0; k < p; k++) {
+      double s = 0.0;
+      for (int i = k + 1 + lane; i < p; i += 32) s += b[i] * A[(int64_t)k * f + i];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) A[(int64_t)k * f + q] = -(b[k] + s);
+    }
+  } else {
+    for (int k = lane; k < p; k += 32) b[k] = A[(int64_t)q * f + k];
+    __syncwarp();
+    for (int i = lane; i < p; i += 32) {
+      double s0 = 0.0, s1 = 0.0;
+      int k = i;
+      for (; k + 2 <= p; k += 2) {
+        s0 += A[(int64_t)k * f + i] * b[k];
+        s1 += A[(int64_t)(k + 1) * f + i] * b[k + 1];
+      }
+      if (k < p) s0 += A[(int64_t)k * f + i] * b[k];
+      A[(int64_t)q * f + i] = -(s0 + s1);
+    }
+  }
+}
+
 // X = Kinv B for a dense inverse (n x n, row-major): one warp per row, lane c owns right-hand side c;
 // four accumulators keep the inverse-row and B-row loads in flight
 __global__ void __launch_bounds__(256) dense_inverse_apply_kernel(int64_t n, const double* __restrict__ Kinv,
@@ -895,6 +1105,91 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
     x.aend = s.asm_ptr[f + 1];
     x.eptr = s.ea_ptr[f];
   }
+  for (FrontDesc& x : fdh) x.prow = x.aux = 0;
+  // Tiled levels: the narrow upper levels (at most 2 * num_sms / CL small fronts, or any front too
+  // large for one CTA) whose fronts all have p <= kTiledMaxP. Their fronts get pull lists (for each
+  // front row, the children's update rows that add into it) and factor-time work items.
+  level_tiled.assign(nlevels, 0);
+  tf_ptr.assign(nlevels + 1, 0);
+  tb_ptr.assign(nlevels + 1, 0);
+  std::vector<int32_t> tf_h, tb_h, mid_h, wide_h, wi_h, pi_h, sstr_h;
+  std::vector<int64_t> prow_h, soff_h;
+  nmid = nwide = npinv = 0;
+  max_mid_p = max_wide_p = max_tiled_p = 0;
+  int64_t sq_total = 0;
+  const bool single_dense = nf == 1 && max_p == max_f && max_f <= 4096;   // factor() inverts it whole
+  for (int l = 0; l < nlevels; l++) {
+    tf_ptr[l] = (int32_t)(tf_h.size() / 2);
+    tb_ptr[l] = (int32_t)(tb_h.size() / 2);
+    int ns = 0, nl = 0;
+    bool fits = true;
+    for (int k = s.level_ptr[l]; k < s.level_ptr[l + 1]; k++) {
+      const int fr = s.level_fronts[k];
+      if (s.p[fr] <= kSmallP && s.f[fr] <= kSmallF) ns++;
+      else nl++;
+      if (s.p[fr] > kTiledMaxP) fits = false;
+    }
+    if (single_dense || !fits || !(nl > 0 || ns * CL <= 2 * c.num_sms)) continue;
+    level_tiled[l] = 1;
+    for (int k = s.level_ptr[l]; k < s.level_ptr[l + 1]; k++) {
+      const int fr = s.level_fronts[k];
+      const int F = s.f[fr], P = s.p[fr];
+      max_tiled_p = std::max(max_tiled_p, P);
+      for (int r0 = 0; r0 < F; r0 += kTileRows) tf_h.insert(tf_h.end(), {fr, r0});
+      for (int r0 = 0; r0 < P; r0 += kTileRows) tb_h.insert(tb_h.end(), {fr, r0});
+      const bool small = P <= kSmallP && F <= kSmallF;
+      if (!small && P > 0 && P <= kSmallP) {
+        mid_h.push_back(fr);
+        max_mid_p = std::max(max_mid_p, P);
+      }
+      if (P > kSmallP) {
+        wide_h.push_back(fr);
+        fdh[fr].aux = sq_total;
+        sq_total += (int64_t)P * P;
+        max_wide_p = std::max(max_wide_p, P);
+        for (int j0 = 0; j0 < P; j0 += 32) wi_h.insert(wi_h.end(), {fr, j0});
+      }
+      if (P > 0)
+        for (int t0 = 0; t0 < F - P; t0 += kTileRows) pi_h.insert(pi_h.end(), {fr, 0, t0, 0, fr, 1, t0, 0});
+      // pull lists: row u of the front (before pivoting) receives row i of child ch's update block
+      std::vector<std::vector<std::pair<int64_t, int32_t>>> rows(F);
+      for (int slot = 0; slot < MAXKIDS; slot++) {
+        const int ch = kids[fr][slot];
+        if (ch < 0) continue;
+        const int sc = s.f[ch] - s.p[ch];
+        for (int i = 0; i < sc; i++) {
+          const int u = s.ea_map[s.ea_ptr[ch] + i];
+          if (u < 0 || u >= F) fail(FEM2D_E_INVALID_ARG, "extend-add map outside the parent front");
+          rows[u].push_back({woff_h[ch] + s.p[ch] + i, s.f[ch]});
+        }
+      }
+      fdh[fr].prow = (int64_t)prow_h.size();
+      for (int u = 0; u < F; u++) {
+        prow_h.push_back((int64_t)soff_h.size());
+        for (const auto& e : rows[u]) {
+          soff_h.push_back(e.first);
+          sstr_h.push_back(e.second);
+        }
+      }
+      prow_h.push_back((int64_t)soff_h.size());
+    }
+  }
+  tf_ptr[nlevels] = (int32_t)(tf_h.size() / 2);
+  tb_ptr[nlevels] = (int32_t)(tb_h.size() / 2);
+  nmid = (int)mid_h.size();
+  nwide = (int)wide_h.size();
+  nwide_items = (int)(wi_h.size() / 2);
+  npinv = (int)(pi_h.size() / 4);
+  tf_items.upload(tf_h, st);
+  tb_items.upload(tb_h, st);
+  prow.upload(prow_h, st);
+  src_off.upload(soff_h, st);
+  src_str.upload(sstr_h, st);
+  lmid.upload(mid_h, st);
+  lwide.upload(wide_h, st);
+  wide_items.upload(wi_h, st);
+  pinv_items.upload(pi_h, st);
+  sq.alloc(std::max<int64_t>(sq_total, 1));
   std::vector<uint8_t> raw(fdh.size() * sizeof(FrontDesc));
   std::memcpy(raw.data(), fdh.data(), raw.size());
   desc.upload(raw, st);
@@ -965,6 +1260,10 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
                                     (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
     FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmallF * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_invdiag_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTiledMaxP * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_partinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTileRows * kTiledMaxP * (int)sizeof(double)));
     attr_done[c.device] = true;
   }
 }
@@ -1043,6 +1342,22 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
                                                                                               Fbuf.p);
     c.launches++;
   }
+  // the tiled levels' fronts: inverted diagonal squares, then L21' = -L21 L11^-1 and U12' = -U11^-1 U12
+  if (nmid > 0) {
+    mf_invdiag_kernel<<<nmid, 256, (size_t)max_mid_p * max_mid_p * sizeof(double), st>>>(lmid.p, fd, Fbuf.p);
+    c.launches++;
+  }
+  if (nwide > 0) {
+    mf_square_copy_kernel<<<dim3(64, nwide), 256, 0, st>>>(lwide.p, fd, Fbuf.p, sq.p);
+    mf_invdiag_wide_kernel<<<nwide_items, 32, (size_t)max_wide_p * 32 * sizeof(double), st>>>(
+        reinterpret_cast<const int2*>(wide_items.p), fd, sq.p, Fbuf.p);
+    c.launches += 2;
+  }
+  if (npinv > 0) {
+    mf_partinv_kernel<<<npinv, 256, (size_t)kTileRows * max_tiled_p * sizeof(double), st>>>(
+        reinterpret_cast<const int4*>(pinv_items.p), fd, Fbuf.p);
+    c.launches++;
+  }
 
   FEM2D_CUDA(cudaGetLastError());
   out.flags = read_flags(c);
@@ -1078,7 +1393,19 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
   // the whole solve is one profiled region: per-level events would dominate the short level launches
   ProfScope ps(c, "mf_solve", 2.0 * fbytes, 2.0 * 2.0 * (fbytes / 8.0) * nb);
   SolveArgs a{fd, dofs.p, ea_map.p, fac.perm.p, fac.iperm.p, piv_off.p, woff.p, Fbuf.p, B, ldb, work.p, X, ldx, nb};
+  TiledArgs ta{fd,     dofs.p, fac.perm.p, piv_off.p, woff.p, prow.p, src_off.p, src_str.p,
+               Fbuf.p, B,      ldb,        work.p,    X,      ldx,    nb};
+  const int2* tfi = reinterpret_cast<const int2*>(tf_items.p);
+  const int2* tbi = reinterpret_cast<const int2*>(tb_items.p);
   for (int l = 0; l < nlevels; l++) {
+    if (level_tiled[l]) {
+      const int ni = tf_ptr[l + 1] - tf_ptr[l];
+      if (ni > 0) {
+        mf_forward_tiled_kernel<<<ni, 256, 0, st>>>(tfi + tf_ptr[l], ta);
+        c.launches++;
+      }
+      continue;
+    }
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)(level_small_f[l] + level_small_p[l]) * nb * sizeof(double);
@@ -1098,6 +1425,14 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     }
   }
   for (int l = nlevels - 1; l >= 0; l--) {
+    if (level_tiled[l]) {
+      const int ni = tb_ptr[l + 1] - tb_ptr[l];
+      if (ni > 0) {
+        mf_backward_tiled_kernel<<<ni, 256, 0, st>>>(tbi + tb_ptr[l], ta);
+        c.launches++;
+      }
+      continue;
+    }
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)level_small_f[l] * nb * sizeof(double);

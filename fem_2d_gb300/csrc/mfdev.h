@@ -43,6 +43,18 @@ struct MFDevice {
   std::vector<int32_t> level_small_f, level_small_p;
   DBuf<int32_t> lsmall, llarge;
   int nsmall = 0, max_small_p = 0;
+  // tiled levels (narrow upper levels solved through the fronts' partitioned inverses, rows spread over
+  // many CTAs): per level a flag and offsets into the (front, first row) items of each direction
+  std::vector<uint8_t> level_tiled;
+  std::vector<int32_t> tf_ptr, tb_ptr;
+  DBuf<int32_t> tf_items, tb_items;
+  DBuf<int64_t> prow, src_off;   // pull lists of the tiled fronts' right-hand sides
+  DBuf<int32_t> src_str;
+  // factor-time work of the tiled fronts: diagonal inversion of those outside lsmall (p <= kSmallP:
+  // lmid; larger: lwide, 32-column items, scratch squares sq), then the partitioned-inverse items
+  DBuf<int32_t> lmid, lwide, wide_items, pinv_items;
+  DBuf<double> sq;
+  int nmid = 0, max_mid_p = 0, nwide = 0, nwide_items = 0, max_wide_p = 0, npinv = 0, max_tiled_p = 0;
 
   void setup(Ctx& c, const MFSymbolic& s, int nb_max);
   // factor c_a*A + c_b*B (values in full-CSR order); Cholesky mode skips pivoting (SPD shifts)

@@ -43,3 +43,23 @@ def test_shifted_solve_residual(kat, ctx, name, ca, cb, spd):
     Xs = sla.splu(K.tocsc()).solve(R)
     rels = np.linalg.norm(K @ Xs - R, axis=0) / np.linalg.norm(R, axis=0)
     assert np.max(rel) <= max(1e-9, 100 * np.max(rels)), (rel, rels)
+
+
+@pytest.mark.parametrize("ca,cb,spd", [(1.0, -10.0, False), (1.0, 10.0, True)])
+def test_shifted_solve_wide_fronts(ctx, ca, cb, spd):
+    """A 389,566-DoF full-form mesh whose top separator fronts have p > 160: the narrow upper levels are
+    solved through the fronts' partitioned inverses (the wide ones inverted column-parallel); the
+    normwise backward error ||K X - R|| / (||K|| ||X|| + ||R||) stays at the FP64 level."""
+    w = configs.full_scale(seed=0, basis=0, nx=64, ny=32, rounds=1, fraction=0.44)
+    dom = fg.Domain.from_mesh(configs.build_mesh(w))
+    fronts = fg.factor_plan(dom)["fronts"]
+    assert np.max(fronts[:, 3]) > 160   # the case the wide inversion covers
+    gep = fg.galerkin_sample_gep_hcurl(fg.HierPoly, fg.CurlCurl, fg.L2Inner, dom, list(w.glq), ctx=ctx)
+    A, B = gep.scipy()
+    K = (ca * A + cb * B).tocsr()
+    R = np.random.default_rng(1).standard_normal((gep.dimension, 4))
+    X = gep.shifted_solve(ca, cb, R, spd=spd)
+    knorm = np.max(np.asarray(abs(K).sum(axis=1)).ravel())
+    bwd = np.max(np.abs(K @ X - R), axis=0) / (knorm * np.max(np.abs(X), axis=0) + np.max(np.abs(R), axis=0))
+    assert np.all(np.isfinite(X))
+    assert np.max(bwd) < 1e-13, bwd
