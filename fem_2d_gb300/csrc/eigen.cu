@@ -444,18 +444,16 @@ struct Dev {
 
   void spmm(double ca, double cb, const double* X, int64_t ldx, int nb, double* Y, int64_t ldy) {
     const double nv = (ca != 0.0) + (cb != 0.0);
-    if (tcs && nb <= 32 && nv == 1.0) {
+    double coef = 1.0;
+    const int slot = (tcs && nb <= 32 && nv > 0.0) ? tcs->find(ca, cb, &coef) : -1;
+    if (slot >= 0) {
       ProfScope ps(c, "spmm_tc", (double)tcs->plane_units * 16.0 + 4.0 * h.nnz_full + 16.0 * h.n * nb,
                    2.0 * (double)h.nnz_full * nb);
-      const int64_t zb = std::min<int64_t>((h.n * nb + 255) / 256, (int64_t)c.num_sms * 8);
-      zero_block_kernel<<<(int)std::max<int64_t>(zb, 1), 256, 0, c.stream>>>(h.n, nb, Y, ldy);
-      c.launches++;
       if (ozerr.n == 0) {
         ozerr.alloc_on(1, c.stream);
         FEM2D_CUDA(cudaMemsetAsync(ozerr.p, 0, sizeof(int), c.stream));
       }
-      tcs->apply(c, ca != 0.0 ? 0 : 1, ca != 0.0 ? ca : cb, d.grp.p, d.row_ptr.p, d.col.p, X, ldx, nb, Y, ldy,
-                 ozerr.p);
+      tcs->apply(c, slot, coef, d.grp.p, d.row_ptr.p, d.col.p, X, ldx, nb, Y, ldy, ozerr.p);
       return;
     }
     ProfScope ps(c, "spmm", (double)h.nnz_full * (4.0 + 8.0 * nv) + 8.0 * (h.n + 1) + 16.0 * h.n * nb,
@@ -769,7 +767,7 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   double inner_worst = 0.0;
 
   Dev D{c, h, d, sa.p, sb.p};
-  D.dense_mode = o.dense == 1 ? 1 : 0;
+  D.dense_mode = o.dense == 1 ? 1 : 0;   // 3: tensor Gram products and block updates, FP64 operator products
   DBuf<double> V, AV, BV, X, AX, BX, G0, W1, W2, W3;
   V.alloc_on((size_t)n * mmax, c.stream);
   AV.alloc_on((size_t)n * mmax, c.stream);
@@ -966,13 +964,18 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
 
   const double norm_a = pencil_norm(1.0, 0.0), norm_b = pencil_norm(0.0, 1.0);
   // products with A or B alone (the T applications, the basis products) on the tensor cores from here
-  // on: the scaled pencil is final, so its values are sliced once
+  // on: the scaled pencil is final, so its values are sliced once (by default from kTensorSpmmNnz
+  // nonzeros, where the slicing is amortised; always with dense = 2)
+  constexpr int64_t kTensorSpmmNnz = 1000000;
   TcSpmm tcs;
-  if (o.dense == 2 && d.nwork > 0) {
-    ProfScope ps(c, "spmm_slice", 16.0 * h.nnz_full, 0.0);
+  if (d.nwork > 0 && (o.dense == 2 || (o.dense == 0 && h.nnz_full >= kTensorSpmmNnz))) {
+    ProfScope ps(c, "spmm_slice", 2.0 * (8.0 * h.nnz_full + 16.0 * h.nnz_full), 0.0);
     tcs.build(c, n, row_runs(h), h.row_ptr);
-    tcs.slice(c, d.grp.p, d.row_ptr.p, sa.p, 0);
-    tcs.slice(c, d.grp.p, d.row_ptr.p, sb.p, 1);
+    tcs.slice(c, 0, d.grp.p, d.row_ptr.p, sa.p, nullptr, 1.0, 0.0);
+    tcs.slice(c, 1, d.grp.p, d.row_ptr.p, nullptr, sb.p, 0.0, 1.0);
+    // the shifted matrices of the refinement residuals (exact solves with refinement steps)
+    if (!iterative && nref_p > 0) tcs.slice(c, 2, d.grp.p, d.row_ptr.p, sa.p, sb.p, 1.0, cshift);
+    if (!iterative && nref_m > 0) tcs.slice(c, 3, d.grp.p, d.row_ptr.p, sa.p, sb.p, 1.0, -sigma);
     D.tcs = &tcs;
   }
   // start block: T applied to a fixed pseudo-random block
@@ -1535,7 +1538,8 @@ void gep_spmm_tensor(Ctx& c, const HostGEP& h, const DeviceGEP& d, int which, do
   if (nb < 1 || nb > 32) fail(FEM2D_E_INVALID_ARG, "1..32 columns");
   TcSpmm tcs;
   tcs.build(c, h.n, row_runs(h), h.row_ptr);
-  tcs.slice(c, d.grp.p, d.row_ptr.p, which == 0 ? d.a.p : d.b.p, which);
+  tcs.slice(c, 0, d.grp.p, d.row_ptr.p, which == 0 ? d.a.p : nullptr, which == 1 ? d.b.p : nullptr,
+            which == 0 ? 1.0 : 0.0, which == 1 ? 1.0 : 0.0);
   Dev D{c, h, d, d.a.p, d.b.p};
   D.tcs = &tcs;
   D.spmm(which == 0 ? coef : 0.0, which == 1 ? coef : 0.0, X, ldx, nb, Y, ldy);

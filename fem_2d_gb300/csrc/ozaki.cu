@@ -580,23 +580,73 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Operator products Y = coef M X for one matrix M (A or B) of the pencil, nb <= 32 columns.
-// Rows of one Elem's interior functions share a column list (a run, at most 64 rows); a chunk item is
-// (run, 128 consecutive columns of that list). M's values are sliced once per solve (spmm_slice_kernel)
-// into digit planes per (item, 32-column sub-block) in the core-matrix layout the MMA reads, with one
-// exponent per (item, row). The product (spmm_tc_kernel) gathers the item's 128 rows of X, slices them
-// with one exponent per column, runs the 36 digit-pair MMAs per sub-block (M = 128 with the run's rows
-// first; rows past the run are never read back) and adds the exactly recombined chunk into Y.
-constexpr int kPlaneB128 = kN * kChunk * 2;          // one digit plane of the gathered X (32 x 128 bf16)
-constexpr int kSpmmSmem = kDigits * kPlaneA + kDigits * kPlaneB128 + 1024;
+// Operator products Y = coef M X for one matrix M (A or B) of the pencil, nb <= 32 columns of X.
+//
+// Rows of one Elem's interior functions share a column list (a run of R <= 64 rows); an item is one
+// run and 64 consecutive columns of its list. M's values are sliced once per solve (spmm_slice_kernel)
+// into the eight 7-bit digit planes of digits8 (one exponent per item row), in the K-major
+// core-matrix layout the MMA reads. The product kernel gathers the item's 64 rows of X and slices them
+// the same way (one exponent per column) into a sequence of digit planes of X, 16 or 32 rows (one per
+// column) each, preceded by zero planes. The MMA's 128 rows are (digit-sum group g, column of X) and
+// its N the run's rows: for the accumulator of group g, the MMA with digit plane t of M reads the
+// window of X planes that starts at digit g - t, so each accumulator sums exactly the pairs (s, t) with
+// s + t = g -- at most 8 pairs x 64 columns x 127^2 < 2^24, exact in FP32 -- and each TMEM lane holds
+// one or two such sums per run row. With nb <= 16 the eight groups x 16 columns fill one 128-row
+// operand (8 MMAs per plane step); with nb <= 32, groups 0..3 and 4..7 x 32 columns fill two (4 and 8
+// MMAs). Sums are combined exactly in int64 across lanes and warps (fixed order), converted once per
+// item and output to FP64 and summed per run in registers; every run is owned by one CTA, which writes
+// its rows of Y once (no atomics, no zero fill, deterministic). Pairs with s + t >= 8 are dropped: below
+// 2^-52 of max|m| max|x| of the item per term, FP64 rounding level in the normwise sense.
+//
+// Pipeline per CTA (one per SM): two shared-memory stages; while the MMAs of item k run, thread 0 has
+// the next item's digit planes of M brought in by one bulk asynchronous copy and all threads gather and
+// slice the next item's rows of X into the other stage. Every mbarrier wait is bounded (one second): on
+// expiry the kernel raises the error flag, lets its copies and MMAs in flight finish (bounded), frees
+// its TMEM and returns.
+constexpr int kSpK = 64;                                // columns of a run's list per item
+constexpr int kSpThreads = 256;
+constexpr int kSpXPlaneW = 32 * kSpK * 2;               // a digit plane of X, 32 columns (4 KB)
+constexpr int kSpXPlaneP = 16 * kSpK * 2;               // 16 columns (2 KB)
+constexpr int kSpXBytes = 11 * kSpXPlaneW;              // 3 zero + 8 digit planes (wide); 7 + 8 (packed)
+constexpr int kSpMBytes = 2 * kDigits * 64 * 64 + 2048; // planes of a 64-row item + row-block overrun
+constexpr int kSpSmem = kSpXBytes + kSpMBytes + 1536;   // one stage; two CTAs per SM
+constexpr uint32_t kSpTmemCols = 128;
 
-__global__ void __launch_bounds__(kThreads) spmm_slice_kernel(int nitems, const int4* __restrict__ items,
-                                                               const int32_t* __restrict__ grp,
-                                                               const int64_t* __restrict__ rp,
-                                                               const int64_t* __restrict__ poff,
-                                                               const int64_t* __restrict__ eoff,
-                                                               const double* __restrict__ v, uint4* __restrict__ planes,
-                                                               int* __restrict__ ex) {
+// uint4 units of one item's digit planes: 2 sub-blocks of 32 K x 8 planes x R8 rows x 4 k-groups
+__host__ __device__ constexpr int sp_item_units(int r8) { return 2 * kDigits * r8 * 4; }
+
+// digits8 with integer digit extraction on 32-bit halves and a float conversion by the 2^23 offset
+// (no integer-to-float conversions); the same eight values as digits8
+__device__ __forceinline__ void digits8_fast(double v, int E, float (&d)[kDigits]) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  const int shift = E - ex;
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const unsigned long long A = (ex == 0 || shift > 55) ? 0ull : ((mant << 3) >> shift);
+  const uint32_t hi = (uint32_t)(A >> 32), lo = (uint32_t)A;
+  const float sg = (bits >> 63) ? -1.0f : 1.0f, off = -8388608.0f * sg;
+  const uint32_t dg[kDigits] = {(hi >> 17) & 0x7Fu, (hi >> 10) & 0x7Fu, (hi >> 3) & 0x7Fu,
+                                __funnelshift_r(lo, hi, 28) & 0x7Fu, (lo >> 21) & 0x7Fu, (lo >> 14) & 0x7Fu,
+                                (lo >> 7) & 0x7Fu, lo & 0x7Fu};
+#pragma unroll
+  for (int s = 0; s < kDigits; s++) d[s] = fmaf(__uint_as_float(0x4B000000u | dg[s]), sg, off);
+}
+
+__global__ void __launch_bounds__(256) spmm_slice_kernel(int nitems, const int4* __restrict__ items,
+                                                          const int32_t* __restrict__ grp,
+                                                          const int64_t* __restrict__ rp,
+                                                          const int64_t* __restrict__ poff,
+                                                          const int64_t* __restrict__ eoff,
+                                                          const double* __restrict__ va, const double* __restrict__ vb,
+                                                          double ca, double cb, uint4* __restrict__ planes,
+                                                          int* __restrict__ ex) {
+  // the sliced matrix's value at CSR position k: ca A + cb B, rounded as the FP64 product kernels do
+  auto val = [&](int64_t k) {
+    double x = 0.0;
+    if (ca != 0.0) x += ca * va[k];
+    if (cb != 0.0) x += cb * vb[k];
+    return x;
+  };
   __shared__ int erow[64];
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int4 w = items[it];   // x: run, y: first column, z: rows R, w: columns Lc
@@ -604,33 +654,32 @@ __global__ void __launch_bounds__(kThreads) spmm_slice_kernel(int nitems, const 
     __syncthreads();
     if (threadIdx.x < 64) erow[threadIdx.x] = 0;
     __syncthreads();
-    for (int t = threadIdx.x; t < R * 16; t += blockDim.x) {   // row r, 8-column group
-      const int r = t / 16, q8 = (t % 16) * 8;
-      const double* vr = v + rp[r0 + r] + w.y;
+    for (int t = threadIdx.x; t < R * 4; t += blockDim.x) {   // row r, 16-column quarter
+      const int r = t >> 2, q0 = (t & 3) * 16;
+      const int64_t k0 = rp[r0 + r] + w.y;
       int e = 0;
-      for (int q = q8; q < min(q8 + 8, Lc); q++) e = max(e, biased_exp(vr[q]));
+      for (int q = q0; q < min(q0 + 16, Lc); q++) e = max(e, biased_exp(val(k0 + q)));
       atomicMax(&erow[r], e);
     }
     __syncthreads();
     if (threadIdx.x < R) ex[eoff[it] + threadIdx.x] = erow[threadIdx.x];
-    // digit planes: sub-block s (32 columns), plane t, core (rg, kg): 16 bytes per (row, k group)
+    // sub-block sb (32 columns), plane t, core matrix (r / 8, kg): 16 bytes at row r % 8
     uint4* pl = planes + poff[it];
-    const int per_sub = kDigits * R8 * 4;   // uint4 units per sub-block (R8 rows x 4 k groups per plane)
-    for (int t = threadIdx.x; t < R8 * 16; t += blockDim.x) {
-      const int r = t / 16, kg16 = t % 16, sb = kg16 / 4, kg = kg16 % 4;
-      uint32_t pk[kDigits][4];
-      const double* vr = r < R ? v + rp[r0 + r] + w.y : nullptr;
+    const int per_sub = kDigits * R8 * 4;
+    for (int t = threadIdx.x; t < R8 * 8; t += blockDim.x) {
+      const int r = t >> 3, kg8 = t & 7, sb = kg8 >> 2, kg = kg8 & 3;
+      const int64_t k0 = r < R ? rp[r0 + r] + w.y : -1;
       const int E = r < R ? erow[r] : 0;
+      uint32_t pk[kDigits][4];
 #pragma unroll
       for (int r8 = 0; r8 < 8; r8 += 2) {
-        const int q = sb * 32 + kg * 8 + r8;
+        const int q = kg8 * 8 + r8;
         float d0[kDigits], d1[kDigits];
-        digits8((vr && q < Lc) ? vr[q] : 0.0, E, d0);
-        digits8((vr && q + 1 < Lc) ? vr[q + 1] : 0.0, E, d1);
+        digits8((k0 >= 0 && q < Lc) ? val(k0 + q) : 0.0, E, d0);
+        digits8((k0 >= 0 && q + 1 < Lc) ? val(k0 + q + 1) : 0.0, E, d1);
 #pragma unroll
         for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
       }
-      // core matrix (r / 8, kg) of plane s2: 16 bytes at row r % 8
       const int64_t cm = (int64_t)((r >> 3) * 4 + kg) * 8 + (r & 7);   // uint4 index within a plane
 #pragma unroll
       for (int s2 = 0; s2 < kDigits; s2++)
@@ -639,157 +688,312 @@ __global__ void __launch_bounds__(kThreads) spmm_slice_kernel(int nitems, const 
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
-    spmm_tc_kernel(int nitems, const int4* __restrict__ items, const int32_t* __restrict__ grp,
-                   const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const int64_t* __restrict__ poff,
-                   const int64_t* __restrict__ eoff, const uint4* __restrict__ planes, const int* __restrict__ ex,
-                   double coef, const double* __restrict__ X, int64_t ldx, int nb, double* __restrict__ Y, int64_t ldy,
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+// gather the item's 64 rows of X (their indices in cq, -1 past the item's columns), find each column's
+// exponent (ecol: zeroed by the caller) and write the digit planes of X into xs (after its zero planes)
+__device__ __forceinline__ void sp_stage_x(const int* cq, const double* __restrict__ X, int64_t ldx, int nb,
+                                           bool packed, uint8_t* xs, int* ecol) {
+  const int tid = threadIdx.x;
+  if (!packed) {
+    // thread: column j, rows q = 8 part .. 8 part + 7 (one core-matrix row of 8 K values per digit)
+    const int j = tid & 31, part = tid >> 5;
+    double xv[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const int c = cq[part * 8 + r];
+      xv[r] = (j < nb && c >= 0) ? __ldg(X + (int64_t)c * ldx + j) : 0.0;
+    }
+    int e = 0;
+#pragma unroll
+    for (int r = 0; r < 8; r++) e = max(e, biased_exp(xv[r]));
+    if (j < nb) atomicMax(&ecol[j], e);
+    __syncthreads();
+    const int E = ecol[j];
+    uint32_t pk[kDigits][4];
+#pragma unroll
+    for (int r = 0; r < 8; r += 2) {
+      float d0[kDigits], d1[kDigits];
+      digits8_fast(xv[r], E, d0);
+      digits8_fast(xv[r + 1], E, d1);
+#pragma unroll
+      for (int s = 0; s < kDigits; s++) pk[s][r >> 1] = pack_bf16(d0[s], d1[s]);
+    }
+    // digit s: plane 3 + s, row j
+#pragma unroll
+    for (int s = 0; s < kDigits; s++)
+      *reinterpret_cast<uint4*>(xs + (3 + s) * kSpXPlaneW + (j >> 3) * 1024 + part * 128 + (j & 7) * 16) =
+          make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+  } else {
+    // thread: column j < 16, rows q = 4 part .. 4 part + 3 (half a core-matrix row per digit)
+    const int j = tid & 15, part = tid >> 4;
+    double xv[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int c = cq[part * 4 + r];
+      xv[r] = (j < nb && c >= 0) ? __ldg(X + (int64_t)c * ldx + j) : 0.0;
+    }
+    int e = 0;
+#pragma unroll
+    for (int r = 0; r < 4; r++) e = max(e, biased_exp(xv[r]));
+    if (j < nb) atomicMax(&ecol[j], e);
+    __syncthreads();
+    const int E = ecol[j];
+    uint32_t pk[kDigits][2];
+#pragma unroll
+    for (int r = 0; r < 4; r += 2) {
+      float d0[kDigits], d1[kDigits];
+      digits8_fast(xv[r], E, d0);
+      digits8_fast(xv[r + 1], E, d1);
+#pragma unroll
+      for (int s = 0; s < kDigits; s++) pk[s][r >> 1] = pack_bf16(d0[s], d1[s]);
+    }
+    // digit s: plane 7 + s, row j
+#pragma unroll
+    for (int s = 0; s < kDigits; s++)
+      *reinterpret_cast<uint2*>(xs + (7 + s) * kSpXPlaneP + (j >> 3) * 1024 + (part >> 1) * 128 + (j & 7) * 16 +
+                                (part & 1) * 8) = make_uint2(pk[s][0], pk[s][1]);
+  }
+}
+
+__global__ void __launch_bounds__(kSpThreads, 2)
+    spmm_tc_kernel(const TcSpmmItem* __restrict__ items, const int32_t* __restrict__ cta_ptr,
+                   const int2* __restrict__ zruns, int nzero, const int32_t* __restrict__ col,
+                   const uint4* __restrict__ planes, const int* __restrict__ ex, double coef,
+                   const double* __restrict__ X, int64_t ldx, int nb, double* __restrict__ Y, int64_t ldy,
                    int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA = smem;                               // kDigits planes of kM x kSub (the item's sub-block of M)
-  uint8_t* sB = smem + kDigits * kPlaneA;           // kDigits planes of kN x kChunk (gathered X)
-  int* eY = reinterpret_cast<int*>(sB + kDigits * kPlaneB128);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(eY + kN);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  uint8_t* xs = smem;                          // zero planes + digit planes of X
+  uint8_t* ms = smem + kSpXBytes;              // digit planes of M; the readout's partial sums afterwards
+  int* ecol = reinterpret_cast<int*>(ms + kSpMBytes);   // [2][32] column exponents of X (by item parity)
+  int* em = ecol + 64;                                   // [2][64] row exponents of M
+  int* cq = em + 128;                                    // [2][64] the items' column indices (-1 past Lc)
+  uint64_t* bar_full = reinterpret_cast<uint64_t*>(cq + 128);   // M planes arrived
+  uint64_t* bar_mma = bar_full + 1;                              // MMAs committed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_mma + 1);
+  int* sfail = reinterpret_cast<int*>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool packed = nb <= 16;
+
+  // runs without columns: their rows of Y are zero
+  for (int z = blockIdx.x; z < nzero; z += gridDim.x) {
+    const int2 zr = zruns[z];
+    for (int t = tid; t < zr.y * nb; t += kSpThreads) Y[(int64_t)(zr.x + t / nb) * ldy + t % nb] = 0.0;
+  }
+  // the buffers start zeroed: the zero planes of X stay so, and the MMAs read whole 8-row groups past
+  // short runs
+  for (int t = tid; t < (kSpXBytes + kSpMBytes) / 16; t += kSpThreads)
+    reinterpret_cast<uint4*>(smem)[t] = make_uint4(0, 0, 0, 0);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
-                 "r"(kTmemCols)
+                 "r"(kSpTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar_full)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar_mma)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *sfail = 0;
   }
+  const int i0 = cta_ptr[blockIdx.x], i1 = cta_ptr[blockIdx.x + 1];
+  if (i0 < i1 && tid < 64) {   // the first item's exponent slots and column indices
+    const TcSpmmItem f = items[i0];
+    em[tid] = tid < f.R ? ex[f.eoff + tid] : 0;
+    cq[tid] = tid < f.Lc ? __ldg(col + f.cbase + tid) : -1;
+    if (tid < 32) ecol[tid] = 0;
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t mb = smem_addr(mbar);
-  uint32_t phase = 0;
-  bool failed = false;
-  constexpr uint32_t idesc = instr_desc(kM, kN);
-  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t mbf = smem_addr(bar_full), mbm = smem_addr(bar_mma);
+  const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  // descriptors of the X planes and of the M planes (address offsets are added in 16-byte units)
+  const uint64_t dX = smem_desc(smem_addr(xs), 128, 1024);
+  const uint64_t dM = smem_desc(smem_addr(ms), 128, 512);
+  uint32_t ph_full = 0u, ph_mma = 0u;
+  bool copy_out = false, failed = false;
+  double acc[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) acc[o] = 0.0;
 
-  for (int it = blockIdx.x; it < nitems && !failed; it += gridDim.x) {
-    const int4 w = items[it];
-    const int r0 = grp[w.x], R = w.z, R8 = (R + 7) & ~7, Lc = w.w;
-    const int32_t* cols = col + rp[r0] + w.y;
-    // gathered X rows: column exponents (4 threads per column, 32 rows each), then digit planes
-    if (tid < kN) eY[tid] = 0;
-    __syncthreads();
-    {
-      const int j = tid % kN, part = tid / kN;
-      int e = 0;
-      if (j < nb) {
-        const int q1 = min(Lc, part * 32 + 32);
-        for (int q = part * 32; q < q1; q++) e = max(e, biased_exp(__ldg(X + (int64_t)__ldg(cols + q) * ldx + j)));
-      }
-      atomicMax(&eY[j], e);
+  for (int idx = i0, k = 0; idx < i1; idx++, k++) {
+    const TcSpmmItem w = items[idx];
+    const bool more = idx + 1 < i1;
+    const int R = w.R, R8 = (R + 7) & ~7, nrb = (R + 31) >> 5;
+    int* ecs = ecol + 32 * (k & 1);
+    int* ems = em + 64 * (k & 1);
+    // the item's digit planes of M (the buffer's previous readers finished before the last barrier)
+    if (tid == 0) {
+      bulk_copy_g2s(smem_addr(ms), planes + w.poff, (uint32_t)sp_item_units(R8) * 16u, mbf);
+      copy_out = true;
     }
-    __syncthreads();
-    for (int t = tid; t < kN * (kChunk / 8); t += kThreads) {
-      const int j = t % kN, kg = t / kN;
-      uint32_t pk[kDigits][4];
-      double xv[8];
-#pragma unroll
-      for (int r8 = 0; r8 < 8; r8++) {
-        const int q = kg * 8 + r8;
-        xv[r8] = (j < nb && q < Lc) ? __ldg(X + (int64_t)__ldg(cols + q) * ldx + j) : 0.0;
-      }
-#pragma unroll
-      for (int r8 = 0; r8 < 8; r8 += 2) {
-        float d0[kDigits], d1[kDigits];
-        digits8(xv[r8], eY[j], d0);
-        digits8(xv[r8 + 1], eY[j], d1);
-#pragma unroll
-        for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
-      }
-      const int off = core_off_k(j >> 3, kg, kChunk) + (j & 7) * 16;
-#pragma unroll
-      for (int s2 = 0; s2 < kDigits; s2++)
-        *reinterpret_cast<uint4*>(sB + s2 * kPlaneB128 + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+    // the next item's column indices (used after this item's gathers for an L2 prefetch of its rows of
+    // X, and by its own gathers), exponent slots of the other parity
+    int nc = -1;
+    if (more && tid < 64) {
+      const TcSpmmItem wn = items[idx + 1];
+      nc = tid < wn.Lc ? __ldg(col + wn.cbase + tid) : -1;
+      ecol[32 * ((k + 1) & 1) + (tid & 31)] = 0;
+      em[64 * ((k + 1) & 1) + tid] = tid < wn.R ? ex[wn.eoff + tid] : 0;
     }
-    const uint4* pl = planes + poff[it];
-    const int per_sub = kDigits * R8 * 4;
-    for (int sb = 0; sb < kChunk / kSub && !failed; sb++) {
-      // the item's digit planes of this sub-block: plane s2 (R8 rows) to the start of smem plane s2
-      for (int t = tid; t < per_sub; t += kThreads) {
-        const int s2 = t / (R8 * 4), rem = t % (R8 * 4);
-        *reinterpret_cast<uint4*>(sA + s2 * kPlaneA + rem * 16) = __ldg(pl + (int64_t)sb * per_sub + t);
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (tid == 0) {
-        const uint32_t aBase = smem_addr(sA), bBase = smem_addr(sB);
-#pragma unroll 1
-        for (int g = 0; g < kDigits; g++)
-          for (int s2 = 0; s2 <= g; s2++) {
-            const int t = g - s2;
-#pragma unroll
-            for (int kk = 0; kk < kSub / 16; kk++) {
-              const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
-              const uint64_t db =
-                  smem_desc(bBase + t * kPlaneB128 + (sb * 4 + 2 * kk) * 128, 128, (kChunk / 8) * 128);
-              const uint32_t accum = (sb > 0 || s2 > 0 || kk > 0) ? 1u : 0u;
-              mma_bf16(tmem + (uint32_t)(g * kN), da, db, idesc, accum);
-            }
-          }
-        mma_commit(mb);
-      }
-      if (!mbar_wait(mb, phase)) failed = true;
-      phase ^= 1;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      __syncthreads();   // the sub-block's planes are free for the next one
+    sp_stage_x(cq + 64 * (k & 1), X, ldx, nb, packed, xs, ecs);
+    if (nc >= 0) {
+      const double* xr = X + (int64_t)nc * ldx;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(xr));
+      if (nb > 16) asm volatile("prefetch.global.L2 [%0];" ::"l"(xr + 16));
     }
-    if (failed) break;
-    if (warp * 32 < R) {   // warps holding rows of the run read their lanes back
-      const int Er = tid < R ? ex[eoff[it] + tid] : 0;
-#pragma unroll
-      for (int cb = 0; cb < kN; cb += 8) {
-        long long Th[8], Tl[8];
-#pragma unroll
-        for (int q = 0; q < 8; q++) Th[q] = Tl[q] = 0;
-#pragma unroll
-        for (int g = 0; g < kDigits; g++) {
-          float v[8];
-          tmem_ld8(lane_base + (uint32_t)(g * kN + cb), v);
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-          for (int q = 0; q < 8; q++) {
-            const long long iv = (long long)__float2int_rn(v[q]);
-            if (g < 4) Th[q] += iv << (7 * (3 - g));
-            else Tl[q] += iv << (7 * (7 - g));
-          }
-        }
-        if (tid < R) {
-#pragma unroll
-          for (int q = 0; q < 8; q++) {
-            const int j = cb + q;
-            if (j < nb) {
-              const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
-              atomicAdd(Y + (int64_t)(r0 + tid) * ldy + j, coef * (t * pow2(Er + eY[j] - 2044 - 35)));
-            }
-          }
-        }
-      }
-    }
+    if (more && tid < 64) cq[64 * ((k + 1) & 1) + tid] = nc;
+    // the X planes (generic stores) are visible to the tensor core's async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0) {
+      if (mbar_wait(mbf, ph_full)) {
+        ph_full ^= 1u;
+        copy_out = false;
+        const uint32_t plane = (uint32_t)R8 * 64u, sub = kDigits * plane;
+        for (int b = 0; b < nrb; b++) {
+          const int N = min(32, R - 32 * b) > 16 ? 32 : 16;
+          const uint32_t idesc = instr_desc(128, N);
+#pragma unroll 1
+          for (int ks = 0; ks < kSpK / 16; ks++) {
+            const uint64_t db = dM + (((ks >> 1) * sub + b * 2048u + (ks & 1) * 256u) >> 4);
+            const uint64_t dx = dX + (uint64_t)(ks * 16);
+            if (packed) {
+              // accumulator of row block b: lanes (group g, column j); plane t of M meets X digits g - t
+#pragma unroll
+              for (int t = 0; t < kDigits; t++)
+                mma_bf16(tmem + (uint32_t)(b * 32), dx + (uint64_t)((7 - t) * (kSpXPlaneP >> 4)),
+                         db + (uint64_t)(t * (plane >> 4)), idesc, (ks > 0 || t > 0) ? 1u : 0u);
+            } else {
+              // groups 0..3 (t <= 3) and 4..7: two accumulators per row block
+#pragma unroll
+              for (int t = 0; t < 4; t++)
+                mma_bf16(tmem + (uint32_t)(b * 64), dx + (uint64_t)((3 - t) * (kSpXPlaneW >> 4)),
+                         db + (uint64_t)(t * (plane >> 4)), idesc, (ks > 0 || t > 0) ? 1u : 0u);
+#pragma unroll
+              for (int t = 0; t < kDigits; t++)
+                mma_bf16(tmem + (uint32_t)(b * 64 + 32), dx + (uint64_t)((7 - t) * (kSpXPlaneW >> 4)),
+                         db + (uint64_t)(t * (plane >> 4)), idesc, (ks > 0 || t > 0) ? 1u : 0u);
+            }
+          }
+        }
+      } else {
+        *sfail = 1;
+      }
+      mma_commit(mbm);
+    }
+    const bool ok = mbar_wait(mbm, ph_mma);
+    ph_mma ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (__syncthreads_or(!ok || (tid == 0 && *sfail))) {
+      failed = true;
+      break;
+    }
+    // readout into the M buffer (its planes are consumed): per lane (group g, column j) the exact int64
+    // digit sums T_hi = sum_{g<4} D_g 2^(7 (3 - g)), T_lo = sum_{g>=4} D_g 2^(7 (7 - g)), one partial per
+    // warp; D_g < 8 * 64 * 127^2 < 2^23, so the partials stay below 2^46
+    long long* PH = reinterpret_cast<long long*>(ms);
+    long long* PL = PH + 4096;
+    const int rounds = packed ? 1 : nrb;
+    for (int rb = 0; rb < rounds; rb++) {
+      if (!packed) {
+        // lane (r = warp % 4, column j = lane): groups r (block 0) and 4 + r (block 1) of row block rb;
+        // warps 0-3 take the first half of its row groups, 4-7 the second
+        const int r = warp & 3, j = lane;
+        const int ngr = min(32, R - 32 * rb) > 16 ? 4 : 2;
+        const int g0 = warp < 4 ? 0 : ngr / 2, g1 = warp < 4 ? ngr / 2 : ngr;
+        for (int ig = g0; ig < g1; ig++) {
+          float v0[8], v1[8];
+          tmem_ld8(lane_base + (uint32_t)(rb * 64 + ig * 8), v0);
+          tmem_ld8(lane_base + (uint32_t)(rb * 64 + 32 + ig * 8), v1);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const int e = (r * 32 + ig * 8 + q) * 32 + j;
+            PH[e] = (long long)__float2int_rn(v0[q]) << (7 * (3 - r));
+            PL[e] = (long long)__float2int_rn(v1[q]) << (7 * (3 - r));
+          }
+        }
+      } else {
+        // lane (group g = 2 (warp % 4) + lane / 16, column j = lane % 16); the two groups of a warp are
+        // both below 4 (warps 0, 1) or both above (2, 3) and are added by a shuffle; warps 0-3 and 4-7
+        // split the row groups (the two row blocks, or the halves of one)
+        const int g = 2 * (warp & 3) + (lane >> 4), j = lane & 15;
+        const int sh = g < 4 ? 7 * (3 - g) : 7 * (7 - g);
+        const int ngr_total = nrb == 2 ? 4 + ((R - 32) > 16 ? 4 : 2) : (R > 16 ? 4 : 2);
+        const int first = warp < 4 ? 0 : (nrb == 2 ? 4 : ngr_total / 2);
+        const int last = warp < 4 ? (nrb == 2 ? 4 : ngr_total / 2) : ngr_total;
+        for (int gi = first; gi < last; gi++) {
+          const int b = gi >> 2, ig = gi & 3;
+          float v[8];
+          tmem_ld8(lane_base + (uint32_t)(b * 32 + ig * 8), v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            long long t = (long long)__float2int_rn(v[q]) << sh;
+            t += __shfl_xor_sync(0xffffffffu, t, 16);
+            if (lane < 16) PH[((warp & 3) * 64 + b * 32 + ig * 8 + q) * 16 + j] = t;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // convert: thread tid owns pairs p = tid + 256 o of the run (row p / 32 and column p % 32, or
+      // row p / 16 and column p % 16 with nb <= 16); the partials are added in a fixed order
+#pragma unroll
+      for (int o = 0; o < 8; o++) {
+        const int p = tid + 256 * o;
+        const int i = packed ? p >> 4 : p >> 5, j = packed ? p & 15 : p & 31;
+        const bool mine = packed ? o < 4 : (o >> 2) == rb;
+        if (!mine || i >= R || j >= nb) continue;
+        long long th, tl;
+        if (packed) {
+          th = PH[i * 16 + j] + PH[(64 + i) * 16 + j];
+          tl = PH[(128 + i) * 16 + j] + PH[(192 + i) * 16 + j];
+        } else {
+          const int e = (i - 32 * rb) * 32 + j;
+          th = PH[e] + PH[1024 + e] + PH[2048 + e] + PH[3072 + e];
+          tl = PL[e] + PL[1024 + e] + PL[2048 + e] + PL[3072 + e];
+        }
+        const double t = fma((double)tl, 0x1p-28, (double)th);
+        acc[o] = fma(t, pow2(ecs[j] + ems[i] - 2044 - 35), acc[o]);
+      }
+      if (rb + 1 < rounds) __syncthreads();
+    }
+    if (w.last) {   // the run is complete: its rows of Y
+#pragma unroll
+      for (int o = 0; o < 8; o++) {
+        const int p = tid + 256 * o;
+        const int i = packed ? p >> 4 : p >> 5, j = packed ? p & 15 : p & 31;
+        if ((!packed || o < 4) && i < R && j < nb) Y[(int64_t)(w.r0 + i) * ldy + j] = coef * acc[o];
+        acc[o] = 0.0;
+      }
+    }
+    // the readout's generic accesses to the M buffer precede the next bulk copy into it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
   }
-  if (failed) {
+  if (failed && tid == 0) {
     atomicOr(err, 1);
-    mbar_wait(mb, phase ^ 1);
+    if (copy_out) mbar_wait(mbf, ph_full);   // bounded
+    mbar_wait(mbm, ph_mma ^ 1u);             // bounded: MMAs still in flight finish before TMEM is freed
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kSpTmemCols) : "memory");
 }
 
 std::mutex g_attr_mu;
@@ -838,61 +1042,116 @@ void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
 void TcSpmm::build(Ctx& c, int64_t n, const std::vector<int32_t>& grp_h, const std::vector<int64_t>& row_ptr) {
   std::vector<int4> it;
   std::vector<int64_t> po, eo;
+  std::vector<int32_t> run_first;   // first item of each run
+  std::vector<int2> zr;
   int64_t pcur = 0, ecur = 0;
-  for (size_t g = 0; g + 1 < grp_h.size(); g++) {
+  const int nruns = (int)grp_h.size() - 1;
+  for (int g = 0; g < nruns; g++) {
+    run_first.push_back((int32_t)it.size());
     const int r0 = grp_h[g], R = grp_h[g + 1] - r0;
     if (R <= 0) continue;
     if (R > 64) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: a row run longer than 64 rows");
     const int64_t len = row_ptr[r0 + 1] - row_ptr[r0];
+    if (len == 0) zr.push_back(make_int2(r0, R));
     const int R8 = (R + 7) & ~7;
-    for (int64_t q0 = 0; q0 < len; q0 += kChunk) {
-      it.push_back(make_int4((int)g, (int)q0, R, (int)std::min<int64_t>(kChunk, len - q0)));
+    for (int64_t q0 = 0; q0 < len; q0 += kSpK) {
+      it.push_back(make_int4(g, (int)q0, R, (int)std::min<int64_t>(kSpK, len - q0)));
       po.push_back(pcur);
       eo.push_back(ecur);
-      pcur += (int64_t)(kChunk / kSub) * kDigits * R8 * 4;   // uint4 units
+      pcur += sp_item_units(R8);
       ecur += R;
     }
   }
+  run_first.push_back((int32_t)it.size());
+  if (ecur > INT32_MAX) fail(FEM2D_E_TOO_LARGE, "tensor SpMM: too many row exponents");
   nitems = (int)it.size();
   plane_units = pcur;
   exp_count = ecur;
+  nzero = (int)zr.size();
+  // the product kernel's order: CTA b takes the runs b, b + grid, ... (two CTAs per SM)
+  grid = std::max(1, std::min(std::max(nruns, 1), 2 * c.num_sms));
+  std::vector<TcSpmmItem> ci;
+  std::vector<int32_t> cp;
+  ci.reserve(it.size());
+  for (int b = 0; b < grid; b++) {
+    cp.push_back((int32_t)ci.size());
+    for (int g = b; g < nruns; g += grid)
+      for (int q = run_first[g]; q < run_first[g + 1]; q++) {
+        const int4 w = it[q];
+        TcSpmmItem m;
+        m.cbase = row_ptr[grp_h[g]] + w.y;
+        m.poff = po[q];
+        m.eoff = (int32_t)eo[q];
+        m.r0 = grp_h[g];
+        m.R = (int16_t)w.z;
+        m.Lc = (int16_t)w.w;
+        m.last = q + 1 == run_first[g + 1] ? 1 : 0;
+        ci.push_back(m);
+      }
+  }
+  cp.push_back((int32_t)ci.size());
   items.upload(it, c.stream);
   poff.upload(po, c.stream);
   eoff.upload(eo, c.stream);
+  citems.upload(ci, c.stream);
+  cta_ptr.upload(cp, c.stream);
+  zruns.upload(zr.empty() ? std::vector<int2>{make_int2(0, 0)} : zr, c.stream);
   (void)n;
 }
 
-void TcSpmm::slice(Ctx& c, const int32_t* grp, const int64_t* rp, const double* v, int which) {
-  DBuf<uint4>& pl = which == 0 ? planesA : planesB;
-  DBuf<int>& ex = which == 0 ? expA : expB;
-  if (pl.n != (size_t)std::max<int64_t>(plane_units, 1)) pl.alloc_on(std::max<int64_t>(plane_units, 1), c.stream);
-  if (ex.n != (size_t)std::max<int64_t>(exp_count, 1)) ex.alloc_on(std::max<int64_t>(exp_count, 1), c.stream);
+void TcSpmm::slice(Ctx& c, int k, const int32_t* grp, const int64_t* rp, const double* va, const double* vb,
+                   double ca, double cb) {
+  if (k < 0 || k >= kSlots) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: slot out of range");
+  Slot& sl = slot[k];
+  if (sl.planes.n != (size_t)std::max<int64_t>(plane_units, 1)) sl.planes.alloc_on(std::max<int64_t>(plane_units, 1), c.stream);
+  if (sl.exps.n != (size_t)std::max<int64_t>(exp_count, 1)) sl.exps.alloc_on(std::max<int64_t>(exp_count, 1), c.stream);
+  sl.ca = ca;
+  sl.cb = cb;
+  sl.ready = true;
   if (nitems == 0) return;
   const int grid = std::max(1, std::min(nitems, c.num_sms * 8));
-  spmm_slice_kernel<<<grid, kThreads, 0, c.stream>>>(nitems, items.p, grp, rp, poff.p, eoff.p, v, pl.p, ex.p);
+  spmm_slice_kernel<<<grid, 256, 0, c.stream>>>(nitems, items.p, grp, rp, poff.p, eoff.p, va, vb, ca, cb, sl.planes.p,
+                                                 sl.exps.p);
   FEM2D_CUDA(cudaGetLastError());
   c.launches++;
-  (which == 0 ? readyA : readyB) = true;
 }
 
-void TcSpmm::apply(Ctx& c, int which, double coef, const int32_t* grp, const int64_t* rp, const int32_t* col,
+int TcSpmm::find(double ca, double cb, double* coef) const {
+  for (int k = 0; k < kSlots; k++) {
+    const Slot& sl = slot[k];
+    if (!sl.ready) continue;
+    if (sl.ca == 1.0 && sl.cb == 0.0 && cb == 0.0 && ca != 0.0) {
+      *coef = ca;
+      return k;
+    }
+    if (sl.ca == 0.0 && sl.cb == 1.0 && ca == 0.0 && cb != 0.0) {
+      *coef = cb;
+      return k;
+    }
+    if (sl.ca == ca && sl.cb == cb) {
+      *coef = 1.0;
+      return k;
+    }
+  }
+  return -1;
+}
+
+void TcSpmm::apply(Ctx& c, int k, double coef, const int32_t* grp, const int64_t* rp, const int32_t* col,
                    const double* X, int64_t ldx, int nb, double* Y, int64_t ldy, int* err) {
-  if (nb < 1 || nb > kN) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: 1..32 columns");
-  if (!(which == 0 ? readyA : readyB)) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: matrix not sliced");
+  if (nb < 1 || nb > 32) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: 1..32 columns");
+  if (k < 0 || k >= kSlots || !slot[k].ready) fail(FEM2D_E_INVALID_ARG, "tensor SpMM: matrix not sliced");
   static std::mutex mu;
   static bool done[256] = {};
   {
     std::lock_guard<std::mutex> lk(mu);
     if (c.device >= 0 && c.device < 256 && !done[c.device]) {
-      FEM2D_CUDA(cudaFuncSetAttribute(spmm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmmSmem));
+      FEM2D_CUDA(cudaFuncSetAttribute(spmm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpSmem));
       done[c.device] = true;
     }
   }
-  if (nitems == 0) return;
-  const int grid = std::max(1, std::min(nitems, c.num_sms));
-  spmm_tc_kernel<<<grid, kThreads, kSpmmSmem, c.stream>>>(nitems, items.p, grp, rp, col, poff.p, eoff.p,
-                                                         which == 0 ? planesA.p : planesB.p,
-                                                         which == 0 ? expA.p : expB.p, coef, X, ldx, nb, Y, ldy, err);
+  if (grid == 0) return;
+  spmm_tc_kernel<<<grid, kSpThreads, kSpSmem, c.stream>>>(citems.p, cta_ptr.p, zruns.p, nzero, col, slot[k].planes.p,
+                                                          slot[k].exps.p, coef, X, ldx, nb, Y, ldy, err);
   FEM2D_CUDA(cudaGetLastError());
   c.launches++;
 }

@@ -240,8 +240,9 @@ int fem2d_gep_spmm_device(fem2d_ctx* c, const fem2d_gep* g, double c_a, double c
  * FP64 rounding level), method 1: FP64 on the CUDA cores. Synchronises; FEM2D_E_TIMEOUT if a bounded
  * wait inside the tensor kernel expired. */
 /* Y = coef M X with M = A (which 0) or B (which 1) of the GEP, on the tensor cores: FP64 emulated by
- * exact 7-bit digit slices of M's values (one exponent per row and 128-column chunk of each row run)
- * and of X (one exponent per column and chunk), FP32-exact digit sums in TMEM, exact int64 recombination.
+ * exact 7-bit digit slices of M's values (one exponent per row and 64-column chunk of each row run)
+ * and of X (one exponent per column and chunk), FP32-exact digit sums in TMEM, exact int64 recombination;
+ * every row of Y is written, and the result does not depend on scheduling (bitwise reproducible).
  * The operator product gpu_solve_gep uses for its T applications and basis products (no counterpart in the
  * reference), exposed for checking and timing; the values are sliced on every call here. Device row-major
  * n x nb blocks, 1 <= nb <= 32. Synchronises. */
@@ -276,12 +277,13 @@ typedef struct fem2d_solve_opts {
                            row-run blocks when the Jacobi-scaled factorizations are inaccurate),
                            1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's diagonal blocks
                            over runs of rows with one column list) */
-  int dense;            /* the eigensolver's FP64 contractions: 0 = Gram products and block updates of
-                           the B-orthogonalisation and Rayleigh-Ritz steps emulated on the tensor cores
-                           (tcgen05, exact integer slicing; default), operator products on the FP64
-                           CUDA cores; 1 = everything on the FP64 CUDA cores; 2 = as 0 plus the operator
-                           products with A or B alone on the tensor cores (slower than the CUDA-core
-                           kernel at present: Elem row runs of a few rows fill 128-row MMA tiles poorly) */
+  int dense;            /* the eigensolver's FP64 contractions: 0 = default: Gram products and block
+                           updates of the B-orthogonalisation and Rayleigh-Ritz steps emulated on the
+                           tensor cores (tcgen05, exact integer slicing), and from 1,000,000 nonzeros the
+                           operator products with A or B alone as well; 1 = everything on the FP64 CUDA
+                           cores; 2 = as 0 with the tensor-core operator products at every size;
+                           3 = tensor-core Gram products and block updates, operator products on the
+                           FP64 CUDA cores */
   const fem2d_patchnet* net;   /* trained patch network (precond 2), else NULL */
   int refine;           /* FP64 iterative-refinement steps per exact shifted solve: 0 = calibrated on a random
                            block (default; up to 3 while they reduce the residual), k > 0 = k steps
