@@ -92,6 +92,7 @@ void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
     for (int64_t c0 = 0; c0 < std::max<int64_t>(len, 1); c0 += 256) work.push_back(make_int2((int)q, (int)c0));
   }
   d.grp.upload(grp, s);
+  d.grp_h = grp;
   d.gwork.upload(work, s);
   d.ngrp = (int)grp.size() - 1;
   d.nwork = (int)work.size();

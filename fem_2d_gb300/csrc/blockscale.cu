@@ -156,46 +156,40 @@ __global__ void __launch_bounds__(256) run_back_kernel(const int32_t* __restrict
 }  // namespace
 
 void BlockScale::build(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* sa, double* sb) {
-  const int64_t n = h.n;
-  // runs exactly as device_upload forms them, their column-run segments, block offsets
-  std::vector<int32_t> grp{0};
-  for (int64_t i = 1; i <= n; i++) {
-    const int64_t g = grp.back();
-    bool brk = i == n || i - g >= 64;
-    if (!brk) {
-      const int64_t li = h.row_ptr[i + 1] - h.row_ptr[i], lg = h.row_ptr[g + 1] - h.row_ptr[g];
-      brk = li != lg || std::memcmp(h.col.data() + h.row_ptr[i], h.col.data() + h.row_ptr[g], li * sizeof(int32_t)) != 0;
+  if (!ready) {
+    const int64_t n = h.n;
+    // runs exactly as device_upload forms them, their column-run segments, block offsets
+    const std::vector<int32_t>& grp = d.grp_h;
+    ngrp = (int)grp.size() - 1;
+    std::vector<int32_t> run_of(n);
+    for (int g = 0; g < ngrp; g++)
+      for (int32_t i = grp[g]; i < grp[g + 1]; i++) run_of[i] = g;
+    std::vector<int64_t> so(ngrp + 1, 0), sp(ngrp + 1, 0);
+    std::vector<int2> sg;
+    for (int g = 0; g < ngrp; g++) {
+      const int R = grp[g + 1] - grp[g];
+      so[g + 1] = so[g] + (int64_t)R * R;
+      const int64_t b = h.row_ptr[grp[g]], e = h.row_ptr[grp[g] + 1];
+      int64_t q = b;
+      while (q < e) {
+        const int32_t hr = run_of[h.col[q]];
+        const int H = grp[hr + 1] - grp[hr];
+        // a column run appears whole and in order (its columns are consecutive DoFs)
+        if (h.col[q] != grp[hr] || q + H > e || h.col[q + H - 1] != grp[hr] + H - 1)
+          fail(FEM2D_E_INVALID_ARG, "block scaling: a column run is split in a row pattern");
+        sg.push_back(make_int2(hr, (int)(q - b)));
+        q += H;
+      }
+      sp[g + 1] = (int64_t)sg.size();
     }
-    if (brk) grp.push_back((int32_t)i);
+    // kept in the GEP's plan across solves: plain (not stream-ordered) allocations
+    grp_d.upload(grp, c.stream);
+    soff.upload(so, c.stream);
+    seg_ptr.upload(sp, c.stream);
+    seg.upload(sg, c.stream);
+    S.alloc(std::max<int64_t>(so[ngrp], 1));
+    ready = true;
   }
-  if (n == 0) grp.assign(1, 0);
-  ngrp = (int)grp.size() - 1;
-  std::vector<int32_t> run_of(n);
-  for (int g = 0; g < ngrp; g++)
-    for (int32_t i = grp[g]; i < grp[g + 1]; i++) run_of[i] = g;
-  std::vector<int64_t> so(ngrp + 1, 0), sp(ngrp + 1, 0);
-  std::vector<int2> sg;
-  for (int g = 0; g < ngrp; g++) {
-    const int R = grp[g + 1] - grp[g];
-    so[g + 1] = so[g] + (int64_t)R * R;
-    const int64_t b = h.row_ptr[grp[g]], e = h.row_ptr[grp[g] + 1];
-    int64_t q = b;
-    while (q < e) {
-      const int32_t hr = run_of[h.col[q]];
-      const int H = grp[hr + 1] - grp[hr];
-      // a column run appears whole and in order (its columns are consecutive DoFs)
-      if (h.col[q] != grp[hr] || q + H > e || h.col[q + H - 1] != grp[hr] + H - 1)
-        fail(FEM2D_E_INVALID_ARG, "block scaling: a column run is split in a row pattern");
-      sg.push_back(make_int2(hr, (int)(q - b)));
-      q += H;
-    }
-    sp[g + 1] = (int64_t)sg.size();
-  }
-  grp_d.upload_on(grp, c.stream);
-  soff.upload_on(so, c.stream);
-  seg_ptr.upload_on(sp, c.stream);
-  seg.upload_on(sg, c.stream);
-  S.alloc_on(std::max<int64_t>(so[ngrp], 1), c.stream);
   DBuf<int> flag;
   flag.alloc_on(1, c.stream);
   FEM2D_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c.stream));

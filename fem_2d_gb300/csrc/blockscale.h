@@ -13,7 +13,9 @@ struct BlockScale {
   DBuf<int64_t> seg_ptr;   // per run, its column-run segments
   DBuf<int2> seg;          // (column run, offset of its first column within the run's rows)
   DBuf<double> S;          // blockdiag(L_g^-1), row-major lower-triangular blocks
-  // S from B's diagonal blocks; sa = S A S^T, sb = S B S^T (full CSR order, same pattern)
+  bool ready = false;      // the pattern part (runs, block offsets, segments) is set up
+  // S from B's diagonal blocks; sa = S A S^T, sb = S B S^T (full CSR order, same pattern). The pattern
+  // part is set up on the first call and kept.
   void build(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* sa, double* sb);
   // X <- S^T X for an n x nb block (nb <= 32): eigenvectors of the scaled pencil back to the GEP's
   void unscale(Ctx& c, double* X, int64_t ldx, int nb) const;

@@ -142,6 +142,7 @@ struct DeviceGEP {
   // runs of consecutive rows with identical column lists (at most 64 rows each): row starts, ngrp + 1;
   // work items (run, first column of a <= 256-column segment) for the operator products
   DBuf<int32_t> grp;
+  std::vector<int32_t> grp_h;   // the same run starts on the host
   DBuf<int2> gwork;
   int ngrp = 0, nwork = 0;
   int nivl = 0;

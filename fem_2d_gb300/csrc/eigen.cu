@@ -707,7 +707,15 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // than the solve gains (about 8 ms per solve at 2-4k DoFs).
   constexpr int64_t kLargeN = 10000;
   const bool large = n >= kLargeN;
-  BlockScale bsc;
+  // the pattern-only structures kept in the plan (block scaling, tensor-core products) belong to the
+  // device they were built on
+  if (plan.aux_device != c.device) {
+    plan.bsc.reset();
+    plan.tcs.reset();
+    plan.aux_device = c.device;
+  }
+  if (!plan.bsc) plan.bsc = std::make_unique<BlockScale>();
+  BlockScale& bsc = *plan.bsc;
   bool blocked = false;
   if (o.scaling == 2 || (o.scaling == 0 && large)) {
     try {
@@ -967,10 +975,26 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   // on: the scaled pencil is final, so its values are sliced once (by default from kTensorSpmmNnz
   // nonzeros, where the slicing is amortised; always with dense = 2)
   constexpr int64_t kTensorSpmmNnz = 1000000;
-  TcSpmm tcs;
+  // the sliced pencil lives for this solve only (stream-ordered buffers, released on every exit path)
+  struct SliceRelease {
+    TcSpmm* t = nullptr;
+    ~SliceRelease() {
+      if (t)
+        for (auto& sl : t->slot) {
+          sl.planes.release();
+          sl.exps.release();
+          sl.ready = false;
+        }
+    }
+  } slice_release;
   if (d.nwork > 0 && (o.dense == 2 || (o.dense == 0 && h.nnz_full >= kTensorSpmmNnz))) {
     ProfScope ps(c, "spmm_slice", 2.0 * (8.0 * h.nnz_full + 16.0 * h.nnz_full), 0.0);
-    tcs.build(c, n, row_runs(h), h.row_ptr);
+    if (!plan.tcs) {
+      plan.tcs = std::make_unique<TcSpmm>();
+      plan.tcs->build(c, n, d.grp_h, h.row_ptr);
+    }
+    TcSpmm& tcs = *plan.tcs;
+    slice_release.t = &tcs;
     tcs.slice(c, 0, d.grp.p, d.row_ptr.p, sa.p, nullptr, 1.0, 0.0);
     tcs.slice(c, 1, d.grp.p, d.row_ptr.p, nullptr, sb.p, 0.0, 1.0);
     // the shifted matrices of the refinement residuals (exact solves with refinement steps)
@@ -1537,7 +1561,7 @@ void gep_spmm_tensor(Ctx& c, const HostGEP& h, const DeviceGEP& d, int which, do
   if (which != 0 && which != 1) fail(FEM2D_E_INVALID_ARG, "which must be 0 (A) or 1 (B)");
   if (nb < 1 || nb > 32) fail(FEM2D_E_INVALID_ARG, "1..32 columns");
   TcSpmm tcs;
-  tcs.build(c, h.n, row_runs(h), h.row_ptr);
+  tcs.build(c, h.n, d.grp_h, h.row_ptr);
   tcs.slice(c, 0, d.grp.p, d.row_ptr.p, which == 0 ? d.a.p : nullptr, which == 1 ? d.b.p : nullptr,
             which == 0 ? 1.0 : 0.0, which == 1 ? 1.0 : 0.0);
   Dev D{c, h, d, d.a.p, d.b.p};

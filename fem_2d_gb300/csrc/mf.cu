@@ -495,6 +495,38 @@ struct SolveArgs {
   int nb;
 };
 
+// the front's gathered right-hand side v[c * f + i] (pivot rows permuted): the pivot rows' entries of
+// B, then each child's update vector added in slot order (rows are distinct within one child, so no
+// atomics are needed, and the fixed order makes the sums, and the whole solve, reproducible bit for bit)
+__device__ __forceinline__ void gather_front_rhs(const FrontDesc& d, const FrontDesc* __restrict__ fd,
+                                                 const int32_t* __restrict__ emap, const int32_t* __restrict__ ipm,
+                                                 const double* __restrict__ W, const int64_t* __restrict__ woff,
+                                                 const double* __restrict__ B, int64_t ldb,
+                                                 const int32_t* __restrict__ D, const int32_t* __restrict__ pm, int nb,
+                                                 double* v) {
+  const int f = d.f, p = d.p;
+  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) {
+    const int i = t % f, c = t / f;
+    v[t] = i < p ? B[(int64_t)D[pm[i]] * ldb + c] : 0.0;
+  }
+  for (int slot = 0; slot < MAXKIDS; slot++) {
+    const int ch = d.kid[slot];
+    if (ch < 0) continue;   // uniform across the CTA
+    const FrontDesc cd = fd[ch];
+    const int sz = cd.f - cd.p;
+    const double* cw = W + woff[ch];
+    const int32_t* m = emap + cd.eptr;
+    __syncthreads();
+    for (int t = threadIdx.x; t < sz * nb; t += blockDim.x) {
+      const int i = t % sz, c = t / sz;
+      const int mi = m[i];
+      const int row = mi < p ? ipm[mi] : mi;   // pivot rows are stored permuted
+      v[c * f + row] += cw[(int64_t)c * cd.f + cd.p + i];
+    }
+  }
+  __syncthreads();
+}
+
 // forward solve of one small front by the calling CTA (sm: (f + p) * nb doubles)
 __device__ __forceinline__ void forward_small_front(int fr, const SolveArgs& a, double* sm) {
   const FrontDesc* __restrict__ fd = a.fd;
@@ -517,29 +549,7 @@ __device__ __forceinline__ void forward_small_front(int fr, const SolveArgs& a, 
   const int32_t* pm = perm + piv_off[fr];
   const int32_t* ipm = iperm + piv_off[fr];
   const double* A = F + d.off;
-  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) v[t] = 0.0;
-  __syncthreads();
-  // the pivot rows' right-hand side and every child's update vector in one pass (shared-memory
-  // atomics: two children can feed the same parent row), so their dependent index loads overlap
-  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
-    const int i = t % p, c = t / p;
-    atomicAdd(v + c * f + i, B[(int64_t)D[pm[i]] * ldb + c]);
-  }
-  for (int slot = 0; slot < MAXKIDS; slot++) {
-    const int ch = d.kid[slot];
-    if (ch < 0) continue;
-    const FrontDesc cd = fd[ch];
-    const int sz = cd.f - cd.p;
-    const double* cw = W + woff[ch];
-    const int32_t* m = emap + cd.eptr;
-    for (int t = threadIdx.x; t < sz * nb; t += blockDim.x) {
-      const int i = t % sz, c = t / sz;
-      const int mi = m[i];
-      const int row = mi < p ? ipm[mi] : mi;   // pivot rows are stored permuted
-      atomicAdd(v + c * f + row, cw[(int64_t)c * cd.f + cd.p + i]);
-    }
-  }
-  __syncthreads();
+  gather_front_rhs(d, fd, emap, ipm, W, woff, B, ldb, D, pm, nb, v);
   for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
     const int i = t % p, c = t / p;
     const double* vc = v + c * f;
@@ -640,27 +650,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(256)
   const int32_t* D = a.dofs + d.dptr;
   const double* A = a.F + d.off;
   double* out = a.W + a.woff[fr];
-  for (int t = threadIdx.x; t < f * nb; t += blockDim.x) v[t] = 0.0;
-  __syncthreads();
-  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
-    const int i = t % p, c = t / p;
-    atomicAdd(v + c * f + i, a.B[(int64_t)D[pm[i]] * a.ldb + c]);
-  }
-  for (int slot = 0; slot < MAXKIDS; slot++) {
-    const int ch = d.kid[slot];
-    if (ch < 0) continue;
-    const FrontDesc cd = fd[ch];
-    const int sz = cd.f - cd.p;
-    const double* cw = a.W + a.woff[ch];
-    const int32_t* m = emap + cd.eptr;
-    for (int t = threadIdx.x; t < sz * nb; t += blockDim.x) {
-      const int i = t % sz, c = t / sz;
-      const int mi = m[i];
-      const int row = mi < p ? ipm[mi] : mi;
-      atomicAdd(v + c * f + row, cw[(int64_t)c * cd.f + cd.p + i]);
-    }
-  }
-  __syncthreads();
+  gather_front_rhs(d, fd, emap, ipm, a.W, a.woff, a.B, a.ldb, D, pm, nb, v);
   // y = L11^-1 v[0:p] for this CTA's slice of pivot rows, straight into the workspace
   int r0, r1;
   row_slice(p, r, r0, r1);

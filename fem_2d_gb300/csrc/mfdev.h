@@ -5,8 +5,10 @@
 #include <mutex>
 #include <vector>
 
+#include "blockscale.h"
 #include "device.h"
 #include "mf.h"
+#include "ozaki.h"
 
 namespace fem2d {
 
@@ -75,6 +77,12 @@ struct MFPlan {
   bool dense = false;   // a single dense front (chosen when the sparse plan's solves are inaccurate)
   std::vector<uint8_t> lift;   // per DoF: levels its elimination was moved up (delayed pivots)
   int device = -1;
+  // pattern-only structures of the eigensolver, built on first use on the plan's device: the row-run
+  // block scaling's blocks and segments, the tensor-core operator products' items (their values are
+  // recomputed, and the pencil re-sliced, by every solve)
+  std::unique_ptr<BlockScale> bsc;
+  std::unique_ptr<TcSpmm> tcs;
+  int aux_device = -1;
   std::mutex mu;
 };
 

@@ -45,7 +45,6 @@ constexpr int kChunk = 128;    // rows per exact accumulation
 constexpr int kSub = 32;       // rows per shared-memory sub-block
 constexpr int kM = 128;        // tile rows (columns of X)
 constexpr int kN = 32;         // tile columns (columns of Y)
-constexpr int kThreads = 128;
 constexpr uint32_t kTmemCols = kDigits * kN;   // one FP32 accumulator of kN columns per digit sum
 constexpr int kPlaneA = kM * kSub * 2;         // bytes of one digit plane of X (128 rows x 32 bf16)
 constexpr int kPlaneB = kN * kSub * 2;         // bytes of one digit plane of Y
@@ -128,6 +127,23 @@ __device__ __forceinline__ void digits8(double v, int E, float (&d)[kDigits]) {
     const int dg = (int)((A >> (49 - 7 * s)) & 0x7F);
     d[s] = (float)(neg ? -dg : dg);
   }
+}
+
+// digits8 with integer digit extraction on 32-bit halves and a float conversion by the 2^23 offset
+// (no integer-to-float conversions); the same eight values as digits8
+__device__ __forceinline__ void digits8_fast(double v, int E, float (&d)[kDigits]) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  const int shift = E - ex;
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const unsigned long long A = (ex == 0 || shift > 55) ? 0ull : ((mant << 3) >> shift);
+  const uint32_t hi = (uint32_t)(A >> 32), lo = (uint32_t)A;
+  const float sg = (bits >> 63) ? -1.0f : 1.0f, off = -8388608.0f * sg;
+  const uint32_t dg[kDigits] = {(hi >> 17) & 0x7Fu, (hi >> 10) & 0x7Fu, (hi >> 3) & 0x7Fu,
+                                __funnelshift_r(lo, hi, 28) & 0x7Fu, (lo >> 21) & 0x7Fu, (lo >> 14) & 0x7Fu,
+                                (lo >> 7) & 0x7Fu, lo & 0x7Fu};
+#pragma unroll
+  for (int s = 0; s < kDigits; s++) d[s] = fmaf(__uint_as_float(0x4B000000u | dg[s]), sg, off);
 }
 
 __device__ __forceinline__ int biased_exp(double v) {
@@ -242,12 +258,14 @@ __global__ void __launch_bounds__(kGramThreads, 2)
         yv[r] = (y_ok && ra < r1) ? __ldg(Y + ra * ldy + cy0 + yj) : 0.0;
       }
       if (pending) {   // the digit planes are free once the previous sub-block's MMAs have completed
-        if (!mbar_wait(mb, phase)) failed = true;
-        phase ^= 1;
-        pending = false;
+        if (mbar_wait(mb, phase)) {
+          phase ^= 1;
+          pending = false;
+        } else {
+          failed = true;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
-      if (failed) break;
 #pragma unroll
       for (int kh = 0; kh < kSub / 16; kh++) {
         const int kg = half * (kSub / 16) + kh;
@@ -255,8 +273,8 @@ __global__ void __launch_bounds__(kGramThreads, 2)
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
           float d0[kDigits], d1[kDigits];
-          digits8(xv[kh * 8 + r8], Ex, d0);
-          digits8(xv[kh * 8 + r8 + 1], Ex, d1);
+          digits8_fast(xv[kh * 8 + r8], Ex, d0);
+          digits8_fast(xv[kh * 8 + r8 + 1], Ex, d1);
 #pragma unroll
           for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
         }
@@ -270,8 +288,8 @@ __global__ void __launch_bounds__(kGramThreads, 2)
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
           float d0[kDigits], d1[kDigits];
-          digits8(yv[r8], Ey, d0);
-          digits8(yv[r8 + 1], Ey, d1);
+          digits8_fast(yv[r8], Ey, d0);
+          digits8_fast(yv[r8 + 1], Ey, d1);
 #pragma unroll
           for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
         }
@@ -283,7 +301,10 @@ __global__ void __launch_bounds__(kGramThreads, 2)
       // the generic-proxy stores above must be visible to the tensor core's (async) proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
+      if (__syncthreads_or(failed)) {   // a bounded wait expired somewhere: every thread leaves together
+        failed = true;
+        break;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (tid == 0) {
         const uint32_t aBase = smem_addr(sA), bBase = smem_addr(sB);
@@ -305,12 +326,18 @@ __global__ void __launch_bounds__(kGramThreads, 2)
     }
     if (failed) break;
     if (pending) {   // the chunk's last MMAs, before its accumulators are read
-      if (!mbar_wait(mb, phase)) failed = true;
-      phase ^= 1;
-      pending = false;
+      if (mbar_wait(mb, phase)) {
+        phase ^= 1;
+        pending = false;
+      } else {
+        failed = true;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
-    if (failed) break;
+    if (__syncthreads_or(failed)) {
+      failed = true;
+      break;
+    }
     // combine the eight exact digit-sum accumulators of this chunk (this thread's row and column half,
     // 8 columns at a time). acc_g <= (g + 1) 128 127^2 < 2^24; in int64, exactly,
     //   T_hi = sum_{g<4} acc_g 2^(7 (3 - g)) < 2^43,   T_lo = sum_{g>=4} acc_g 2^(7 (7 - g)) < 2^47,
@@ -345,9 +372,9 @@ __global__ void __launch_bounds__(kGramThreads, 2)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  if (failed) {
+  if (failed && tid == 0) {   // every thread arrives here (uniform exits)
     atomicOr(err, 1);
-    mbar_wait(mb, phase ^ 1);   // bounded: let MMAs still in flight finish before TMEM is freed
+    if (pending) mbar_wait(mb, phase);   // bounded: let MMAs still in flight finish before TMEM is freed
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -376,15 +403,20 @@ __global__ void ozaki_reduce_kernel(const double* __restrict__ P, int nrb, int n
 // ---------------------------------------------------------------------------------------------------
 // Z = beta Z + alpha X C for a tall X (n x a, a <= 256) and a small C (a x b, b <= 32): the block
 // updates of the B-orthogonalisation and the Ritz-vector products. Each CTA owns 128-row tiles of X
-// and Z (one row per thread). X is sliced with one exponent per row (over its a entries) and C with one
-// per column (over its a entries), so every K sub-block's digit sums share one scale: they are read
-// from TMEM after each 128 columns of K (the exact-accumulation limit) and summed exactly in int64,
-// and converted to FP64 once per output element. C's digit planes stay in shared memory for all tiles.
-// The row exponents come from a coalesced pre-pass (row_exp_kernel), and each sub-block's loads are
-// issued before waiting on the previous sub-block's MMAs.
+// and Z (TMEM lane = row; 8 warps, two threads per row, each slicing 16 of a sub-block's 32 columns of
+// X and owning 16 of the 32 columns of Z). X is sliced with one exponent per row (over its a entries)
+// and C with one per column (over its a entries), so every K sub-block's digit sums share one scale:
+// they are read from TMEM after each 128 columns of K (the exact-accumulation limit) and summed exactly
+// in int64, and converted to FP64 once per output element. C's digit planes (K padded to kc) stay in
+// shared memory for all tiles; the sub-blocks of X alternate between two digit-plane stages (one when C
+// is too wide for two), so the slicing of one overlaps the MMAs of the previous. The row exponents come
+// from a coalesced pre-pass (row_exp_kernel).
 constexpr int kGemmKMax = 256;
-constexpr int kPlaneC = kN * kGemmKMax * 2;          // one digit plane of C (32 x 256 bf16, K-major)
-constexpr int kGemmSmem = kDigits * kPlaneA + kDigits * kPlaneC + 1024;
+constexpr int kGemmThreads = 256;
+constexpr int kGemmStage = kDigits * kPlaneA;   // digit planes of one 128 x 32 sub-block of X (64 KB)
+constexpr int kGemmSmemMax = 227 * 1024;
+// shared memory of the block update for K padded to kc, with `stages` sub-block stages
+__host__ __device__ constexpr int gemm_smem(int kc, int stages) { return stages * kGemmStage + kDigits * kN * kc * 2 + 1024; }
 
 // byte offset of core matrix (row group rg, k group kg) in a K-major tile with kc columns
 __device__ __forceinline__ int core_off_k(int rg, int kg, int kc) { return (rg * (kc / 8) + kg) * 128; }
@@ -403,18 +435,19 @@ __global__ void __launch_bounds__(256) row_exp_kernel(int64_t n, const double* _
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kGemmThreads, 1)
     ozaki_gemm_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ C, int b,
                       double alpha, double beta, double* __restrict__ Z, int64_t ldz, const int* __restrict__ EXr,
-                      int* __restrict__ err) {
+                      int stages, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA = smem;                              // kDigits planes of kM x kSub (X sub-block)
-  uint8_t* sC = smem + kDigits * kPlaneA;          // kDigits planes of kN x kGemmKMax (all of C)
-  int* eC = reinterpret_cast<int*>(sC + kDigits * kPlaneC);   // kN column exponents of C
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(eC + kN);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
   const int kc = (a + kSub - 1) / kSub * kSub;     // K padded to whole sub-blocks
+  const int planeC = kN * kc * 2;                  // one digit plane of C (32 x kc bf16, K-major)
+  uint8_t* sC = smem + stages * kGemmStage;
+  int* eC = reinterpret_cast<int*>(sC + kDigits * planeC);   // kN column exponents of C
+  uint64_t* bar = reinterpret_cast<uint64_t*>(eC + kN);       // [2] MMAs of a stage committed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int rl = tid & (kM - 1), half = tid >> 7;  // row of the tile (TMEM lane), column half
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
@@ -423,7 +456,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar + 1)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // C's column exponents, then its digit planes (row j of the B operand = column j of C)
@@ -434,7 +468,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     eC[tid] = e;
   }
   __syncthreads();
-  for (int t = tid; t < kN * (kc / 8); t += kThreads) {
+  for (int t = tid; t < kN * (kc / 8); t += kGemmThreads) {
     const int j = t % kN, kg = t / kN;
     uint32_t pk[kDigits][4];
 #pragma unroll
@@ -446,131 +480,149 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
     }
-    const int off = core_off_k(j >> 3, kg, kGemmKMax) + (j & 7) * 16;
+    const int off = core_off_k(j >> 3, kg, kc) + (j & 7) * 16;
 #pragma unroll
     for (int s2 = 0; s2 < kDigits; s2++)
-      *reinterpret_cast<uint4*>(sC + s2 * kPlaneC + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+      *reinterpret_cast<uint4*>(sC + s2 * planeC + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
   }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t mb = smem_addr(mbar);
-  uint32_t phase = 0;
   bool failed = false;
   constexpr uint32_t idesc = instr_desc(kM, kN);
-  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const uint64_t dC = smem_desc(smem_addr(sC), 128, (uint32_t)kc * 16u);
+  uint32_t ph = 0u;          // bit st: phase of stage st's barrier
+  uint32_t pending = 0u;     // bit st: MMAs committed on stage st and not yet waited for
+  int sbc = 0;               // sub-blocks issued so far (selects the stage)
 
   const int64_t ntiles = (n + kM - 1) / kM;
-  bool pending = false;
   for (int64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-    const int64_t row = tile * kM + tid;
+    const int64_t row = tile * kM + rl;
     const bool row_ok = row < n;
     const double* xr = X + row * ldx;
     const int Ex = row_ok ? EXr[row] : 0;
-    long long Th[kN], Tl[kN];
+    long long Th[kN / 2], Tl[kN / 2];
 #pragma unroll
-    for (int j = 0; j < kN; j++) Th[j] = Tl[j] = 0;
-    for (int k0 = 0; k0 < kc && !failed; k0 += kSub) {
-      // this thread's row of the X sub-block (32 columns), loaded before waiting on the previous MMAs
-      double xv[kSub];
+    for (int j = 0; j < kN / 2; j++) Th[j] = Tl[j] = 0;
+    for (int k0 = 0; k0 < kc && !failed; k0 += kSub, sbc++) {
+      const int st = stages == 2 ? (sbc & 1) : 0;
+      uint8_t* sA = smem + st * kGemmStage;
+      // this thread's 16 columns of the row's sub-block, loaded before waiting on the stage's MMAs
+      double xv[kSub / 2];
 #pragma unroll
-      for (int q = 0; q < kSub; q++) xv[q] = (row_ok && k0 + q < a) ? __ldg(xr + k0 + q) : 0.0;
-      if (pending) {
-        if (!mbar_wait(mb, phase)) failed = true;
-        phase ^= 1;
-        pending = false;
+      for (int q = 0; q < kSub / 2; q++) {
+        const int kq = k0 + half * (kSub / 2) + q;
+        xv[q] = (row_ok && kq < a) ? __ldg(xr + kq) : 0.0;
+      }
+      if ((pending >> st) & 1u) {   // the stage's digit planes are free once its last MMAs completed
+        if (mbar_wait(smem_addr(bar + st), (ph >> st) & 1u)) {
+          ph ^= 1u << st;
+          pending &= ~(1u << st);
+        } else {
+          failed = true;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
-      if (failed) break;
 #pragma unroll
-      for (int kg = 0; kg < kSub / 8; kg++) {
+      for (int kh = 0; kh < 2; kh++) {
+        const int kg = half * 2 + kh;
         uint32_t pk[kDigits][4];
 #pragma unroll
         for (int r8 = 0; r8 < 8; r8 += 2) {
           float d0[kDigits], d1[kDigits];
-          digits8(xv[kg * 8 + r8], Ex, d0);
-          digits8(xv[kg * 8 + r8 + 1], Ex, d1);
+          digits8_fast(xv[kh * 8 + r8], Ex, d0);
+          digits8_fast(xv[kh * 8 + r8 + 1], Ex, d1);
 #pragma unroll
           for (int s2 = 0; s2 < kDigits; s2++) pk[s2][r8 >> 1] = pack_bf16(d0[s2], d1[s2]);
         }
-        const int off = core_off(tid >> 3, kg) + (tid & 7) * 16;
+        const int off = core_off(rl >> 3, kg) + (rl & 7) * 16;
 #pragma unroll
         for (int s2 = 0; s2 < kDigits; s2++)
           *reinterpret_cast<uint4*>(sA + s2 * kPlaneA + off) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
+      if (__syncthreads_or(failed)) {   // a bounded wait expired somewhere: every thread leaves together
+        failed = true;
+        break;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const bool first = (k0 % kChunk) == 0;   // the accumulators restart every 128 columns of K
       if (tid == 0) {
-        const uint32_t aBase = smem_addr(sA), cBase = smem_addr(sC);
+        const uint64_t dA = smem_desc(smem_addr(sA), 128, (kSub / 8) * 128);
 #pragma unroll 1
         for (int g = 0; g < kDigits; g++)
           for (int s2 = 0; s2 <= g; s2++) {
             const int t = g - s2;
 #pragma unroll
             for (int kk = 0; kk < kSub / 16; kk++) {
-              const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
-              const uint64_t dc =
-                  smem_desc(cBase + t * kPlaneC + ((k0 / 8) + 2 * kk) * 128, 128, (kGemmKMax / 8) * 128);
               const uint32_t accum = (!first || s2 > 0 || kk > 0) ? 1u : 0u;
-              mma_bf16(tmem + (uint32_t)(g * kN), da, dc, idesc, accum);
+              mma_bf16(tmem + (uint32_t)(g * kN), dA + (uint64_t)((s2 * kPlaneA + kk * 256) >> 4),
+                       dC + (uint64_t)((t * planeC + ((k0 / 8) + 2 * kk) * 128) >> 4), idesc, accum);
             }
           }
-        mma_commit(mb);
+        mma_commit(smem_addr(bar + st));
       }
-      pending = true;
+      pending |= 1u << st;
       const bool last = (k0 + kSub) % kChunk == 0 || k0 + kSub >= kc;
       if (last) {   // the accumulators are read back: wait for these MMAs now
-        if (!mbar_wait(mb, phase)) failed = true;
-        phase ^= 1;
-        pending = false;
+        if (mbar_wait(smem_addr(bar + st), (ph >> st) & 1u)) {
+          ph ^= 1u << st;
+          pending &= ~(1u << st);
+        } else {
+          failed = true;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      }
-      if (last && !failed) {
-        // exact digit sums of these (at most 128) columns of K into the int64 accumulators
+        if (__syncthreads_or(failed)) {
+          failed = true;
+          break;
+        }
+        {
+          // exact digit sums of these (at most 128) columns of K into the int64 accumulators
 #pragma unroll
-        for (int cb = 0; cb < kN; cb += 8) {
+          for (int cb = 0; cb < kN / 2; cb += 8) {
+            float v[kDigits][8];
 #pragma unroll
-          for (int g = 0; g < kDigits; g++) {
-            float v[8];
-            tmem_ld8(lane_base + (uint32_t)(g * kN + cb), v);
+            for (int g = 0; g < kDigits; g++) tmem_ld8(lane_base + (uint32_t)(g * kN + half * (kN / 2) + cb), v[g]);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-              const long long iv = (long long)__float2int_rn(v[q]);
-              if (g < 4) Th[cb + q] += iv << (7 * (3 - g));
-              else Tl[cb + q] += iv << (7 * (7 - g));
-            }
+            for (int g = 0; g < kDigits; g++)
+#pragma unroll
+              for (int q = 0; q < 8; q++) {
+                const long long iv = (long long)__float2int_rn(v[g][q]);
+                if (g < 4) Th[cb + q] += iv << (7 * (3 - g));
+                else Tl[cb + q] += iv << (7 * (7 - g));
+              }
           }
         }
+        // every thread's reads of the accumulators precede the next MMAs
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      }
-      // after `last`, every thread's reads of the accumulators precede the next MMAs
-      if (last) {
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
     }
     if (failed) break;
     if (row_ok) {
-      double* zr = Z + row * ldz;
+      double* zr = Z + row * ldz + half * (kN / 2);
 #pragma unroll
-      for (int j = 0; j < kN; j++) {
+      for (int q = 0; q < kN / 2; q++) {
+        const int j = half * (kN / 2) + q;
         if (j >= b) break;
-        const double t = fma((double)Tl[j], 0x1p-28, (double)Th[j]);
+        const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
         const double v = alpha * (t * pow2(Ex + eC[j] - 2044 - 35));
-        zr[j] = beta == 0.0 ? v : fma(beta, zr[j], v);
+        zr[q] = beta == 0.0 ? v : fma(beta, zr[q], v);
       }
     }
   }
-  if (failed) {
-    atomicOr(err, 1);
-    mbar_wait(mb, phase ^ 1);
-  } else if (pending) {
-    if (!mbar_wait(mb, phase)) atomicOr(err, 1);
+  if (failed) {   // every thread arrives here (uniform exits); MMAs in flight finish before TMEM is freed
+    if (tid == 0) {
+      atomicOr(err, 1);
+      for (int q = 0; q < 2; q++)
+        if ((pending >> q) & 1u) mbar_wait(smem_addr(bar + q), (ph >> q) & 1u);   // bounded
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -614,23 +666,6 @@ constexpr uint32_t kSpTmemCols = 128;
 
 // uint4 units of one item's digit planes: 2 sub-blocks of 32 K x 8 planes x R8 rows x 4 k-groups
 __host__ __device__ constexpr int sp_item_units(int r8) { return 2 * kDigits * r8 * 4; }
-
-// digits8 with integer digit extraction on 32-bit halves and a float conversion by the 2^23 offset
-// (no integer-to-float conversions); the same eight values as digits8
-__device__ __forceinline__ void digits8_fast(double v, int E, float (&d)[kDigits]) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  const int ex = (int)((bits >> 52) & 0x7FF);
-  const int shift = E - ex;
-  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const unsigned long long A = (ex == 0 || shift > 55) ? 0ull : ((mant << 3) >> shift);
-  const uint32_t hi = (uint32_t)(A >> 32), lo = (uint32_t)A;
-  const float sg = (bits >> 63) ? -1.0f : 1.0f, off = -8388608.0f * sg;
-  const uint32_t dg[kDigits] = {(hi >> 17) & 0x7Fu, (hi >> 10) & 0x7Fu, (hi >> 3) & 0x7Fu,
-                                __funnelshift_r(lo, hi, 28) & 0x7Fu, (lo >> 21) & 0x7Fu, (lo >> 14) & 0x7Fu,
-                                (lo >> 7) & 0x7Fu, lo & 0x7Fu};
-#pragma unroll
-  for (int s = 0; s < kDigits; s++) d[s] = fmaf(__uint_as_float(0x4B000000u | dg[s]), sg, off);
-}
 
 __global__ void __launch_bounds__(256) spmm_slice_kernel(int nitems, const int4* __restrict__ items,
                                                           const int32_t* __restrict__ grp,
@@ -1026,15 +1061,18 @@ void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
   {
     std::lock_guard<std::mutex> lk(mu);
     if (c.device >= 0 && c.device < 256 && !done[c.device]) {
-      FEM2D_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
+      FEM2D_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmemMax));
       done[c.device] = true;
     }
   }
+  const int kc = (a + kSub - 1) / kSub * kSub;
+  const int stages = gemm_smem(kc, 2) <= kGemmSmemMax ? 2 : 1;
   const int64_t ntiles = (n + kM - 1) / kM;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)c.num_sms));
   row_exp_kernel<<<(int)std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c.num_sms * 16), 256, 0, c.stream>>>(
       n, X, ldx, a, rowexp);
-  ozaki_gemm_kernel<<<grid, kThreads, kGemmSmem, c.stream>>>(n, X, ldx, a, C, b, alpha, beta, Z, ldz, rowexp, err);
+  ozaki_gemm_kernel<<<grid, kGemmThreads, gemm_smem(kc, stages), c.stream>>>(n, X, ldx, a, C, b, alpha, beta, Z, ldz,
+                                                                            rowexp, stages, err);
   FEM2D_CUDA(cudaGetLastError());
   c.launches += 2;
 }
