@@ -235,7 +235,6 @@ __global__ void __launch_bounds__(kGramThreads, 2)
   const bool col_ok = my_col < a;
   const int yj = tid % kN, ykg = tid / kN;   // threads 0..127: a column of Y and its 8-row group
   const bool y_ok = tid < kN * (kSub / 8) && cy0 + yj < b;
-  constexpr uint32_t idesc = instr_desc(kM, kN);
 
   for (int64_t c0 = r0; c0 < r1 && !failed; c0 += kChunk) {
     const int64_t chunk = c0 / kChunk;
@@ -309,16 +308,17 @@ __global__ void __launch_bounds__(kGramThreads, 2)
       if (tid == 0) {
         const uint32_t aBase = smem_addr(sA), bBase = smem_addr(sB);
 #pragma unroll 1
-        for (int g = 0; g < kDigits; g++)
-          for (int s2 = 0; s2 <= g; s2++) {
-            const int t = g - s2;
+        // digit s2 of X against Y's digit planes 0 .. 7 - s2 stacked along N, written at TMEM column
+        // 32 s2: the pair (s2, t) lands in accumulator g = s2 + t (one MMA per digit of X; an MMA costs
+        // about the same for every N up to 64, so wide N pays)
+#pragma unroll 1
+        for (int s2 = 0; s2 < kDigits; s2++)
 #pragma unroll
-            for (int kk = 0; kk < kSub / 16; kk++) {
-              const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
-              const uint64_t db = smem_desc(bBase + t * kPlaneB + kk * 256, 128, (kSub / 8) * 128);
-              const uint32_t accum = (sb > 0 || s2 > 0 || kk > 0) ? 1u : 0u;
-              mma_bf16(tmem + (uint32_t)(g * kN), da, db, idesc, accum);
-            }
+          for (int kk = 0; kk < kSub / 16; kk++) {
+            const uint64_t da = smem_desc(aBase + s2 * kPlaneA + kk * 256, 128, (kSub / 8) * 128);
+            const uint64_t db = smem_desc(bBase + kk * 256, 128, (kSub / 8) * 128);
+            const uint32_t accum = (sb > 0 || s2 > 0 || kk > 0) ? 1u : 0u;
+            mma_bf16(tmem + (uint32_t)(s2 * kN), da, db, instr_desc(kM, (kDigits - s2) * kN), accum);
           }
         mma_commit(mb);
       }
@@ -408,15 +408,20 @@ __global__ void ozaki_reduce_kernel(const double* __restrict__ P, int nrb, int n
 // and C with one per column (over its a entries), so every K sub-block's digit sums share one scale:
 // they are read from TMEM after each 128 columns of K (the exact-accumulation limit) and summed exactly
 // in int64, and converted to FP64 once per output element. C's digit planes (K padded to kc) stay in
-// shared memory for all tiles; the sub-blocks of X alternate between two digit-plane stages (one when C
-// is too wide for two), so the slicing of one overlaps the MMAs of the previous. The row exponents come
-// from a coalesced pre-pass (row_exp_kernel).
+// shared memory for all tiles. Each 128 x 32 sub-block of X is brought in by coalesced asynchronous
+// copies (cp.async, a whole row segment per warp instruction) into a padded staging buffer, one
+// sub-block ahead of its slicing when two staging buffers fit. The row exponents come from a
+// coalesced pre-pass (row_exp_kernel).
 constexpr int kGemmKMax = 256;
 constexpr int kGemmThreads = 256;
-constexpr int kGemmStage = kDigits * kPlaneA;   // digit planes of one 128 x 32 sub-block of X (64 KB)
+constexpr int kGemmPlanes = kDigits * kPlaneA;   // digit planes of one 128 x 32 sub-block of X (64 KB)
+constexpr int kGemmRow = kSub + 1;               // staged doubles per row (padded: no bank conflicts)
+constexpr int kGemmStage = kM * kGemmRow * 8;    // one staged 128 x 32 sub-block of X (33 KB)
 constexpr int kGemmSmemMax = 227 * 1024;
-// shared memory of the block update for K padded to kc, with `stages` sub-block stages
-__host__ __device__ constexpr int gemm_smem(int kc, int stages) { return stages * kGemmStage + kDigits * kN * kc * 2 + 1024; }
+// shared memory of the block update for K padded to kc, with `stages` staging buffers
+__host__ __device__ constexpr int gemm_smem(int kc, int stages) {
+  return kGemmPlanes + stages * kGemmStage + kDigits * kN * kc * 2 + 1024;
+}
 
 // byte offset of core matrix (row group rg, k group kg) in a K-major tile with kc columns
 __device__ __forceinline__ int core_off_k(int rg, int kg, int kc) { return (rg * (kc / 8) + kg) * 128; }
@@ -435,6 +440,24 @@ __global__ void __launch_bounds__(256) row_exp_kernel(int64_t n, const double* _
   }
 }
 
+// rows of X tile `tile`, columns k0 .. k0 + 31, into the staging buffer sx (row r at r * kGemmRow);
+// entries outside X are zero-filled
+__device__ __forceinline__ void gemm_stage(const double* __restrict__ X, int64_t n, int64_t ldx, int a, int64_t tile,
+                                           int k0, double* sx) {
+#pragma unroll
+  for (int i = 0; i < kM * kSub / kGemmThreads; i++) {
+    const int e = threadIdx.x + kGemmThreads * i;
+    const int r = e >> 5, q = e & 31;
+    const int64_t row = tile * kM + r;
+    const bool ok = row < n && k0 + q < a;
+    const double* src = ok ? X + row * ldx + k0 + q : X;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_addr(sx + r * kGemmRow + q)), "l"(src),
+                 "r"(ok ? 8 : 0)
+                 : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(kGemmThreads, 1)
     ozaki_gemm_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a, const double* __restrict__ C, int b,
                       double alpha, double beta, double* __restrict__ Z, int64_t ldz, const int* __restrict__ EXr,
@@ -442,12 +465,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   extern __shared__ __align__(1024) uint8_t smem[];
   const int kc = (a + kSub - 1) / kSub * kSub;     // K padded to whole sub-blocks
   const int planeC = kN * kc * 2;                  // one digit plane of C (32 x kc bf16, K-major)
-  uint8_t* sC = smem + stages * kGemmStage;
+  uint8_t* sA = smem;                              // digit planes of the current sub-block of X
+  double* sX = reinterpret_cast<double*>(smem + kGemmPlanes);   // staging buffers
+  uint8_t* sC = smem + kGemmPlanes + stages * kGemmStage;
   int* eC = reinterpret_cast<int*>(sC + kDigits * planeC);   // kN column exponents of C
-  uint64_t* bar = reinterpret_cast<uint64_t*>(eC + kN);       // [2] MMAs of a stage committed
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(eC + kN);       // MMAs committed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int rl = tid & (kM - 1), half = tid >> 7;  // row of the tile (TMEM lane), column half
+  const int64_t ntiles = (n + kM - 1) / kM;
+  const int nsub = kc / kSub;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
@@ -457,10 +484,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar + 1)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // C's column exponents, then its digit planes (row j of the B operand = column j of C)
+  // the first sub-block's copies, then C's column exponents and digit planes (row j of the B operand =
+  // column j of C)
+  if (blockIdx.x < ntiles) gemm_stage(X, n, ldx, a, blockIdx.x, 0, sX);
   if (tid < kN) {
     int e = 0;
     if (tid < b)
@@ -491,36 +519,45 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   bool failed = false;
-  constexpr uint32_t idesc = instr_desc(kM, kN);
   const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const uint64_t dA = smem_desc(smem_addr(sA), 128, (kSub / 8) * 128);
   const uint64_t dC = smem_desc(smem_addr(sC), 128, (uint32_t)kc * 16u);
-  uint32_t ph = 0u;          // bit st: phase of stage st's barrier
-  uint32_t pending = 0u;     // bit st: MMAs committed on stage st and not yet waited for
-  int sbc = 0;               // sub-blocks issued so far (selects the stage)
+  uint32_t ph = 0u;
+  bool pending = false;   // MMAs committed and not yet waited for (they read sA)
+  int sbc = 0;            // sub-blocks staged so far (selects the staging buffer)
 
-  const int64_t ntiles = (n + kM - 1) / kM;
   for (int64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
     const int64_t row = tile * kM + rl;
     const bool row_ok = row < n;
-    const double* xr = X + row * ldx;
     const int Ex = row_ok ? EXr[row] : 0;
     long long Th[kN / 2], Tl[kN / 2];
 #pragma unroll
     for (int j = 0; j < kN / 2; j++) Th[j] = Tl[j] = 0;
-    for (int k0 = 0; k0 < kc && !failed; k0 += kSub, sbc++) {
-      const int st = stages == 2 ? (sbc & 1) : 0;
-      uint8_t* sA = smem + st * kGemmStage;
-      // this thread's 16 columns of the row's sub-block, loaded before waiting on the stage's MMAs
+    for (int sb = 0; sb < nsub && !failed; sb++, sbc++) {
+      const int k0 = sb * kSub;
+      const double* sx = sX + (stages == 2 ? (sbc & 1) : 0) * (kGemmStage / 8);
+      // the next sub-block's copies into the other staging buffer (with one buffer, after the slicing)
+      int64_t nt = tile;
+      int nk = k0 + kSub;
+      if (nk >= kc) {
+        nt = tile + gridDim.x;
+        nk = 0;
+      }
+      const bool more = nt < ntiles;
+      if (stages == 2 && more) {
+        gemm_stage(X, n, ldx, a, nt, nk, sX + ((sbc + 1) & 1) * (kGemmStage / 8));
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
+      __syncthreads();   // every thread's copies of this sub-block have landed
       double xv[kSub / 2];
 #pragma unroll
-      for (int q = 0; q < kSub / 2; q++) {
-        const int kq = k0 + half * (kSub / 2) + q;
-        xv[q] = (row_ok && kq < a) ? __ldg(xr + kq) : 0.0;
-      }
-      if ((pending >> st) & 1u) {   // the stage's digit planes are free once its last MMAs completed
-        if (mbar_wait(smem_addr(bar + st), (ph >> st) & 1u)) {
-          ph ^= 1u << st;
-          pending &= ~(1u << st);
+      for (int q = 0; q < kSub / 2; q++) xv[q] = sx[rl * kGemmRow + half * (kSub / 2) + q];
+      if (pending) {   // the digit planes are free once the previous MMAs completed
+        if (mbar_wait(smem_addr(bar), ph)) {
+          ph ^= 1u;
+          pending = false;
         } else {
           failed = true;
         }
@@ -550,28 +587,29 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // with one staging buffer the next sub-block's copies start now (its slot was read above)
+      if (stages == 1 && more) gemm_stage(X, n, ldx, a, nt, nk, sX);
       const bool first = (k0 % kChunk) == 0;   // the accumulators restart every 128 columns of K
       if (tid == 0) {
-        const uint64_t dA = smem_desc(smem_addr(sA), 128, (kSub / 8) * 128);
 #pragma unroll 1
-        for (int g = 0; g < kDigits; g++)
-          for (int s2 = 0; s2 <= g; s2++) {
-            const int t = g - s2;
+        // digit s2 of X against C's digit planes 0 .. 7 - s2 stacked along N, written at TMEM column
+        // 32 s2: the pair (s2, t) lands in accumulator g = s2 + t
+#pragma unroll 1
+        for (int s2 = 0; s2 < kDigits; s2++)
 #pragma unroll
-            for (int kk = 0; kk < kSub / 16; kk++) {
-              const uint32_t accum = (!first || s2 > 0 || kk > 0) ? 1u : 0u;
-              mma_bf16(tmem + (uint32_t)(g * kN), dA + (uint64_t)((s2 * kPlaneA + kk * 256) >> 4),
-                       dC + (uint64_t)((t * planeC + ((k0 / 8) + 2 * kk) * 128) >> 4), idesc, accum);
-            }
+          for (int kk = 0; kk < kSub / 16; kk++) {
+            const uint32_t accum = (!first || s2 > 0 || kk > 0) ? 1u : 0u;
+            mma_bf16(tmem + (uint32_t)(s2 * kN), dA + (uint64_t)((s2 * kPlaneA + kk * 256) >> 4),
+                     dC + (uint64_t)((((k0 / 8) + 2 * kk) * 128) >> 4), instr_desc(kM, (kDigits - s2) * kN), accum);
           }
-        mma_commit(smem_addr(bar + st));
+        mma_commit(smem_addr(bar));
       }
-      pending |= 1u << st;
+      pending = true;
       const bool last = (k0 + kSub) % kChunk == 0 || k0 + kSub >= kc;
       if (last) {   // the accumulators are read back: wait for these MMAs now
-        if (mbar_wait(smem_addr(bar + st), (ph >> st) & 1u)) {
-          ph ^= 1u << st;
-          pending &= ~(1u << st);
+        if (mbar_wait(smem_addr(bar), ph)) {
+          ph ^= 1u;
+          pending = false;
         } else {
           failed = true;
         }
@@ -580,23 +618,21 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           failed = true;
           break;
         }
-        {
-          // exact digit sums of these (at most 128) columns of K into the int64 accumulators
+        // exact digit sums of these (at most 128) columns of K into the int64 accumulators
 #pragma unroll
-          for (int cb = 0; cb < kN / 2; cb += 8) {
-            float v[kDigits][8];
+        for (int cb = 0; cb < kN / 2; cb += 8) {
+          float v[kDigits][8];
 #pragma unroll
-            for (int g = 0; g < kDigits; g++) tmem_ld8(lane_base + (uint32_t)(g * kN + half * (kN / 2) + cb), v[g]);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          for (int g = 0; g < kDigits; g++) tmem_ld8(lane_base + (uint32_t)(g * kN + half * (kN / 2) + cb), v[g]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int g = 0; g < kDigits; g++)
+          for (int g = 0; g < kDigits; g++)
 #pragma unroll
-              for (int q = 0; q < 8; q++) {
-                const long long iv = (long long)__float2int_rn(v[g][q]);
-                if (g < 4) Th[cb + q] += iv << (7 * (3 - g));
-                else Tl[cb + q] += iv << (7 * (7 - g));
-              }
-          }
+            for (int q = 0; q < 8; q++) {
+              const long long iv = (long long)__float2int_rn(v[g][q]);
+              if (g < 4) Th[cb + q] += iv << (7 * (3 - g));
+              else Tl[cb + q] += iv << (7 * (7 - g));
+            }
         }
         // every thread's reads of the accumulators precede the next MMAs
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -617,12 +653,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
     }
   }
-  if (failed) {   // every thread arrives here (uniform exits); MMAs in flight finish before TMEM is freed
-    if (tid == 0) {
-      atomicOr(err, 1);
-      for (int q = 0; q < 2; q++)
-        if ((pending >> q) & 1u) mbar_wait(smem_addr(bar + q), (ph >> q) & 1u);   // bounded
-    }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");   // no copy outlives the kernel
+  if (failed && tid == 0) {   // every thread arrives here (uniform exits)
+    atomicOr(err, 1);
+    if (pending) mbar_wait(smem_addr(bar), ph);   // bounded: MMAs in flight finish before TMEM is freed
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -896,30 +930,29 @@ __global__ void __launch_bounds__(kSpThreads, 2)
         ph_full ^= 1u;
         copy_out = false;
         const uint32_t plane = (uint32_t)R8 * 64u, sub = kDigits * plane;
-        for (int b = 0; b < nrb; b++) {
-          const int N = min(32, R - 32 * b) > 16 ? 32 : 16;
-          const uint32_t idesc = instr_desc(128, N);
+        // all the run's rows in one MMA (N = R rounded up to 16, at most 64: an MMA costs about the
+        // same for every N up to 64); TMEM column = run row
+        const uint32_t idesc = instr_desc(128, (R + 15) & ~15);
 #pragma unroll 1
-          for (int ks = 0; ks < kSpK / 16; ks++) {
-            const uint64_t db = dM + (((ks >> 1) * sub + b * 2048u + (ks & 1) * 256u) >> 4);
-            const uint64_t dx = dX + (uint64_t)(ks * 16);
-            if (packed) {
-              // accumulator of row block b: lanes (group g, column j); plane t of M meets X digits g - t
+        for (int ks = 0; ks < kSpK / 16; ks++) {
+          const uint64_t db = dM + (((ks >> 1) * sub + (ks & 1) * 256u) >> 4);
+          const uint64_t dx = dX + (uint64_t)(ks * 16);
+          if (packed) {
+            // lanes (group g, column j); plane t of M meets X digits g - t
 #pragma unroll
-              for (int t = 0; t < kDigits; t++)
-                mma_bf16(tmem + (uint32_t)(b * 32), dx + (uint64_t)((7 - t) * (kSpXPlaneP >> 4)),
-                         db + (uint64_t)(t * (plane >> 4)), idesc, (ks > 0 || t > 0) ? 1u : 0u);
-            } else {
-              // groups 0..3 (t <= 3) and 4..7: two accumulators per row block
+            for (int t = 0; t < kDigits; t++)
+              mma_bf16(tmem, dx + (uint64_t)((7 - t) * (kSpXPlaneP >> 4)), db + (uint64_t)(t * (plane >> 4)), idesc,
+                       (ks > 0 || t > 0) ? 1u : 0u);
+          } else {
+            // groups 0..3 (t <= 3) at TMEM column 0 and 4..7 at column 64
 #pragma unroll
-              for (int t = 0; t < 4; t++)
-                mma_bf16(tmem + (uint32_t)(b * 64), dx + (uint64_t)((3 - t) * (kSpXPlaneW >> 4)),
-                         db + (uint64_t)(t * (plane >> 4)), idesc, (ks > 0 || t > 0) ? 1u : 0u);
+            for (int t = 0; t < 4; t++)
+              mma_bf16(tmem, dx + (uint64_t)((3 - t) * (kSpXPlaneW >> 4)), db + (uint64_t)(t * (plane >> 4)), idesc,
+                       (ks > 0 || t > 0) ? 1u : 0u);
 #pragma unroll
-              for (int t = 0; t < kDigits; t++)
-                mma_bf16(tmem + (uint32_t)(b * 64 + 32), dx + (uint64_t)((7 - t) * (kSpXPlaneW >> 4)),
-                         db + (uint64_t)(t * (plane >> 4)), idesc, (ks > 0 || t > 0) ? 1u : 0u);
-            }
+            for (int t = 0; t < kDigits; t++)
+              mma_bf16(tmem + 64u, dx + (uint64_t)((7 - t) * (kSpXPlaneW >> 4)), db + (uint64_t)(t * (plane >> 4)),
+                       idesc, (ks > 0 || t > 0) ? 1u : 0u);
           }
         }
       } else {
@@ -949,8 +982,8 @@ __global__ void __launch_bounds__(kSpThreads, 2)
         const int g0 = warp < 4 ? 0 : ngr / 2, g1 = warp < 4 ? ngr / 2 : ngr;
         for (int ig = g0; ig < g1; ig++) {
           float v0[8], v1[8];
-          tmem_ld8(lane_base + (uint32_t)(rb * 64 + ig * 8), v0);
-          tmem_ld8(lane_base + (uint32_t)(rb * 64 + 32 + ig * 8), v1);
+          tmem_ld8(lane_base + (uint32_t)(rb * 32 + ig * 8), v0);
+          tmem_ld8(lane_base + (uint32_t)(64 + rb * 32 + ig * 8), v1);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int q = 0; q < 8; q++) {
