@@ -802,7 +802,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     }
   };
   // refinement steps needed by each factorization: measured once on a fixed random block, up to 3
-  // steps, while the relative residual max_j ||rhs_j - K x_j|| / ||rhs_j|| stays above 1e-12
+  // steps, while the solves are not backward stable (normwise backward error above kStableBwd) and the
+  // relative residual max_j ||rhs_j - K x_j|| / ||rhs_j|| stays above 1e-12.
   // The accuracy measure is the normwise backward error ||b - K x|| / (||K|| ||x|| + ||b||) of the
   // solves (||K|| bounded by the largest absolute row sum): a backward-stable factorization keeps it
   // near the unit roundoff whatever cond(K) is, whereas the plain residual ||b - K x|| / ||b|| cannot
@@ -821,6 +822,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     for (double v : hp) m = std::max(m, v);
     return m;
   };
+  // normwise backward error below which the exact solves are used without refinement
+  constexpr double kStableBwd = 1e-13;
   auto calibrate = [&](const MFFactor& fac, double ka, double kb, double& rel_out) -> int {
     const int nb = 4;
     const double knorm = pencil_norm(ka, kb);
@@ -848,7 +851,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
         bwd = std::max(bwd, rn / (knorm * xn + bn[j]));
       }
       if (nref == 0 || rel <= prev) rel_out = bwd;
-      if (rel < 1e-12 || bwd < 1e-15) return nref;        // as accurate as FP64 allows
+      // backward-stable solves apply T to a pencil within rounding of the scaled one: the Krylov space
+      // needs nothing more (the Rayleigh-Ritz step and the residuals use exact products), and the plain
+      // residual's floor eps * cond(K) is no measure of the factorization
+      if (rel < 1e-12 || bwd < kStableBwd) return nref;
       if (rel > 0.5 * prev) return std::max(0, nref - 1);  // refinement no longer improves
       prev = rel;
     }

@@ -286,8 +286,9 @@ typedef struct fem2d_solve_opts {
                            FP64 CUDA cores */
   const fem2d_patchnet* net;   /* trained patch network (precond 2), else NULL */
   int refine;           /* FP64 iterative-refinement steps per exact shifted solve: 0 = calibrated on a random
-                           block (default; up to 3 while they reduce the residual), k > 0 = k steps
-                           (at most 3), -1 = none */
+                           block (default: none when the solves are backward stable, normwise backward
+                           error below 1e-13; else up to 3 while they reduce the residual), k > 0 = k
+                           steps (at most 3), -1 = none */
 } fem2d_solve_opts;
 
 typedef struct fem2d_solve_stats {
