@@ -339,6 +339,58 @@ __global__ void __launch_bounds__(256) resid_partial_kernel(int64_t n, const dou
 }
 
 // s[i] = 1 / sqrt(B_ii) (B is SPD); one warp per row
+// per block of rows and column q < k: the entry of largest magnitude (signed) and its row, the first
+// such row in the block's ascending range (ties keep the smaller row)
+__global__ void __launch_bounds__(256) colmax_partial_kernel(int64_t n, const double* __restrict__ X, int64_t ldx,
+                                                             int k, double* __restrict__ pm, int64_t* __restrict__ pi) {
+  __shared__ double sv[256];
+  __shared__ int64_t si[256];
+  const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+  for (int q = 0; q < k; q++) {
+    double bv = 0.0;
+    int64_t bi = INT64_MAX;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      const double v = X[r * ldx + q];
+      if (fabs(v) > fabs(bv) || bi == INT64_MAX) {
+        bv = v;
+        bi = r;
+      }
+    }
+    sv[threadIdx.x] = bv;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+      if (threadIdx.x < off) {
+        const double ov = sv[threadIdx.x + off];
+        const int64_t oi = si[threadIdx.x + off];
+        const double mv = sv[threadIdx.x];
+        const int64_t mi = si[threadIdx.x];
+        if (oi != INT64_MAX && (mi == INT64_MAX || fabs(ov) > fabs(mv) || (fabs(ov) == fabs(mv) && oi < mi))) {
+          sv[threadIdx.x] = ov;
+          si[threadIdx.x] = oi;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      pm[(int64_t)blockIdx.x * k + q] = sv[0];
+      pi[(int64_t)blockIdx.x * k + q] = si[0] == INT64_MAX ? INT64_MAX : si[0];
+    }
+    __syncthreads();
+  }
+}
+
+// VT[q * n + i] = sgn[q] X[i * ldx + q]: one contiguous vector per pair
+__global__ void signed_transpose_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int k,
+                                        const double* __restrict__ sgn, double* __restrict__ VT) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(t / n);
+    const int64_t i = t - (int64_t)q * n;
+    VT[t] = sgn[q] * X[i * ldx + q];
+  }
+}
+
 __global__ void jacobi_scale_kernel(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                                     const double* __restrict__ vb, double* __restrict__ sc, int* __restrict__ bad) {
   const int lane = threadIdx.x & 31;
@@ -1376,20 +1428,48 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       st->max_backward_error = wb;
     }
   }
-  // outputs: B-normalised (the Ritz vectors are B-orthonormal), sign fixed by the largest entry
-  std::vector<double> Xh((size_t)n * 32);
-  FEM2D_CUDA(cudaMemcpyAsync(Xh.data(), XO.p, Xh.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+  // outputs: B-normalised (the Ritz vectors are B-orthonormal), sign fixed by the largest entry (the
+  // first of equal magnitude); the signs and the transposition to one contiguous vector per pair are
+  // done on the device, so exactly kout x n doubles come back
   for (int q = 0; q < kout; q++) {
     if (values) values[q] = theta_out[q];
     if (residuals) residuals[q] = rel_out[q];
-    if (vectors) {
-      int64_t imax = 0;
-      for (int64_t i = 0; i < n; i++)
-        if (std::fabs(Xh[(size_t)i * 32 + q]) > std::fabs(Xh[(size_t)imax * 32 + q])) imax = i;
-      const double sgn = Xh[(size_t)imax * 32 + q] < 0 ? -1.0 : 1.0;
-      for (int64_t i = 0; i < n; i++) vectors[(size_t)q * n + i] = sgn * Xh[(size_t)i * 32 + q];
+  }
+  if (vectors && kout > 0) {
+    const int nblk = (int)std::min<int64_t>(D.grid_rows(), std::max<int64_t>(1, (n + 255) / 256));
+    DBuf<double> pm;
+    DBuf<int64_t> pi;
+    pm.alloc_on((size_t)nblk * kout, c.stream);
+    pi.alloc_on((size_t)nblk * kout, c.stream);
+    colmax_partial_kernel<<<nblk, 256, 0, c.stream>>>(n, XO.p, 32, kout, pm.p, pi.p);
+    c.launches++;
+    std::vector<double> hm((size_t)nblk * kout);
+    std::vector<int64_t> hi((size_t)nblk * kout);
+    FEM2D_CUDA(cudaMemcpyAsync(hm.data(), pm.p, hm.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaMemcpyAsync(hi.data(), pi.p, hi.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<double> sgn(kout, 1.0);
+    for (int q = 0; q < kout; q++) {
+      double best = -1.0, val = 0.0;
+      int64_t bi = INT64_MAX;
+      for (int b = 0; b < nblk; b++) {   // blocks hold ascending row ranges: keep the first maximum
+        const double m = std::fabs(hm[(size_t)b * kout + q]);
+        if (m > best || (m == best && hi[(size_t)b * kout + q] < bi)) {
+          best = m;
+          bi = hi[(size_t)b * kout + q];
+          val = hm[(size_t)b * kout + q];
+        }
+      }
+      sgn[q] = val < 0 ? -1.0 : 1.0;
     }
+    DBuf<double> sg, VT;
+    sg.upload_on(sgn, c.stream);
+    VT.alloc_on((size_t)kout * n, c.stream);
+    const int64_t tb = std::min<int64_t>((n * kout + 255) / 256, (int64_t)c.num_sms * 16);
+    signed_transpose_kernel<<<(int)std::max<int64_t>(tb, 1), 256, 0, c.stream>>>(n, XO.p, 32, kout, sg.p, VT.p);
+    c.launches++;
+    FEM2D_CUDA(cudaMemcpyAsync(vectors, VT.p, (size_t)kout * n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    FEM2D_CUDA(cudaStreamSynchronize(c.stream));
   }
   if (!converged)
     fail(FEM2D_E_NOT_CONVERGED, "gpu_solve_gep did not reach the residual tolerance (outputs hold the last iterate)");
