@@ -473,6 +473,8 @@ def run_native(args, ws, rank, local):
     dom_name = max(regions, key=lambda k: regions[k]["ms"])
     hbm, peak_kind = peaks()
     fp64 = ctx.fp64_peak()
+    # issue cost of one tcgen05.mma (M = 128, K = 16) by N: the cost model of the tensor-core kernels
+    mma_ns = {str(nn): round(ctx.mma_ns(nn), 2) for nn in (32, 64, 128, 256)}
 
     def roof(reg):
         """The region's achieved HBM bandwidth and FP64 rate against the measured peaks; `bound` is the
@@ -524,7 +526,7 @@ def run_native(args, ws, rank, local):
            "region_rooflines": {k: roof(k) for k in regions if k != dom_name},
            "solve_stats": res.stats if res is not None else None,
            "max_rel_residual": float(np.max(res.residuals)) if res is not None else None,
-           "clocks": clocks}
+           "clocks": clocks, "tensor_mma_ns_per_sm": mma_ns}
     if rank == 0 and not args.no_check:
         out["parity"] = oracle_check(w, args.workload, gep, res)
     if rank == 0 and not args.no_check:

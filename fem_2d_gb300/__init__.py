@@ -144,6 +144,7 @@ def lib():
         "fem2d_ctx_profile_query": (ctypes.c_int, [P, ctypes.c_char_p, dp, i64p, dp]),
         "fem2d_ctx_profile_flops": (ctypes.c_int, [P, ctypes.c_char_p, dp]),
         "fem2d_ctx_fp64_peak": (ctypes.c_int, [P, dp]),
+        "fem2d_ctx_mma_ns": (ctypes.c_int, [P, ctypes.c_int, dp]),
         "fem2d_dense_solve_gep": (ctypes.c_int, [P, P, d, dp, dp]),
         "fem2d_gep_shifted_solve": (ctypes.c_int, [P, P, d, d, ctypes.c_int, ctypes.c_int, dp, dp]),
         "fem2d_gpu_solve_gep": (ctypes.c_int, [P, P, d, ctypes.c_int, ctypes.POINTER(_fem2d_solve_opts), dp, dp, dp,
@@ -482,6 +483,12 @@ class Context:
                                              ctypes.byref(by)))
         _check(lib().fem2d_ctx_profile_flops(self._h, region.encode(), ctypes.byref(fl)))
         return {"ms": ms.value, "count": cnt.value, "bytes": by.value, "flops": fl.value}
+
+    def mma_ns(self, n):
+        """Measured issue cost (ns per instruction and SM) of tcgen05.mma kind::f16, M = 128, K = 16, N = n."""
+        t = ctypes.c_double()
+        _check(lib().fem2d_ctx_mma_ns(self._h, int(n), ctypes.byref(t)))
+        return t.value
 
     def fp64_peak(self):
         """Measured FP64 FMA throughput of the device in TFLOP/s (library microbenchmark)."""

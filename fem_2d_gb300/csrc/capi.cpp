@@ -386,6 +386,14 @@ int fem2d_ctx_profile_flops(const fem2d_ctx* c, const char* region, double* flop
   API_END
 }
 
+int fem2d_ctx_mma_ns(fem2d_ctx* c, int n, double* ns) {
+  API_BEGIN
+  if (!c || !ns) fail(FEM2D_E_INVALID_ARG, "null argument");
+  FEM2D_CUDA(cudaSetDevice(c->c.device));
+  *ns = measure_mma_ns(c->c, n);
+  API_END
+}
+
 int fem2d_ctx_fp64_peak(fem2d_ctx* c, double* tflops) {
   API_BEGIN
   if (!c || !tflops) fail(FEM2D_E_INVALID_ARG, "null argument");

@@ -1064,6 +1064,52 @@ __global__ void __launch_bounds__(kSpThreads, 2)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kSpTmemCols) : "memory");
 }
 
+// The issue cost of tcgen05.mma (kind::f16, M = 128, K = 16) against N: one CTA per SM, thread 0 issues
+// `reps` MMAs on zero operands into two alternating accumulators and waits (bounded) for their commit;
+// the elapsed global time per MMA is written per CTA. The kernels above are shaped by this cost (one
+// MMA costs about the same for every N up to 64).
+__global__ void __launch_bounds__(128, 1) mma_cost_kernel(int N, int reps, unsigned long long* __restrict__ out,
+                                                          int* __restrict__ err) {
+  __shared__ __align__(1024) uint8_t A[128 * 16 * 2];
+  __shared__ __align__(1024) uint8_t B[256 * 16 * 2];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t slot;
+  for (int t = threadIdx.x; t < 128 * 16; t += 128) reinterpret_cast<uint16_t*>(A)[t] = 0;
+  for (int t = threadIdx.x; t < 256 * 16; t += 128) reinterpret_cast<uint16_t*>(B)[t] = 0;
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_addr(&slot)) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = slot;
+  if (threadIdx.x == 0) {
+    // A: 128 rows x 16 K (row groups 256 bytes apart), B: N rows x 16 K
+    const uint64_t da = smem_desc(smem_addr(A), 128, 256), db = smem_desc(smem_addr(B), 128, 256);
+    const uint32_t idesc = instr_desc(128, N);
+    uint32_t ph = 0;
+    for (int pass = 0; pass < 2; pass++) {   // the first pass warms the pipe up
+      const uint64_t t0 = global_ns();
+      for (int r = 0; r < reps; r++) mma_bf16(tmem + (uint32_t)((r & 1) * 256), da, db, idesc, 1u);
+      mma_commit(smem_addr(&bar));
+      if (!mbar_wait(smem_addr(&bar), ph)) atomicOr(err, 1);
+      ph ^= 1u;
+      if (pass == 1) out[blockIdx.x] = global_ns() - t0;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
 std::mutex g_attr_mu;
 bool g_attr_done[256] = {};
 
@@ -1258,6 +1304,29 @@ void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
   ozaki_reduce_kernel<<<(a * b + 255) / 256, 256, 0, c.stream>>>(work, nrb, ny, a, b, C);
   FEM2D_CUDA(cudaGetLastError());
   c.launches += 2;
+}
+
+
+double measure_mma_ns(Ctx& c, int n) {
+  if (n < 16 || n > 256 || n % 16 != 0) fail(FEM2D_E_INVALID_ARG, "MMA cost: N must be a multiple of 16 in 16..256");
+  const int reps = 4096;
+  DBuf<unsigned long long> out;
+  DBuf<int> err;
+  out.alloc(c.num_sms);
+  err.alloc(1);
+  FEM2D_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), c.stream));
+  mma_cost_kernel<<<c.num_sms, 128, 0, c.stream>>>(n, reps, out.p, err.p);
+  FEM2D_CUDA(cudaGetLastError());
+  c.launches++;
+  std::vector<unsigned long long> h(c.num_sms);
+  int he = 0;
+  FEM2D_CUDA(cudaMemcpyAsync(h.data(), out.p, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.stream));
+  FEM2D_CUDA(cudaMemcpyAsync(&he, err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  FEM2D_CUDA(cudaStreamSynchronize(c.stream));
+  if (he) fail(FEM2D_E_TIMEOUT, "MMA cost kernel: a bounded wait expired");
+  double ns = 0.0;
+  for (unsigned long long v : h) ns += (double)v;
+  return ns / h.size() / reps;
 }
 
 }  // namespace fem2d

@@ -25,6 +25,10 @@ void ozaki_gram(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const do
 void ozaki_gemm(Ctx& c, int64_t n, const double* X, int64_t ldx, int a, const double* C, int b, double alpha,
                 double beta, double* Z, int64_t ldz, int* rowexp /* n ints of scratch */, int* err);
 
+// measured issue cost (ns per instruction and SM) of tcgen05.mma kind::f16 with M = 128, K = 16 and the
+// given N (16..256, multiple of 16)
+double measure_mma_ns(Ctx& c, int n);
+
 // Y = coef M X for a matrix M = ca A + cb B of a pencil (its values sliced once into digit planes: a
 // slot), X and Y row-major n x nb (nb <= 32); every row of Y is written (overwritten), bitwise
 // reproducibly. Built per pattern (row runs of at most 64 rows with one column list, 64-column items),

@@ -132,6 +132,10 @@ int fem2d_ctx_profile_flops(const fem2d_ctx* c, const char* region, double* flop
 /* measured FP64 FMA throughput of this device (TFLOP/s): independent fused multiply-add chains on every
  * SM for about 20 ms; the denominator of the FP64-bound kernels' roofline (no reference counterpart) */
 int fem2d_ctx_fp64_peak(fem2d_ctx* c, double* tflops);
+/* measured issue cost of one tcgen05.mma (kind::f16, M = 128, K = 16) with the given N (a multiple of 16
+ * in 16..256), in ns per instruction and SM: the cost model behind the shapes of the tensor-core FP64
+ * emulation (no reference counterpart). FEM2D_E_TIMEOUT if the kernel's bounded wait expired. */
+int fem2d_ctx_mma_ns(fem2d_ctx* c, int n, double* ns);
 
 /* ---------------- Galerkin sampling (src/fem_problem/galerkin.rs:33-187) ---------------- */
 /* galerkin_sample_gep_hcurl::<BSpace, CurlCurl, L2Inner>(&domain, Some([nq_u, nq_v])).

@@ -135,3 +135,15 @@ def test_tensor_spmm_against_fp64(ctx, which):
         absref = 2.0 * (abs(M) @ np.abs(X))
         assert np.all(np.isfinite(Y))
         assert np.max(np.abs(Y - ref) / np.maximum(absref, 1e-300)) < 1e-13
+
+
+def test_mma_issue_cost(ctx):
+    """The measured issue cost of tcgen05.mma (M = 128, K = 16) is positive, does not fall as N grows,
+    and an MMA with N = 256 does at least twice the work per ns of one with N = 32 (the shapes of the
+    tensor-core kernels rest on this)."""
+    c = {n: ctx.mma_ns(n) for n in (32, 64, 256)}
+    assert all(v > 0 for v in c.values())
+    assert c[256] >= 0.9 * c[32]
+    assert (256 / c[256]) >= 2.0 * (32 / c[32])
+    with pytest.raises(fg.Fem2dError):
+        ctx.mma_ns(24)
