@@ -400,7 +400,8 @@ def run_native(args, ws, rank, local):
         gep.recompute()
         ta = ctx.timer_stop()
         ctx.timer_start()
-        res = fg.gpu_solve_gep_n(gep, w.target, w.n_pairs, dense=args.dense, refine=args.refine)
+        res = fg.gpu_solve_gep_n(gep, w.target, w.n_pairs, dense=args.dense, refine=args.refine,
+                                 krylov_steps=args.krylov_steps, block=args.block)
         te = ctx.timer_stop()
         return ta, te, res
 
@@ -441,7 +442,8 @@ def run_native(args, ws, rank, local):
         t1 = time.perf_counter()
         g2 = fg.galerkin_sample_gep_hcurl(bs, fg.CurlCurl, fg.L2Inner, d2, list(w.glq), ctx=ctx)
         t2 = time.perf_counter()
-        r2 = fg.gpu_solve_gep_n(g2, w.target, w.n_pairs, dense=args.dense, refine=args.refine)
+        r2 = fg.gpu_solve_gep_n(g2, w.target, w.n_pairs, dense=args.dense, refine=args.refine,
+                                krylov_steps=args.krylov_steps, block=args.block)
         t3 = time.perf_counter()
         e2e_ms += 1e3 * (t3 - t0)
         tg = g2.timings()
@@ -661,6 +663,9 @@ def main():
     ap.add_argument("--refine", type=int, default=0,
                     help="FP64 refinement steps per exact shifted solve (fem2d_solve_opts.refine): 0 calibrated "
                          "(default), k > 0 fixed, -1 none")
+    ap.add_argument("--krylov-steps", type=int, default=0,
+                    help="block Krylov steps per restart cycle (fem2d_solve_opts.krylov_steps), 0 = default")
+    ap.add_argument("--block", type=int, default=0, help="eigensolver block size (fem2d_solve_opts.block), 0 = default")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true")

@@ -717,11 +717,16 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   setup_gemm_smem(c.device);
   enable_stream_pool(c.device);
   const int64_t n = h.n;
-  const int guard = std::max(4, k / 2);
+  // From kDeepN DoFs the cycles are deeper with a small guard block (5 Krylov steps, b = k + 4): on the
+  // full-form meshes of 160k and 1.07M DoFs (HierPoly and KOLeg) this took 3-5 cycles instead of 5-8
+  // and 13-25% less time; below, the guard of k / 2 and 4 steps are kept.
+  constexpr int64_t kDeepN = 100000;
+  const bool deep = n >= kDeepN;
+  const int guard = deep ? 4 : std::max(4, k / 2);
   int b = o.block > 0 ? o.block : std::min<int64_t>(k + guard, n);
   if (b < k) b = k;
   if (b > 32) fail(FEM2D_E_INVALID_ARG, "block size above 32 (n_pairs too large for one block)");
-  const int steps = o.krylov_steps > 0 ? std::min(o.krylov_steps, 8) : 4;
+  const int steps = o.krylov_steps > 0 ? std::min(o.krylov_steps, 8) : (deep ? 5 : 4);
   // basis columns: the Krylov space of a cycle, and room for up to 32 locked pairs, a 32-column active
   // block and its first expansion (96) whatever the block size
   const int mmax = std::max(b * (steps + 1), 96);

@@ -8,6 +8,10 @@
 // over the inner Elem's dyadic sub-interval) and of the inner Elem. The kernels evaluate exactly
 // that product, in FP64, for each CSR entry.
 #pragma once
+#include <stdlib.h>
+#include <sys/mman.h>
+
+#include <new>
 #include <cstdint>
 #include <memory>
 #include <type_traits>
@@ -49,6 +53,25 @@ struct NoInitAlloc : std::allocator<T> {
   void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) { ::new ((void*)p) U; }
   template <class U, class... Args>
   void construct(U* p, Args&&... args) { ::new ((void*)p) U(std::forward<Args>(args)...); }
+  // large arrays (hundreds of MB at 1M DoFs) are first touched by the parallel fill passes: ask for
+  // transparent huge pages so that first touch costs far fewer page faults
+  static constexpr size_t kLarge = size_t(64) << 20;
+  T* allocate(size_t n) {
+    const size_t bytes = n * sizeof(T);
+    if (bytes >= kLarge) {
+      void* p = nullptr;
+      if (posix_memalign(&p, size_t(2) << 20, bytes) == 0) {
+        madvise(p, bytes, MADV_HUGEPAGE);
+        return static_cast<T*>(p);
+      }
+      throw std::bad_alloc();
+    }
+    return std::allocator<T>::allocate(n);
+  }
+  void deallocate(T* p, size_t n) {
+    if (n * sizeof(T) >= kLarge) free(p);
+    else std::allocator<T>::deallocate(p, n);
+  }
 };
 template <class T>
 using HostVec = std::vector<T, NoInitAlloc<T>>;

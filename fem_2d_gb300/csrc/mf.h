@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <vector>
 
+#include "gep.h"
+
 namespace fem2d {
 
 struct Domain;
@@ -29,8 +31,8 @@ struct MFSymbolic {
   int64_t mat_total = 0;
   // assembly from the CSR: (front-local row*f + col, csr index), grouped per front
   std::vector<int64_t> asm_ptr;
-  std::vector<int64_t> asm_pos;           // row * f + col
-  std::vector<int64_t> asm_csr;
+  HostVec<int64_t> asm_pos;               // row * f + col (written in full by the fill pass: no zeroing)
+  HostVec<int64_t> asm_csr;
   // extend-add of each front's Schur complement into its parent: positions of struct(C) in F_parent
   std::vector<int64_t> ea_ptr;            // per front
   std::vector<int32_t> ea_map;

@@ -272,9 +272,11 @@ typedef struct fem2d_solve_opts {
   int max_inner;        /* iterations per inner CG / MINRES solve (precond 1, 2), 0 = default 5000 */
   double tol;           /* relative residual ||Ax - lambda Bx|| / (|lambda| ||Bx||), 0 = default 1e-10 */
   double inner_tol;     /* relative residual of each inner solve (precond 1, 2), 0 = default 1e-10 */
-  int block;            /* block size, 0 = default (n_pairs + guard) */
+  int block;            /* block size, 0 = default (n_pairs + guard: guard = 4 from 100,000 DoFs, else
+                           max(4, n_pairs / 2)) */
   int verbose;
-  int krylov_steps;     /* block Krylov steps per restart cycle (at most 8), 0 = default 4 */
+  int krylov_steps;     /* block Krylov steps per restart cycle (at most 8), 0 = default (5 from 100,000
+                           DoFs, else 4) */
   double damping;       /* null-space damping c / |sigma| of T = (A - sigma B)^-1 A (A + c B)^-1 B,
                            0 = default (1 from 10,000 DoFs, 0.05 below) */
   int scaling;          /* 0 = automatic (row-run blocks from 10,000 DoFs; below, Jacobi, switching to
