@@ -598,7 +598,7 @@ def run_native_batch(args, ws, rank, local):
         r = fg.gep_batch_recompute(geps, ctx=ctx)
         ctx.synchronize()
         ta = time.perf_counter()
-        res = fg.gpu_solve_gep_batch(geps, 10.0, 4, workers=workers)
+        res = fg.gpu_solve_gep_batch(geps, 10.0, 4, workers=workers, dense=args.dense, refine=args.refine)
         return r, res, ta
 
     for _ in range(args.warmup):

@@ -820,10 +820,10 @@ def gpu_solve_gep_n(gep, target_eigenvalue, n_pairs, precond=0, tol=0.0, max_out
                     max_inner=0, inner_tol=0.0, block=0, verbose=0, ctx=None, krylov_steps=0, damping=0.0, scaling=0,
                     dense=0, net=None, refine=0):
     """The n_pairs eigenpairs nearest target by the device shift-invert solver (on ctx's stream; default:
-    the context the GEP was built on). dense=0 (default) runs the Gram products and block updates, and from
-    1,000,000 nonzeros the operator products, on the tensor cores (FP64 emulation); dense=1 keeps everything on
-    the FP64 CUDA cores; dense=2 uses the tensor-core operator products at every size; dense=3 keeps the operator
-    products on the FP64 CUDA cores. precond: PRECOND_EXACT (multifrontal LU, default), PRECOND_PLAIN
+    the context the GEP was built on). dense=0 (default) runs the Gram products and block updates from 50,000
+    DoFs, and the operator products from 1,000,000 nonzeros, on the tensor cores (FP64 emulation); dense=1 keeps
+    everything on the FP64 CUDA cores; dense=2 uses the tensor cores for all of them at every size; dense=3 uses
+    them for the Gram products and block updates at every size and keeps the operator products on the CUDA cores. precond: PRECOND_EXACT (multifrontal LU, default), PRECOND_PLAIN
     (inner CG / MINRES with the additive-Schwarz preconditioner) or PRECOND_LEARNED (the same with the
     two-level preconditioner of the trained PatchNet `net`)."""
     ctx = ctx or gep.ctx

@@ -832,7 +832,12 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   double inner_worst = 0.0;
 
   Dev D{c, h, d, sa.p, sb.p};
-  D.dense_mode = o.dense == 1 ? 1 : 0;   // 3: tensor Gram products and block updates, FP64 operator products
+  // Gram products and block updates on the tensor cores by default from kTensorDenseN rows: below, their
+  // fixed costs (exponent pre-passes, one CTA per SM) outweigh the FP64 work (256 concurrent small solves
+  // of the batching family: 1.51 s per step on the FP64 kernels against 1.74 s); dense = 2 and 3 use
+  // them at every size
+  constexpr int64_t kTensorDenseN = 50000;
+  D.dense_mode = (o.dense == 1 || (o.dense == 0 && n < kTensorDenseN)) ? 1 : 0;
   DBuf<double> V, AV, BV, X, AX, BX, G0, W1, W2, W3;
   V.alloc_on((size_t)n * mmax, c.stream);
   AV.alloc_on((size_t)n * mmax, c.stream);

@@ -283,13 +283,13 @@ typedef struct fem2d_solve_opts {
                            row-run blocks when the Jacobi-scaled factorizations are inaccurate),
                            1 = Jacobi only, 2 = row-run blocks (Cholesky factors of B's diagonal blocks
                            over runs of rows with one column list) */
-  int dense;            /* the eigensolver's FP64 contractions: 0 = default: Gram products and block
-                           updates of the B-orthogonalisation and Rayleigh-Ritz steps emulated on the
-                           tensor cores (tcgen05, exact integer slicing), and from 1,000,000 nonzeros the
-                           operator products with A or B alone as well; 1 = everything on the FP64 CUDA
-                           cores; 2 = as 0 with the tensor-core operator products at every size;
-                           3 = tensor-core Gram products and block updates, operator products on the
-                           FP64 CUDA cores */
+  int dense;            /* the eigensolver's FP64 contractions: 0 = default: from 50,000 DoFs the Gram
+                           products and block updates of the B-orthogonalisation and Rayleigh-Ritz steps
+                           emulated on the tensor cores (tcgen05, exact integer slicing), and from
+                           1,000,000 nonzeros the operator products as well; below, FP64 CUDA cores;
+                           1 = everything on the FP64 CUDA cores; 2 = everything on the tensor cores at
+                           every size; 3 = tensor-core Gram products and block updates at every size,
+                           operator products on the FP64 CUDA cores */
   const fem2d_patchnet* net;   /* trained patch network (precond 2), else NULL */
   int refine;           /* FP64 iterative-refinement steps per exact shifted solve: 0 = calibrated on a random
                            block (default: none when the solves are backward stable, normwise backward

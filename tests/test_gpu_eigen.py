@@ -73,12 +73,14 @@ def test_gpu_solve_kat_slepc_problem(kat, ctx):
     assert pair.residual < 1e-9
 
 
-@pytest.mark.parametrize("seed,k", [(0, 6), (2, 10)])
-def test_gpu_solve_against_lapack(oracle_lib, ctx, seed, k):
+@pytest.mark.parametrize("seed,k,dense", [(0, 6, 0), (2, 10, 0), (2, 10, 2)])
+def test_gpu_solve_against_lapack(oracle_lib, ctx, seed, k, dense):
+    """dense = 2 runs every contraction on the tensor cores at this small size (the default keeps the
+    FP64 kernels below 50,000 DoFs)."""
     ref = oracle_lib
     w = configs.precision(seed=seed, nx=4, ny=2)
     gep = _gep(w.mesh_json, w.ops, w.basis, w.glq, ctx)
-    res = fg.gpu_solve_gep_n(gep, w.target, k)
+    res = fg.gpu_solve_gep_n(gep, w.target, k, dense=dense)
     A, B = gep.scipy()
     wd, vd = ref.dense_nearest_physical(A, B, w.target, k)
     assert np.max(np.abs(res.values - wd) / np.abs(wd)) <= EIG_TOL
