@@ -893,6 +893,10 @@ __global__ void __launch_bounds__(kSpThreads, 2)
 #pragma unroll
   for (int o = 0; o < 8; o++) acc[o] = 0.0;
 
+  // threads 0..63 hold the next item's record one iteration ahead, so the loads it addresses (column
+  // indices, row exponents) start at the top of an iteration and are consumed after its gathers
+  TcSpmmItem wn_next{};
+  if (tid < 64 && i0 + 1 < i1) wn_next = items[i0 + 1];
   for (int idx = i0, k = 0; idx < i1; idx++, k++) {
     const TcSpmmItem w = items[idx];
     const bool more = idx + 1 < i1;
@@ -906,12 +910,14 @@ __global__ void __launch_bounds__(kSpThreads, 2)
     }
     // the next item's column indices (used after this item's gathers for an L2 prefetch of its rows of
     // X, and by its own gathers), exponent slots of the other parity
-    int nc = -1;
+    int nc = -1, emv = 0;
+    TcSpmmItem wn_after{};
     if (more && tid < 64) {
-      const TcSpmmItem wn = items[idx + 1];
+      const TcSpmmItem wn = wn_next;
       nc = tid < wn.Lc ? __ldg(col + wn.cbase + tid) : -1;
+      emv = tid < wn.R ? __ldg(ex + wn.eoff + tid) : 0;
       ecol[32 * ((k + 1) & 1) + (tid & 31)] = 0;
-      em[64 * ((k + 1) & 1) + tid] = tid < wn.R ? ex[wn.eoff + tid] : 0;
+      if (idx + 2 < i1) wn_after = items[idx + 2];
     }
     sp_stage_x(cq + 64 * (k & 1), X, ldx, nb, packed, xs, ecs);
     if (nc >= 0) {
@@ -919,7 +925,11 @@ __global__ void __launch_bounds__(kSpThreads, 2)
       asm volatile("prefetch.global.L2 [%0];" ::"l"(xr));
       if (nb > 16) asm volatile("prefetch.global.L2 [%0];" ::"l"(xr + 16));
     }
-    if (more && tid < 64) cq[64 * ((k + 1) & 1) + tid] = nc;
+    if (more && tid < 64) {
+      cq[64 * ((k + 1) & 1) + tid] = nc;
+      em[64 * ((k + 1) & 1) + tid] = emv;
+      wn_next = wn_after;
+    }
     // the X planes (generic stores) are visible to the tensor core's async proxy
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -969,7 +979,8 @@ __global__ void __launch_bounds__(kSpThreads, 2)
     }
     // readout into the M buffer (its planes are consumed): per lane (group g, column j) the exact int64
     // digit sums T_hi = sum_{g<4} D_g 2^(7 (3 - g)), T_lo = sum_{g>=4} D_g 2^(7 (7 - g)), one partial per
-    // warp; D_g < 8 * 64 * 127^2 < 2^23, so the partials stay below 2^46
+    // warp; D_g < 8 * 64 * 127^2 < 2^23, so the partials stay below 2^46. Lanes stay in integers: the FP64
+    // conversion is done once per output by its owner (GB300's FP64 pipe is the scarce unit)
     long long* PH = reinterpret_cast<long long*>(ms);
     long long* PL = PH + 4096;
     const int rounds = packed ? 1 : nrb;
