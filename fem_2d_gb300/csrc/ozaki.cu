@@ -157,6 +157,28 @@ __device__ __forceinline__ double pow2(int e) {
   return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// The two exact digit-sum halves T_hi (groups 0..3) and T_lo (groups 4..7, in units of 2^-28 of T_hi's)
+// as one integer in units of 2^-SH of T_hi's: T_hi 2^SH + T_lo 2^(SH - 28) rounded to the nearest
+// integer. The rounding error is at most 2^-(SH + 1) of a unit of T_hi, below one dropped digit pair
+// (s + t >= 8) of a single product. The combination is integer work (GB300's FP64 pipe is the scarce
+// unit): one int64 -> FP64 conversion per output follows. Each caller picks SH from its own bound on
+// |T_hi| so that the result stays below 2^63: the Gram chunk and the operator-product item (|T_hi| < 2^42)
+// take SH = 20, the block update (two chunks of K, |T_hi| < 2^43) SH = 19; |T_lo| < 2^46 everywhere.
+template <int SH>
+__device__ __forceinline__ long long fuse_digit_sums(long long th, long long tl) {
+  return (long long)((unsigned long long)th << SH) + ((tl + (1ll << (27 - SH))) >> (28 - SH));
+}
+constexpr int kFuseGram = 20, kFuseGemm = 19, kFuseSpmm = 20;
+
+// a 2^k, exact, by an integer add to a's exponent field when a and the result are normal; otherwise by
+// an FP64 multiply
+__device__ __forceinline__ double scale_pow2(double a, int k) {
+  const long long bits = __double_as_longlong(a);
+  const int e = (int)((bits >> 52) & 0x7FF);
+  if (e != 0 && e + k >= 1 && e + k <= 2046) return __longlong_as_double(bits + ((long long)k << 52));
+  return a * pow2(k);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&h);
@@ -218,6 +240,10 @@ __global__ void __launch_bounds__(kGramThreads, 2)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // the digit planes of X start zeroed: rows of the tile past column a of X are never written again
+  for (int t = tid; t < kDigits * kPlaneA / 16; t += kGramThreads)
+    reinterpret_cast<uint4*>(sA)[t] = make_uint4(0, 0, 0, 0);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -233,6 +259,8 @@ __global__ void __launch_bounds__(kGramThreads, 2)
 
   const int my_col = col0 + row;   // this thread's column of X (its row of C)
   const bool col_ok = my_col < a;
+  // warps whose 32 rows of the tile all lie past column a of X skip their loads, slicing and readout
+  const bool xw = col0 + 32 * (warp & 3) < a;
   const int yj = tid % kN, ykg = tid / kN;   // threads 0..127: a column of Y and its 8-row group
   const bool y_ok = tid < kN * (kSub / 8) && cy0 + yj < b;
 
@@ -246,10 +274,12 @@ __global__ void __launch_bounds__(kGramThreads, 2)
       const int64_t s0 = c0 + sb * kSub + half * (kSub / 2);
       // this thread's 16 rows of the sub-block, loaded before waiting on the previous MMAs
       double xv[kSub / 2], yv[8];
+      if (xw) {
 #pragma unroll
-      for (int r = 0; r < kSub / 2; r++) {
-        const int64_t ra = s0 + r;
-        xv[r] = (col_ok && ra < r1) ? __ldg(X + ra * ldx + my_col) : 0.0;
+        for (int r = 0; r < kSub / 2; r++) {
+          const int64_t ra = s0 + r;
+          xv[r] = (col_ok && ra < r1) ? __ldg(X + ra * ldx + my_col) : 0.0;
+        }
       }
 #pragma unroll
       for (int r = 0; r < 8; r++) {
@@ -267,6 +297,7 @@ __global__ void __launch_bounds__(kGramThreads, 2)
       }
 #pragma unroll
       for (int kh = 0; kh < kSub / 16; kh++) {
+        if (!xw) break;
         const int kg = half * (kSub / 16) + kh;
         uint32_t pk[kDigits][4];
 #pragma unroll
@@ -341,10 +372,12 @@ __global__ void __launch_bounds__(kGramThreads, 2)
     // combine the eight exact digit-sum accumulators of this chunk (this thread's row and column half,
     // 8 columns at a time). acc_g <= (g + 1) 128 127^2 < 2^24; in int64, exactly,
     //   T_hi = sum_{g<4} acc_g 2^(7 (3 - g)) < 2^43,   T_lo = sum_{g>=4} acc_g 2^(7 (7 - g)) < 2^47,
-    // and the chunk's contribution is (T_hi + T_lo 2^-28) 2^-35 2^(Ex - 1022) 2^(Ey - 1022)
+    // and the chunk's contribution is (T_hi + T_lo 2^-28) 2^-35 2^(Ex - 1022) 2^(Ey - 1022), taken as
+    // fuse_digit_sums(T_hi, T_lo) 2^-20 2^-35 2^(Ex - 1022) 2^(Ey - 1022): one conversion and one FMA
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
 #pragma unroll
     for (int cb = 0; cb < kHalf; cb += 8) {
+      if (!xw) break;
       const int jc = half * kHalf + cb;   // first column of this group in the C tile
       long long Th[8], Tl[8];
 #pragma unroll
@@ -362,10 +395,9 @@ __global__ void __launch_bounds__(kGramThreads, 2)
         }
       }
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
-        acc[cb + q] = fma(t, pow2(Ex + eY[jc + q] - 2044 - 35), acc[cb + q]);
-      }
+      for (int q = 0; q < 8; q++)
+        acc[cb + q] = fma((double)fuse_digit_sums<kFuseGram>(Th[q], Tl[q]),
+                          pow2(Ex + eY[jc + q] - 2044 - 35 - kFuseGram), acc[cb + q]);
     }
     // every thread's TMEM reads are complete before the next chunk's MMAs overwrite the accumulators
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -642,14 +674,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
     if (failed) break;
     if (row_ok) {
+      // one conversion and one multiply (or FMA) per output: alpha and the power-of-two scale are
+      // combined exactly in the exponent field
       double* zr = Z + row * ldz + half * (kN / 2);
 #pragma unroll
       for (int q = 0; q < kN / 2; q++) {
         const int j = half * (kN / 2) + q;
         if (j >= b) break;
-        const double t = fma((double)Tl[q], 0x1p-28, (double)Th[q]);
-        const double v = alpha * (t * pow2(Ex + eC[j] - 2044 - 35));
-        zr[q] = beta == 0.0 ? v : fma(beta, zr[q], v);
+        const double t = (double)fuse_digit_sums<kFuseGemm>(Th[q], Tl[q]);
+        const double m = scale_pow2(alpha, Ex + eC[j] - 2044 - 35 - kFuseGemm);
+        zr[q] = beta == 0.0 ? t * m : fma(t, m, beta == 1.0 ? zr[q] : beta * zr[q]);
       }
     }
   }
@@ -1045,8 +1079,7 @@ __global__ void __launch_bounds__(kSpThreads, 2)
           th = PH[e] + PH[1024 + e] + PH[2048 + e] + PH[3072 + e];
           tl = PL[e] + PL[1024 + e] + PL[2048 + e] + PL[3072 + e];
         }
-        const double t = fma((double)tl, 0x1p-28, (double)th);
-        acc[o] = fma(t, pow2(ecs[j] + ems[i] - 2044 - 35), acc[o]);
+        acc[o] = fma((double)fuse_digit_sums<kFuseSpmm>(th, tl), pow2(ecs[j] + ems[i] - 2044 - 35 - kFuseSpmm), acc[o]);
       }
       if (rb + 1 < rounds) __syncthreads();
     }
