@@ -550,10 +550,15 @@ __device__ __forceinline__ void forward_small_front(int fr, const SolveArgs& a, 
   const int32_t* ipm = iperm + piv_off[fr];
   const double* A = F + d.off;
   gather_front_rhs(d, fd, emap, ipm, W, woff, B, ldb, D, pm, nb, v);
-  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
-    const int i = t % p, c = t / p;
+  // the unit lower triangle: row i is a dot product of length i, so a thread takes the rows q and
+  // p - 1 - q (p - 1 terms together) and the lanes of a warp run equally long
+  const int hp = (p + 1) >> 1;
+  for (int t = threadIdx.x; t < hp * nb; t += blockDim.x) {
+    const int q = t % hp, c = t / hp;
     const double* vc = v + c * f;
-    y[c * p + i] = vc[i] + col_dot(A + i, f, vc, 0, i);
+    y[c * p + q] = vc[q] + col_dot(A + q, f, vc, 0, q);
+    const int i2 = p - 1 - q;
+    if (i2 != q) y[c * p + i2] = vc[i2] + col_dot(A + i2, f, vc, 0, i2);
   }
   __syncthreads();
   double* out = W + woff[fr];
@@ -607,10 +612,14 @@ __device__ __forceinline__ void backward_small_front(int fr, const SolveArgs& a,
     z[c * p + i] = v[(int64_t)c * f + i] - col_dot(A + (int64_t)p * f + i, f, xc, 0, s);
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < p * nb; t += blockDim.x) {
-    const int i = t % p, c = t / p;
+  // the upper triangle: row i is a dot product of length p - i; rows q and p - 1 - q share a thread
+  const int hp = (p + 1) >> 1;
+  for (int t = threadIdx.x; t < hp * nb; t += blockDim.x) {
+    const int q = t % hp, c = t / hp;
     const double* zc = z + c * p;
-    X[(int64_t)D[i] * ldx + c] = col_dot(A + i, f, zc, i, p);
+    X[(int64_t)D[q] * ldx + c] = col_dot(A + q, f, zc, q, p);
+    const int i2 = p - 1 - q;
+    if (i2 != q) X[(int64_t)D[i2] * ldx + c] = col_dot(A + i2, f, zc, i2, p);
   }
 }
 
@@ -1240,9 +1249,13 @@ void MFDevice::setup(Ctx& c, const MFSymbolic& s, int nb_max) {
                                     kSmallP * kSmallP * (int)sizeof(double)));
     FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
     FEM2D_CUDA(cudaFuncSetAttribute(mf_forward_small_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (kSmallF + kSmallP) * 32 * (int)sizeof(double)));
     FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kSmallF * 32 * (int)sizeof(double)));
+    FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmallF * 32 * (int)sizeof(double)));
     FEM2D_CUDA(cudaFuncSetAttribute(mf_backward_small_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     kSmallF * 32 * (int)sizeof(double)));
@@ -1364,6 +1377,16 @@ void MFDevice::factor(Ctx& c, const double* va, const double* vb, double ca, dou
   }
 }
 
+// Threads per front for a level of ns small fronts solved one CTA per front: a level that fits one
+// front per SM takes 1024 threads (one CTA per SM at 40 registers a thread), one that fits two fronts per
+// SM takes 512 (two CTAs per SM when their shared memory fits twice), wider levels 256. Narrow levels are
+// latency-bound within each front, so the threads a front gets set their time.
+static int small_threads(int ns, size_t smem, int num_sms) {
+  if (ns <= num_sms) return 1024;
+  if (ns <= 2 * num_sms && smem <= 100 * 1024) return 512;
+  return 256;
+}
+
 void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, double* X, int64_t ldx, int nb) {
   const DBuf<double>& Fbuf = fac.F;
   cudaStream_t st = c.stream;
@@ -1399,10 +1422,13 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)(level_small_f[l] + level_small_p[l]) * nb * sizeof(double);
+      const int nt = small_threads(ns, smem, c.num_sms);
       if (ns * CL <= 2 * c.num_sms)
         mf_forward_small_cluster_kernel<<<ns * CL, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
-      else if (2 * ns <= c.num_sms)
+      else if (nt == 1024)
         mf_forward_small_kernel<1024><<<ns, 1024, smem, st>>>(lsmall.p + small_ptr[l], a);
+      else if (nt == 512)
+        mf_forward_small_kernel<512><<<ns, 512, smem, st>>>(lsmall.p + small_ptr[l], a);
       else
         mf_forward_small_kernel<256><<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
       c.launches++;
@@ -1426,10 +1452,13 @@ void MFDevice::solve(Ctx& c, const MFFactor& fac, const double* B, int64_t ldb, 
     const int ns = small_ptr[l + 1] - small_ptr[l], nl = large_ptr[l + 1] - large_ptr[l];
     if (ns > 0) {
       const size_t smem = (size_t)level_small_f[l] * nb * sizeof(double);
+      const int nt = small_threads(ns, smem, c.num_sms);
       if (ns * CL <= 2 * c.num_sms)
         mf_backward_small_cluster_kernel<<<ns * CL, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
-      else if (2 * ns <= c.num_sms)
+      else if (nt == 1024)
         mf_backward_small_kernel<1024><<<ns, 1024, smem, st>>>(lsmall.p + small_ptr[l], a);
+      else if (nt == 512)
+        mf_backward_small_kernel<512><<<ns, 512, smem, st>>>(lsmall.p + small_ptr[l], a);
       else
         mf_backward_small_kernel<256><<<ns, 256, smem, st>>>(lsmall.p + small_ptr[l], a);
       c.launches++;
