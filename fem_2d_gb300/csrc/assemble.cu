@@ -27,7 +27,8 @@ __global__ void fem2d_contract1d_kernel(int basis, int P, int nivl, const double
   contract1d_table(basis, P, nivl, blockIdx.x, blockIdx.y, blockIdx.z, ivl, glq, nq_u, nq_v, tables);
 }
 
-__global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const int64_t* __restrict__ cptr,
+__global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const int32_t* __restrict__ fsrc,
+                                                           const int64_t* __restrict__ vptr,
                                                            const uint64_t* __restrict__ codes,
                                                            const GBlock* __restrict__ blocks,
                                                            const uint32_t* __restrict__ specs,
@@ -35,7 +36,8 @@ __global__ void __launch_bounds__(256) fem2d_values_kernel(int64_t nnz, const in
                                                            double* __restrict__ A, double* __restrict__ B) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
     double sa, sb;
-    entry_values(__ldg(cptr + e), __ldg(cptr + e + 1), codes, blocks, specs, tables, P, nivl, sa, sb);
+    const int64_t u = __ldg(fsrc + e);   // the upper entry whose visits this entry sums
+    entry_values(__ldg(vptr + u), __ldg(vptr + u + 1), codes, blocks, specs, tables, P, nivl, sa, sb);
     A[e] = sa;
     B[e] = sb;
   }
@@ -62,7 +64,8 @@ void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
   cudaStream_t s = c.stream;
   d.row_ptr.upload(g.row_ptr, s);
   d.col.upload(g.col, s);
-  d.cptr.upload(g.cptr, s);
+  d.vptr.upload(g.vptr, s);
+  d.fsrc.upload(g.fsrc, s);
   d.codes.upload(g.codes, s);
   d.blocks.upload(g.blocks, s);
   d.specs.upload(g.specs, s);
@@ -96,7 +99,7 @@ void device_upload(Ctx& c, const HostGEP& g, DeviceGEP& d) {
   d.gwork.upload(work, s);
   d.ngrp = (int)grp.size() - 1;
   d.nwork = (int)work.size();
-  d.h2d_bytes = (int64_t)(grp.size() * 4 + work.size() * 8 + g.row_ptr.size() * 8 + g.col.size() * 4 + g.cptr.size() * 8 + g.codes.size() * 8 +
+  d.h2d_bytes = (int64_t)(grp.size() * 4 + work.size() * 8 + g.row_ptr.size() * 8 + g.col.size() * 4 + g.vptr.size() * 8 + g.fsrc.size() * 4 + g.codes.size() * 8 +
                           g.blocks.size() * sizeof(GBlock) + g.specs.size() * 4 + iv.size() * 8 + q.size() * 8);
 }
 
@@ -114,12 +117,12 @@ void device_assemble(Ctx& c, const HostGEP& g, DeviceGEP& d, float* ms_tables, f
   c.launches++;
   FEM2D_CUDA(cudaEventRecord(e1, s));
   if (g.nnz_full > 0) {
-    ProfScope ps(c, "assembly_values", 16.0 * g.nnz_full + 8.0 * (g.nnz_full + 1) + 8.0 * g.codes.size());
+    ProfScope ps(c, "assembly_values", 20.0 * g.nnz_full + 8.0 * (g.nnz_upper + 1) + 8.0 * g.codes.size());
     const int threads = 256;
     int64_t want = (g.nnz_full + threads - 1) / threads;
     int64_t cap = (int64_t)c.num_sms * 8 * 4;   // persistent-ish grid: 8 blocks/SM x 4 waves
     int grid = (int)std::max<int64_t>(1, std::min(want, cap));
-    fem2d_values_kernel<<<grid, threads, 0, s>>>(g.nnz_full, d.cptr.p, d.codes.p, d.blocks.p, d.specs.p,
+    fem2d_values_kernel<<<grid, threads, 0, s>>>(g.nnz_full, d.fsrc.p, d.vptr.p, d.codes.p, d.blocks.p, d.specs.p,
                                                  d.tables.p, P, d.nivl, d.a.p, d.b.p);
     FEM2D_CUDA(cudaGetLastError());
     c.launches++;
@@ -198,8 +201,8 @@ void device_values_noalloc(Ctx& c, const HostGEP& g, const DeviceGEP& d, double*
     int64_t want = (g.nnz_full + threads - 1) / threads;
     int64_t cap = (int64_t)c.num_sms * 8 * 4;
     int grid = (int)std::max<int64_t>(1, std::min(want, cap));
-    fem2d_values_kernel<<<grid, threads, 0, c.stream>>>(g.nnz_full, d.cptr.p, d.codes.p, d.blocks.p, d.specs.p, tables,
-                                                        P, d.nivl, out_a, out_b);
+    fem2d_values_kernel<<<grid, threads, 0, c.stream>>>(g.nnz_full, d.fsrc.p, d.vptr.p, d.codes.p, d.blocks.p,
+                                                        d.specs.p, tables, P, d.nivl, out_a, out_b);
     FEM2D_CUDA(cudaGetLastError());
     c.launches++;
   }

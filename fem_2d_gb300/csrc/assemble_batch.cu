@@ -29,7 +29,8 @@ namespace fem2d {
 namespace {
 
 struct BatchItem {
-  const int64_t* cptr;
+  const int32_t* fsrc;
+  const int64_t* vptr;
   const uint64_t* codes;
   const GBlock* blocks;
   const uint32_t* specs;
@@ -66,10 +67,9 @@ __global__ void fem2d_values_batch_kernel(const BatchItem* __restrict__ items, c
     const int it = find_item(nnz_pref, count, e);
     const BatchItem& b = items[it];
     const int64_t local = e - __ldg(nnz_pref + it);
-    const int64_t* cptr = b.cptr;
+    const int64_t u = __ldg(b.fsrc + local);
     double sa, sb;
-    entry_values(__ldg(cptr + local), __ldg(cptr + local + 1), b.codes, b.blocks, b.specs, b.tables, b.P, b.nivl, sa,
-                 sb);
+    entry_values(__ldg(b.vptr + u), __ldg(b.vptr + u + 1), b.codes, b.blocks, b.specs, b.tables, b.P, b.nivl, sa, sb);
     b.A[local] = sa;
     b.B[local] = sb;
   }
@@ -111,7 +111,8 @@ void batch_assemble(Ctx& c, const std::vector<BatchMember>& members, bool autotu
     const HostGEP& h = *members[i].h;
     DeviceGEP& d = *members[i].d;
     BatchItem& b = items[i];
-    b.cptr = d.cptr.p;
+    b.fsrc = d.fsrc.p;
+    b.vptr = d.vptr.p;
     b.codes = d.codes.p;
     b.blocks = d.blocks.p;
     b.specs = d.specs.p;

@@ -110,8 +110,7 @@ __device__ __forceinline__ double curl2(V2 a) { return a.x * -1.0 + a.y * 1.0; }
 
 struct BPArgs {
   int64_t nu;
-  const int64_t* ufull;
-  const int64_t* cptr;
+  const int64_t* vptr;
   const uint64_t* codes;
   const GBlock* blocks;
   const double* braw;
@@ -233,12 +232,12 @@ __device__ void visit(const BPArgs& A, uint64_t code, double* out) {
 __global__ void __launch_bounds__(128) byparts_kernel(BPArgs A) {
   const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (u >= A.nu) return;
-  const int64_t e = A.ufull[u];
   double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int64_t c = A.cptr[e]; c < A.cptr[e + 1]; c++) {
+  const int64_t c0 = A.vptr[u], c1 = A.vptr[u + 1];
+  for (int64_t c = c0; c < c1; c++) {
     double v[6];
     visit(A, A.codes[c], v);
-    for (int t = 0; t < 6; t++) acc[t] = c == A.cptr[e] ? v[t] : acc[t] + v[t];
+    for (int t = 0; t < 6; t++) acc[t] = c == c0 ? v[t] : acc[t] + v[t];
   }
   for (int t = 0; t < 6; t++) A.out[u * 6 + t] = acc[t];
 }
@@ -273,16 +272,9 @@ void gep_by_parts(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* out6) {
         for (int a = 0; a < P; a++) tv[(((size_t)iv * kFam + f) * P + a) * Mv + n] = buf[f * P + a];
     }
   }
-  // the upper-triangle entries in (row, col) order, as full CSR positions
-  std::vector<int64_t> ufull;
-  ufull.reserve(h.nnz_upper);
-  for (int64_t r = 0; r < h.n; r++)
-    for (int64_t e = h.row_ptr[r]; e < h.row_ptr[r + 1]; e++)
-      if (h.col[e] >= r) ufull.push_back(e);
-  const int64_t nu = (int64_t)ufull.size();
-  DBuf<int64_t> uf;
+  // one result per upper-triangle entry, in (row, col) order: the GEP's visit lists are grouped by it
+  const int64_t nu = h.nnz_upper;
   DBuf<double> braw, tab_u, tab_v, wud, wvd, ivs, out;
-  uf.upload_on(ufull, c.stream);
   braw.upload_on(h.braw, c.stream);
   tab_u.upload_on(tu, c.stream);
   tab_v.upload_on(tv, c.stream);
@@ -290,7 +282,7 @@ void gep_by_parts(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* out6) {
   wvd.upload_on(wv, c.stream);
   ivs.upload_on(h.ivl_s, c.stream);
   out.alloc_on((size_t)std::max<int64_t>(nu, 1) * 6, c.stream);
-  BPArgs a{nu, uf.p, d.cptr.p, d.codes.p, d.blocks.p, braw.p, d.specs.p, ivs.p, tab_u.p, tab_v.p, wud.p, wvd.p,
+  BPArgs a{nu, d.vptr.p, d.codes.p, d.blocks.p, braw.p, d.specs.p, ivs.p, tab_u.p, tab_v.p, wud.p, wvd.p,
            Mu, Mv, P, out.p};
   if (nu > 0) {
     byparts_kernel<<<(unsigned)((nu + 127) / 128), 128, 0, c.stream>>>(a);

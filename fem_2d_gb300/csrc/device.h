@@ -132,8 +132,8 @@ struct DBuf {
 };
 
 struct DeviceGEP {
-  DBuf<int64_t> row_ptr, cptr;
-  DBuf<int32_t> col;
+  DBuf<int64_t> row_ptr, vptr;
+  DBuf<int32_t> col, fsrc;
   DBuf<uint64_t> codes;
   DBuf<GBlock> blocks;
   DBuf<uint32_t> specs;

@@ -4,8 +4,9 @@
 // its own spec list (local-local, diagonal included) and every (spec of E) x (spec of D) for each
 // descendant D of E in depth-first order. Each visit lands on the key (min dof, max dof) of the
 // upper triangle (sparse_matrix.rs:68-98) and collisions are summed. Here the visits are bucketed
-// by key row, sorted, and turned into a full symmetric CSR pattern plus, per CSR entry, the list of
-// visits that sum into it. The pattern is integer work and bit-exact with the reference's BTreeMap.
+// by key row, sorted, and turned into a full symmetric CSR pattern plus, per key (upper-triangle
+// entry), the list of visits that sum into it; each full entry names the key it mirrors. The pattern
+// is integer work and bit-exact with the reference's BTreeMap.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -272,8 +273,10 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   for (int64_t r = 0; r < n; r++) uptr[r + 1] = uptr[r] + ucnt[r];
   const int64_t nu = uptr[n];
   g.nnz_upper = nu;
+  if (nu >= (int64_t)INT32_MAX) fail(FEM2D_E_TOO_LARGE, "more than 2^31 - 1 upper-triangle entries");
   std::unique_ptr<int32_t[]> ucol(new int32_t[nu]);
-  std::unique_ptr<int64_t[]> uc0(new int64_t[nu + 1]);   // start of each upper entry's items (grouped by entry)
+  g.vptr.resize(nu + 1);
+  int64_t* uc0 = g.vptr.data();   // start of each upper entry's items (grouped by entry)
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
       int64_t u = uptr[r];
@@ -314,7 +317,8 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   const int64_t nf = g.row_ptr[n];
   g.nnz_full = nf;
   g.col.resize(nf);
-  std::unique_ptr<int64_t[]> src(new int64_t[nf]);
+  g.fsrc.resize(nf);
+  int32_t* src = g.fsrc.data();   // the upper entry of each full entry
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
       int64_t o = g.row_ptr[r];
@@ -332,7 +336,7 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
         if (ucol[u] != r) {
           const int64_t p = pos[ucol[u]]++;
           g.col[p] = (int32_t)r;
-          src[p] = u;
+          src[p] = (int32_t)u;
         }
   });
   parallel_for(n, [&](int64_t r0, int64_t r1) {
@@ -340,37 +344,15 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
       int64_t pos = g.row_ptr[r] + lcnt[r];
       for (int64_t u = uptr[r]; u < uptr[r + 1]; u++, pos++) {
         g.col[pos] = ucol[u];
-        src[pos] = u;
+        src[pos] = (int32_t)u;
       }
     }
   });
-  // visit lists per full entry: lengths, a two-pass parallel prefix sum, then the copies
-  g.cptr.resize(nf + 1);
-  g.cptr[0] = 0;
-  {
-    const int64_t chunk = (nf + nt - 1) / nt;
-    std::vector<int64_t> part(nt + 1, 0);
-    run_threads(nt, [&](int t) {
-      const int64_t e0 = std::min(nf, t * chunk), e1 = std::min(nf, e0 + chunk);
-      int64_t acc = 0;
-      for (int64_t e = e0; e < e1; e++) {
-        acc += uc0[src[e] + 1] - uc0[src[e]];
-        g.cptr[e + 1] = acc;
-      }
-      part[t + 1] = acc;
-    });
-    for (int t = 0; t < nt; t++) part[t + 1] += part[t];
-    run_threads(nt, [&](int t) {
-      const int64_t e0 = std::min(nf, t * chunk), e1 = std::min(nf, e0 + chunk);
-      for (int64_t e = e0; e < e1; e++) g.cptr[e + 1] += part[t];
-    });
-  }
-  g.codes.resize(g.cptr[nf]);
-  parallel_for(nf, [&](int64_t e0, int64_t e1) {
-    for (int64_t e = e0; e < e1; e++) {
-      int64_t o = g.cptr[e];
-      for (int64_t k = uc0[src[e]]; k < uc0[src[e] + 1]; k++) g.codes[o++] = items[k].code;
-    }
+  // the visit codes in upper-entry order: the items of upper entry u are items[uc0[u] .. uc0[u + 1]),
+  // already grouped and sorted, so the codes are a straight copy
+  g.codes.resize(V);
+  parallel_for(V, [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; k++) g.codes[k] = items[k].code;
   });
 }
 

@@ -85,9 +85,12 @@ struct HostGEP {
   // full symmetric CSR pattern (A and B share it)
   std::vector<int64_t> row_ptr;        // n + 1
   HostVec<int32_t> col;                // nnz_full
-  // per full entry, its contribution list (codes), in a fixed order
-  HostVec<int64_t> cptr;               // nnz_full + 1
-  HostVec<uint64_t> codes;
+  // contributions: per upper-triangle entry u (rows in order, columns ascending within a row) its visit
+  // codes codes[vptr[u] .. vptr[u + 1]) in a fixed order; per full entry the upper entry it mirrors
+  // (an entry (r, c) and its transpose (c, r) sum the same visits)
+  HostVec<int64_t> vptr;               // nnz_upper + 1
+  HostVec<int32_t> fsrc;               // nnz_full
+  HostVec<uint64_t> codes;             // visits
   // visit blocks, packed specs, intervals
   std::vector<GBlock> blocks;
   std::vector<double> braw;            // per block, 12 doubles of raw pair geometry (integrate_by_parts)
