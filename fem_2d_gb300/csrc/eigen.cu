@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <future>
 #include <cmath>
 #include <mutex>
 #include <numeric>
@@ -681,13 +682,17 @@ void random_block_device(Ctx& c, int64_t n, int b, uint64_t seed, double* out, i
 
 }  // namespace
 
-MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h) {
+MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h, std::unique_ptr<MFSymbolic> pre) {
   if (!p.ready || p.device != c.device) {
     p.ready = false;
     p.mf.reset();
-    p.sym.reset(new MFSymbolic);
-    if (p.dense) mf_symbolic_dense(h, *p.sym);
-    else mf_symbolic(dom, h, *p.sym, p.lift.empty() ? nullptr : &p.lift);
+    if (pre && !p.dense) {
+      p.sym = std::move(pre);   // computed ahead on a host thread
+    } else {
+      p.sym.reset(new MFSymbolic);
+      if (p.dense) mf_symbolic_dense(h, *p.sym);
+      else mf_symbolic(dom, h, *p.sym, p.lift.empty() ? nullptr : &p.lift);
+    }
     p.mf.reset(new MFDevice);
     p.mf->setup(c, *p.sym, 32);
     p.device = c.device;
@@ -773,6 +778,21 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
   }
   if (!plan.bsc) plan.bsc = std::make_unique<BlockScale>();
   BlockScale& bsc = *plan.bsc;
+  // precond 1 / 2: T's two shifted solves by preconditioned CG (A + c B) and MINRES (A - sigma B) with
+  // the plain additive-Schwarz preconditioner or the learned two-level one, instead of multifrontal LU
+  const bool iterative = o.precond == 1 || o.precond == 2;
+  // a plan still to be built: its symbolic analysis (host only, pattern only) runs on a host thread
+  // while the device computes the scaling below; the future is joined before the plan is set up, and
+  // on every exit path by its destructor
+  std::future<std::unique_ptr<MFSymbolic>> sym_job;
+  if (!iterative && !plan.dense && (!plan.ready || plan.device != c.device)) {
+    std::vector<uint8_t> lift = plan.lift;
+    sym_job = std::async(std::launch::async, [&dom, &h, lift]() {
+      auto s = std::make_unique<MFSymbolic>();
+      mf_symbolic(dom, h, *s, lift.empty() ? nullptr : &lift);
+      return s;
+    });
+  }
   bool blocked = false;
   if (o.scaling == 2 || (o.scaling == 0 && large)) {
     try {
@@ -787,12 +807,9 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       c.launches++;
     }
   }
-  // precond 1 / 2: T's two shifted solves by preconditioned CG (A + c B) and MINRES (A - sigma B) with
-  // the plain additive-Schwarz preconditioner or the learned two-level one, instead of multifrontal LU
-  const bool iterative = o.precond == 1 || o.precond == 2;
   if (o.precond == 2 && !net) fail(FEM2D_E_INVALID_ARG, "precond 2 (learned) needs a trained network");
   if (o.precond < 0 || o.precond > 2) fail(FEM2D_E_INVALID_ARG, "precond must be 0, 1 or 2");
-  MFDevice* M = iterative ? nullptr : &mf_plan(plan, c, dom, h);
+  MFDevice* M = iterative ? nullptr : &mf_plan(plan, c, dom, h, sym_job.valid() ? sym_job.get() : nullptr);
   MFFactor fm, fp;
   // A + c B (c > 0) is SPD: factored without pivoting. c = |sigma| by default from kLargeN DoFs: the null
   // space of the curl-curl operator, smeared by rounding to |lambda| <~ eps ||A|| / lambda_min(B) (which

@@ -246,7 +246,9 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   struct Item { int32_t col; uint64_t code; };
   // scratch arrays are left uninitialised (every element is written before it is read): zeroing them
   // would add a full serial pass over hundreds of MB at 1M DoFs
-  std::unique_ptr<Item[]> items(new Item[V]);
+  HostVec<Item> items_buf;   // huge-page backed above 64 MB (fewer first-touch faults)
+  items_buf.resize(V);
+  Item* items = items_buf.data();
   run_threads(nt, [&](int t) {
     std::vector<int64_t>& pos = tcnt[t];
     for (int64_t b = brange[t]; b < brange[t + 1]; b++)
@@ -260,8 +262,8 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   std::vector<int64_t> ucnt(n, 0);
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
-      Item* a = items.get() + bptr[r];
-      Item* z = items.get() + bptr[r + 1];
+      Item* a = items + bptr[r];
+      Item* z = items + bptr[r + 1];
       std::sort(a, z, [](const Item& x, const Item& y) { return x.col != y.col ? x.col < y.col : x.code < y.code; });
       int64_t u = 0;
       for (Item* it = a; it < z; it++)
@@ -274,7 +276,9 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   const int64_t nu = uptr[n];
   g.nnz_upper = nu;
   if (nu >= (int64_t)INT32_MAX) fail(FEM2D_E_TOO_LARGE, "more than 2^31 - 1 upper-triangle entries");
-  std::unique_ptr<int32_t[]> ucol(new int32_t[nu]);
+  HostVec<int32_t> ucol_buf;
+  ucol_buf.resize(nu);
+  int32_t* ucol = ucol_buf.data();
   g.vptr.resize(nu + 1);
   int64_t* uc0 = g.vptr.data();   // start of each upper entry's items (grouped by entry)
   parallel_for(n, [&](int64_t r0, int64_t r1) {

@@ -86,8 +86,9 @@ struct MFPlan {
   std::mutex mu;
 };
 
-// the plan's MFDevice, building the plan on first use (or after a device change)
-MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h);
+// the plan's MFDevice, building the plan on first use (or after a device change); `pre`, when given, is
+// the sparse symbolic analysis already computed for this GEP
+MFDevice& mf_plan(MFPlan& p, Ctx& c, const Domain& dom, const HostGEP& h, std::unique_ptr<MFSymbolic> pre = nullptr);
 // replace the plan by the dense single-front plan
 MFDevice& mf_plan_dense(MFPlan& p, Ctx& c, const HostGEP& h);
 
