@@ -85,8 +85,10 @@ __global__ void __launch_bounds__(256) run_cholinv_kernel(const int32_t* __restr
   for (int t = threadIdx.x; t < R * R; t += blockDim.x) out[t] = Li[(t / R) * kRun + t % R];
 }
 
-// per run g and each column run h of its pattern: block <- S_g block S_h^T, for A and B
-__global__ void __launch_bounds__(256) run_transform_kernel(const int32_t* __restrict__ grp,
+// per run g and each column run h of its pattern: block <- S_g block S_h^T, for A and B (256 threads)
+constexpr int kTransformThreads = 256;
+constexpr int kT1Regs = kRun * kRun / kTransformThreads;
+__global__ void __launch_bounds__(kTransformThreads) run_transform_kernel(const int32_t* __restrict__ grp,
                                                             const int64_t* __restrict__ rp,
                                                             const int64_t* __restrict__ seg_ptr,
                                                             const int2* __restrict__ seg,
@@ -97,9 +99,8 @@ __global__ void __launch_bounds__(256) run_transform_kernel(const int32_t* __res
                                                             double* __restrict__ sb) {
   extern __shared__ double smem[];
   double* Sg = smem;                    // R x R
-  double* Sh = Sg + kRun * kRun;        // H x H
-  double* Blk = Sh + kRun * kRun;       // R x H
-  double* T1 = Blk + kRun * kRun;       // R x H
+  double* ShT = Sg + kRun * kRun;       // H x H, transposed: ShT[k H + q] = S_h[q][k]
+  double* Blk = ShT + kRun * kRun;      // R x H: the block, then T1 = S_g Blk in its place
   const int g = blockIdx.x;
   const int g0 = grp[g], R = grp[g + 1] - g0;
   for (int t = threadIdx.x; t < R * R; t += blockDim.x) Sg[t] = S[soff[g] + t];
@@ -107,7 +108,9 @@ __global__ void __launch_bounds__(256) run_transform_kernel(const int32_t* __res
     const int2 sh = seg[sgi];   // (column run h, offset of its first column in the rows of g)
     const int h0 = grp[sh.x], H = grp[sh.x + 1] - h0;
     __syncthreads();
-    for (int t = threadIdx.x; t < H * H; t += blockDim.x) Sh[t] = S[soff[sh.x] + t];
+    // S_h is stored transposed so that the lanes of the second product (consecutive q) read consecutive
+    // doubles (row-major S_h would put all 32 lanes of a warp in one bank for H = 64)
+    for (int t = threadIdx.x; t < H * H; t += blockDim.x) ShT[(t % H) * H + t / H] = S[soff[sh.x] + t];
     for (int m = 0; m < 2; m++) {
       const double* src = m == 0 ? va : vb;
       double* dst = m == 0 ? sa : sb;
@@ -117,17 +120,31 @@ __global__ void __launch_bounds__(256) run_transform_kernel(const int32_t* __res
         Blk[t] = src[rp[g0 + r] + sh.y + q];
       }
       __syncthreads();
-      for (int t = threadIdx.x; t < R * H; t += blockDim.x) {   // T1 = S_g Blk (S_g lower)
-        const int r = t / H, q = t % H;
-        double s = 0.0;
-        for (int k = 0; k <= r; k++) s += Sg[r * R + k] * Blk[k * H + q];
-        T1[t] = s;
+      // T1 = S_g Blk (S_g lower), held in registers (at most 16 entries a thread: 64 x 64 over 256
+      // threads) and written over Blk once every thread has read it: two CTAs fit an SM
+      double t1[kT1Regs];
+#pragma unroll
+      for (int i = 0; i < kT1Regs; i++) {
+        const int t = threadIdx.x + kTransformThreads * i;
+        t1[i] = 0.0;
+        if (t < R * H) {
+          const int r = t / H, q = t % H;
+          double s = 0.0;
+          for (int k = 0; k <= r; k++) s += Sg[r * R + k] * Blk[k * H + q];
+          t1[i] = s;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < kT1Regs; i++) {
+        const int t = threadIdx.x + kTransformThreads * i;
+        if (t < R * H) Blk[t] = t1[i];
       }
       __syncthreads();
       for (int t = threadIdx.x; t < R * H; t += blockDim.x) {   // out = T1 S_h^T (S_h lower)
         const int r = t / H, q = t % H;
         double s = 0.0;
-        for (int k = 0; k <= q; k++) s += T1[r * H + k] * Sh[q * H + k];
+        for (int k = 0; k <= q; k++) s += Blk[r * H + k] * ShT[k * H + q];
         dst[rp[g0 + r] + sh.y + q] = s;
       }
     }
@@ -201,14 +218,14 @@ void BlockScale::build(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* sa,
       FEM2D_CUDA(cudaFuncSetAttribute(run_cholinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       2 * kRun * kRun * (int)sizeof(double)));
       FEM2D_CUDA(cudaFuncSetAttribute(run_transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      4 * kRun * kRun * (int)sizeof(double)));
+                                      3 * kRun * kRun * (int)sizeof(double)));
       attr[c.device] = true;
     }
   }
   run_cholinv_kernel<<<ngrp, 256, 2 * kRun * kRun * sizeof(double), c.stream>>>(grp_d.p, d.row_ptr.p, d.col.p, d.b.p,
                                                                                 soff.p, S.p, flag.p);
   c.launches++;
-  run_transform_kernel<<<ngrp, 256, 4 * kRun * kRun * sizeof(double), c.stream>>>(
+  run_transform_kernel<<<ngrp, kTransformThreads, 3 * kRun * kRun * sizeof(double), c.stream>>>(
       grp_d.p, d.row_ptr.p, seg_ptr.p, seg.p, soff.p, S.p, d.a.p, d.b.p, sa, sb);
   c.launches++;
   FEM2D_CUDA(cudaGetLastError());
