@@ -458,17 +458,28 @@ __host__ __device__ constexpr int gemm_smem(int kc, int stages) {
 // byte offset of core matrix (row group rg, k group kg) in a K-major tile with kc columns
 __device__ __forceinline__ int core_off_k(int rg, int kg, int kc) { return (rg * (kc / 8) + kg) * 128; }
 
-// E[r] = biased exponent of max |X[r][k]| over k < a: one warp per row, lanes across the row
+// E[r] = biased exponent of max |X[r][k]| over k < a: a warp takes 4 rows at a time (lanes across the
+// rows, four independent loads in flight per lane: the pass is bound by load latency)
+constexpr int kRowExpRows = 4;
 __global__ void __launch_bounds__(256) row_exp_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, int a,
                                                        int* __restrict__ E) {
   const int lane = threadIdx.x & 31;
-  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n;
-       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    int e = 0;
-    for (int k = lane; k < a; k += 32) e = max(e, biased_exp(__ldg(X + r * ldx + k)));
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * kRowExpRows; r0 < n;
+       r0 += nwarps * kRowExpRows) {
+    int e[kRowExpRows];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, off));
-    if (lane == 0) E[r] = e;
+    for (int u = 0; u < kRowExpRows; u++) e[u] = 0;
+    for (int k = lane; k < a; k += 32)
+#pragma unroll
+      for (int u = 0; u < kRowExpRows; u++)
+        if (r0 + u < n) e[u] = max(e[u], biased_exp(__ldg(X + (r0 + u) * ldx + k)));
+#pragma unroll
+    for (int u = 0; u < kRowExpRows; u++) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) e[u] = max(e[u], __shfl_xor_sync(0xffffffffu, e[u], off));
+      if (lane == 0 && r0 + u < n) E[r0 + u] = e[u];
+    }
   }
 }
 
