@@ -493,6 +493,13 @@ def run_native(args, ws, rank, local):
                 "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": f_hbm, "peak_source": peak_kind},
                 "fp64": {"achieved": tfl, "peak": fp64, "unit": "TFLOP/s", "frac": f_fp,
                          "peak_source": "measured (library FP64 FMA microbenchmark, this run)"}}
+        if reg == "rr_host":
+            # dense Rayleigh-Ritz on the host CPU: its FLOP rate is reported, no device roofline applies
+            base.update({"bound": "host", "achieved": tfl, "peak": None, "unit": "TFLOP/s", "frac": None,
+                         "note": "host CPU work (symmetric eigen-decompositions and products of the basis size)"})
+            base["fp64"]["frac"] = None
+            base["hbm"]["frac"] = None
+            return base
         if reg in ("gram_tc", "gemm_tc", "spmm_tc"):
             # FP64 emulated on the tensor cores: its FP64-equivalent rate is not bounded by the FP64 pipe;
             # the kernel streams its operands once, so HBM is its roofline (tensor-pipe use from ncu)

@@ -186,6 +186,8 @@ void BlockScale::build(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* sa,
     for (int g = 0; g < ngrp; g++) {
       const int R = grp[g + 1] - grp[g];
       so[g + 1] = so[g] + (int64_t)R * R;
+      alg_flops += (double)R * R * R;        // Cholesky (R^3 / 3 FMA) and inverse (R^3 / 6 FMA)
+      alg_bytes += 8.0 * 3.0 * R * R;        // B's diagonal block read, S_g written and read back
       const int64_t b = h.row_ptr[grp[g]], e = h.row_ptr[grp[g] + 1];
       int64_t q = b;
       while (q < e) {
@@ -195,6 +197,8 @@ void BlockScale::build(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* sa,
         if (h.col[q] != grp[hr] || q + H > e || h.col[q + H - 1] != grp[hr] + H - 1)
           fail(FEM2D_E_INVALID_ARG, "block scaling: a column run is split in a row pattern");
         sg.push_back(make_int2(hr, (int)(q - b)));
+        alg_flops += 2.0 * 2.0 * ((double)R * (R + 1) / 2.0 * H + (double)R * H * (H + 1) / 2.0);
+        alg_bytes += 8.0 * (double)H * H;   // S_h read for this block
         q += H;
       }
       sp[g + 1] = (int64_t)sg.size();
@@ -205,6 +209,7 @@ void BlockScale::build(Ctx& c, const HostGEP& h, const DeviceGEP& d, double* sa,
     seg_ptr.upload(sp, c.stream);
     seg.upload(sg, c.stream);
     S.alloc(std::max<int64_t>(so[ngrp], 1));
+    alg_bytes += 32.0 * (double)h.nnz_full;
     ready = true;
   }
   DBuf<int> flag;

@@ -68,6 +68,7 @@ struct ProfScope {
 struct HostScope {
   Ctx& c;
   const char* name;
+  double flops = 0.0;   // algorithmic FLOPs of the region, set by its owner before the scope ends
   std::chrono::steady_clock::time_point t0;
   HostScope(Ctx& ctx, const char* n) : c(ctx), name(n) {
     if (!c.profile) return;
@@ -78,6 +79,7 @@ struct HostScope {
     if (!c.profile) return;
     ProfRec& r = c.prof[name];
     r.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    r.flops += flops;
     r.count++;
   }
 };

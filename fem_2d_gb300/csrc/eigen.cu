@@ -799,6 +799,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       {
         ProfScope ps_bs(c, "block_scale", 0.0);
         bsc.build(c, h, d, sa.p, sb.p);
+        ps_bs.bytes = bsc.alg_bytes;
+        ps_bs.flops = bsc.alg_flops;
       }
       blocked = true;
     } catch (const Error&) {
@@ -949,6 +951,8 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
       {
         ProfScope ps_bs(c, "block_scale", 0.0);
         bsc.build(c, h, d, sa.p, sb.p);
+        ps_bs.bytes = bsc.alg_bytes;
+        ps_bs.flops = bsc.alg_flops;
       }
       blocked = true;
       factor_both();
@@ -1231,6 +1235,10 @@ void sparse_solve(Ctx& c, const Domain& dom, const HostGEP& h, const DeviceGEP& 
     for (int i = 0; i < ma; i++)
       for (int q = 0; q < nc; q++) Ysub[(size_t)i * nc + q] = Y[(size_t)i * m2 + order[q]];
     for (int q = 0; q < nc; q++) thc[q] = th[order[q]];
+    // the two dense products forming S and the Ritz vectors Y exactly, and 9 n^3 for each symmetric
+    // eigen-decomposition (the nominal count of a tridiagonal reduction with eigenvectors)
+    hs_rr->flops = 2.0 * ((double)ma * ma * m2 + (double)m2 * m2 * ma + (double)ma * m2 * m2) +
+                   9.0 * ((double)ma * ma * ma + (double)m2 * m2 * m2);
     hs_rr.reset();
     DBuf<double> AY, BY, XY, th_d, P;
     AY.alloc_on((size_t)n * nc, c.stream);
