@@ -99,8 +99,8 @@ def test_reference_arm_loads_no_product_library():
 
 
 def test_reference_arm_unavailable_line_from_fixture():
-    """At the full-form 1M workload the committed oracle fixture's single-step time rules out the
-    driver's step count: the arm prints one reasoned `unavailable` line and exits 0."""
+    """At the full-form 1M workload the committed oracle fixture's single-step time rules out a timed
+    run of W + K steps: the arm prints one reasoned `unavailable` line and exits 0."""
     if not os.path.exists(os.path.join(ROOT, "tests", "golden", "full_form_full_1m.json")):
         pytest.skip("full_1m oracle fixture not generated")
     r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "20", "--warmup", "5"],
