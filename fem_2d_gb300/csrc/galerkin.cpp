@@ -55,6 +55,30 @@ static void run_threads(int nt, F f) {
   for (auto& x : th) x.join();
 }
 
+// out[0] = 0, out[r + 1] = out[r] + term(r) for r < n: the terms in parallel, then a two-pass prefix
+// sum over contiguous chunks (the same integers as the serial loop)
+template <class F>
+static void parallel_prefix(int64_t n, int64_t* out, F term) {
+  out[0] = 0;
+  const int nt = (n < 65536 || num_host_threads() <= 1) ? 1 : num_host_threads();
+  const int64_t chunk = (n + nt - 1) / nt;
+  std::vector<int64_t> part(nt + 1, 0);
+  run_threads(nt, [&](int t) {
+    const int64_t r0 = std::min(n, t * chunk), r1 = std::min(n, r0 + chunk);
+    int64_t acc = 0;
+    for (int64_t r = r0; r < r1; r++) {
+      acc += term(r);
+      out[r + 1] = acc;
+    }
+    part[t + 1] = acc;
+  });
+  for (int t = 0; t < nt; t++) part[t + 1] += part[t];
+  run_threads(nt, [&](int t) {
+    const int64_t r0 = std::min(n, t * chunk), r1 = std::min(n, r0 + chunk);
+    for (int64_t r = r0; r < r1; r++) out[r + 1] += part[t];
+  });
+}
+
 // Gauss-Legendre nodes and weights on (-1, 1) by Newton iteration on P_n (the points the reference
 // obtains from the Golub-Welsch eigenproblem, glq.rs:179-222), sorted ascending.
 void glq_points(int n, std::vector<double>& x, std::vector<double>& w) {
@@ -228,11 +252,11 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
       visit_block(b, [&](int32_t dp, int32_t dq, uint32_t, uint32_t) { c[std::min(dp, dq)]++; });
   });
   std::vector<int64_t> bptr(n + 1, 0);
-  for (int64_t r = 0; r < n; r++) {
+  parallel_prefix(n, bptr.data(), [&](int64_t r) {
     int64_t s = 0;
     for (int t = 0; t < nt; t++) s += tcnt[t][r];
-    bptr[r + 1] = bptr[r] + s;
-  }
+    return s;
+  });
   parallel_for(n, [&](int64_t r0, int64_t r1) {
     for (int64_t r = r0; r < r1; r++) {
       int64_t o = bptr[r];
@@ -272,7 +296,7 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
     }
   });
   std::vector<int64_t> uptr(n + 1, 0);
-  for (int64_t r = 0; r < n; r++) uptr[r + 1] = uptr[r] + ucnt[r];
+  parallel_prefix(n, uptr.data(), [&](int64_t r) { return ucnt[r]; });
   const int64_t nu = uptr[n];
   g.nnz_upper = nu;
   if (nu >= (int64_t)INT32_MAX) fail(FEM2D_E_TOO_LARGE, "more than 2^31 - 1 upper-triangle entries");
@@ -312,12 +336,12 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
   });
   g.row_ptr.assign(n + 1, 0);
   std::vector<int64_t> lcnt(n, 0);
-  for (int64_t r = 0; r < n; r++) {
+  parallel_prefix(n, g.row_ptr.data(), [&](int64_t r) {
     int64_t l = 0;
     for (int t = 0; t < nt; t++) l += tcnt[t][r];
     lcnt[r] = l;
-    g.row_ptr[r + 1] = g.row_ptr[r] + l + (uptr[r + 1] - uptr[r]);
-  }
+    return l + (uptr[r + 1] - uptr[r]);
+  });
   const int64_t nf = g.row_ptr[n];
   g.nnz_full = nf;
   g.col.resize(nf);
