@@ -439,11 +439,12 @@ __global__ void ozaki_reduce_kernel(const double* __restrict__ P, int nrb, int n
 // X and owning 16 of the 32 columns of Z). X is sliced with one exponent per row (over its a entries)
 // and C with one per column (over its a entries), so every K sub-block's digit sums share one scale:
 // they are read from TMEM after each 128 columns of K (the exact-accumulation limit) and summed exactly
-// in int64, and converted to FP64 once per output element. C's digit planes (K padded to kc) stay in
-// shared memory for all tiles. Each 128 x 32 sub-block of X is brought in by coalesced asynchronous
-// copies (cp.async, a whole row segment per warp instruction) into a padded staging buffer, one
-// sub-block ahead of its slicing when two staging buffers fit. The row exponents come from a
-// coalesced pre-pass (row_exp_kernel).
+// in int64, fused into one integer (fuse_digit_sums) and converted to FP64 once per output element, with
+// alpha and the power-of-two scale joined exactly in the exponent field. C's digit planes (K padded to
+// kc) stay in shared memory for all tiles. Each 128 x 32 sub-block of X is brought in by coalesced
+// asynchronous copies (cp.async, a whole row segment per warp instruction) into a padded staging
+// buffer, one sub-block ahead of its slicing when two staging buffers fit. The row exponents come from
+// a coalesced pre-pass (row_exp_kernel).
 constexpr int kGemmKMax = 256;
 constexpr int kGemmThreads = 256;
 constexpr int kGemmPlanes = kDigits * kPlaneA;   // digit planes of one 128 x 32 sub-block of X (64 KB)
@@ -724,16 +725,18 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 // s + t = g -- at most 8 pairs x 64 columns x 127^2 < 2^24, exact in FP32 -- and each TMEM lane holds
 // one or two such sums per run row. With nb <= 16 the eight groups x 16 columns fill one 128-row
 // operand (8 MMAs per plane step); with nb <= 32, groups 0..3 and 4..7 x 32 columns fill two (4 and 8
-// MMAs). Sums are combined exactly in int64 across lanes and warps (fixed order), converted once per
-// item and output to FP64 and summed per run in registers; every run is owned by one CTA, which writes
+// MMAs). Sums are combined exactly in int64 across lanes and warps (fixed order), fused into one integer
+// and converted once per item and output to FP64 (one conversion and one FMA) and summed per run in
+// registers; every run is owned by one CTA, which writes
 // its rows of Y once (no atomics, no zero fill, deterministic). Pairs with s + t >= 8 are dropped: below
 // 2^-52 of max|m| max|x| of the item per term, FP64 rounding level in the normwise sense.
 //
-// Pipeline per CTA (one per SM): two shared-memory stages; while the MMAs of item k run, thread 0 has
-// the next item's digit planes of M brought in by one bulk asynchronous copy and all threads gather and
-// slice the next item's rows of X into the other stage. Every mbarrier wait is bounded (one second): on
-// expiry the kernel raises the error flag, lets its copies and MMAs in flight finish (bounded), frees
-// its TMEM and returns.
+// Pipeline: two CTAs per SM, one shared-memory stage each, so one CTA's gathers and slicing overlap the
+// other's MMAs and readout. Per item, thread 0 has its digit planes of M brought in by one bulk
+// asynchronous copy while all threads gather and slice its rows of X (the next item's record, column
+// indices and row exponents are loaded one item ahead, and its rows of X prefetched into L2). Every
+// mbarrier wait is bounded (one second): on expiry the kernel raises the error flag, lets its copies
+// and MMAs in flight finish (bounded), frees its TMEM and returns.
 constexpr int kSpK = 64;                                // columns of a run's list per item
 constexpr int kSpThreads = 256;
 constexpr int kSpXPlaneW = 32 * kSpK * 2;               // a digit plane of X, 32 columns (4 KB)
