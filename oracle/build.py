@@ -17,6 +17,7 @@ def build_oracle(force=False):
     if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
         return out
     cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-function",
+           "-Wno-psabi",   # GCC's note on aarch64 that std::pair argument passing changed in GCC 10
            src, "-o", out + ".tmp"]
     subprocess.check_call(cmd)
     os.replace(out + ".tmp", out)
