@@ -48,56 +48,78 @@ Domain Domain::from_mesh(const Mesh& m, int cc) {
   Mesh& mesh = d.mesh;
   mesh.set_edge_activation();
   const int64_t ne = (int64_t)mesh.elems.size();
-  std::vector<std::vector<Spec>> per(ne);
-  std::vector<std::vector<EdgeSpec>> on_edge(mesh.edges.size());
+  const int64_t nedges = (int64_t)mesh.edges.size();
+  // the U/V specs an Elem generates, in (dir, (i, j)) order; f(i, j, dir, edge slot or -1)
+  auto for_specs = [](const MElem& el, auto&& f) {
+    for (int dir = 0; dir < 2; dir++) {
+      const int imax = dir == 0 ? el.ni - 1 : el.ni;
+      const int jmax = dir == 0 ? el.nj : el.nj - 1;
+      for (int i = 0; i <= imax; i++)
+        for (int j = 0; j <= jmax; j++) f(i, j, dir, edge_slot(i, j, dir));
+    }
+  };
+  // edge specs grouped by Edge (flat, counted then filled), each group in (Elem, dir, (i, j)) order
+  std::vector<int64_t> eptr(nedges + 1, 0);
+  for (int64_t e = 0; e < ne; e++)
+    for_specs(mesh.elems[e], [&](int, int, int, int slot) {
+      if (slot >= 0) eptr[mesh.elems[e].edges[slot] + 1]++;
+    });
+  for (int64_t ed = 0; ed < nedges; ed++) eptr[ed + 1] += eptr[ed];
+  std::vector<EdgeSpec> on_edge(eptr[nedges]);
+  {
+    std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
+    for (int64_t e = 0; e < ne; e++)
+      for_specs(mesh.elems[e], [&](int i, int j, int dir, int slot) {
+        if (slot >= 0)
+          on_edge[fill[mesh.elems[e].edges[slot]]++] = {e, (uint8_t)i, (uint8_t)j, (uint8_t)dir, (uint8_t)slot};
+      });
+  }
+  // interior specs of leaves become DoFs in Elem order; matched edge-spec pairs follow in Edge order.
+  // Each Elem's spec list is its interior specs, then its matched edge specs in the order matched.
+  std::vector<int64_t> nint(ne, 0), nmatch(ne, 0);
+  for (int64_t e = 0; e < ne; e++)
+    if (mesh.elems[e].leaf())
+      for_specs(mesh.elems[e], [&](int, int, int, int slot) { nint[e] += slot < 0; });
+  struct Match { int64_t ea, eb, sa, sb; int32_t dof; };   // sa, sb: indices into on_edge
+  std::vector<Match> matches;
   int32_t next = 0;
-  // spec generation in (Elem, dir, (i, j)) order; interior specs of leaves become DoFs at once
-  for (int64_t e = 0; e < ne; e++) {
-    const MElem& el = mesh.elems[e];
-    for (int dir = 0; dir < 2; dir++) {
-      int imax = dir == 0 ? el.ni - 1 : el.ni;
-      int jmax = dir == 0 ? el.nj : el.nj - 1;
-      for (int i = 0; i <= imax; i++)
-        for (int j = 0; j <= jmax; j++) {
-          int slot = edge_slot(i, j, dir);
-          if (slot >= 0) on_edge[el.edges[slot]].push_back({e, (uint8_t)i, (uint8_t)j, (uint8_t)dir, (uint8_t)slot});
-        }
-    }
-  }
-  for (int64_t e = 0; e < ne; e++) {
-    const MElem& el = mesh.elems[e];
-    if (!el.leaf()) continue;
-    for (int dir = 0; dir < 2; dir++) {
-      int imax = dir == 0 ? el.ni - 1 : el.ni;
-      int jmax = dir == 0 ? el.nj : el.nj - 1;
-      for (int i = 0; i <= imax; i++)
-        for (int j = 0; j <= jmax; j++)
-          if (edge_slot(i, j, dir) < 0) per[e].push_back({(uint8_t)i, (uint8_t)j, (uint8_t)dir, next++});
-    }
-  }
-  std::vector<EdgeSpec> rel;
-  std::vector<char> used;
-  for (size_t ed = 0; ed < mesh.edges.size(); ed++) {
+  for (int64_t e = 0; e < ne; e++) next += (int32_t)nint[e];
+  std::vector<int64_t> rel;   // indices into on_edge of the specs of the Edge's active Elems
+  for (int64_t ed = 0; ed < nedges; ed++) {
     const MEdge& E = mesh.edges[ed];
-    if (!E.active || on_edge[ed].empty()) continue;
+    if (!E.active || eptr[ed] == eptr[ed + 1]) continue;
     rel.clear();
-    for (auto& s : on_edge[ed])
-      if (s.elem == E.act[0] || s.elem == E.act[1]) rel.push_back(s);
+    for (int64_t q = eptr[ed]; q < eptr[ed + 1]; q++)
+      if (on_edge[q].elem == E.act[0] || on_edge[q].elem == E.act[1]) rel.push_back(q);
     for (size_t a = 0; a < rel.size(); a++)
       for (size_t b = a + 1; b < rel.size(); b++)
-        if (edge_match(rel[a], rel[b])) {
-          int32_t dof = next++;
-          per[rel[a].elem].push_back({rel[a].i, rel[a].j, rel[a].dir, dof});
-          per[rel[b].elem].push_back({rel[b].i, rel[b].j, rel[b].dir, dof});
+        if (edge_match(on_edge[rel[a]], on_edge[rel[b]])) {
+          const EdgeSpec &sa = on_edge[rel[a]], &sb = on_edge[rel[b]];
+          matches.push_back({sa.elem, sb.elem, rel[a], rel[b], next++});
+          nmatch[sa.elem]++;
+          nmatch[sb.elem]++;
           break;
         }
   }
   d.ndofs = next;
   d.spec_ptr.resize(ne + 1);
   d.spec_ptr[0] = 0;
-  for (int64_t e = 0; e < ne; e++) d.spec_ptr[e + 1] = d.spec_ptr[e] + (int64_t)per[e].size();
-  d.specs.reserve(d.spec_ptr[ne]);
-  for (auto& v : per) d.specs.insert(d.specs.end(), v.begin(), v.end());
+  for (int64_t e = 0; e < ne; e++) d.spec_ptr[e + 1] = d.spec_ptr[e] + nint[e] + nmatch[e];
+  d.specs.resize(d.spec_ptr[ne]);
+  std::vector<int64_t> pos(ne);
+  int32_t dof = 0;
+  for (int64_t e = 0; e < ne; e++) {
+    pos[e] = d.spec_ptr[e];
+    if (!mesh.elems[e].leaf()) continue;
+    for_specs(mesh.elems[e], [&](int i, int j, int dir, int slot) {
+      if (slot < 0) d.specs[pos[e]++] = {(uint8_t)i, (uint8_t)j, (uint8_t)dir, dof++};
+    });
+  }
+  for (const Match& mt : matches) {
+    const EdgeSpec &sa = on_edge[mt.sa], &sb = on_edge[mt.sb];
+    d.specs[pos[mt.ea]++] = {sa.i, sa.j, sa.dir, mt.dof};
+    d.specs[pos[mt.eb]++] = {sb.i, sb.j, sb.dir, mt.dof};
+  }
   return d;
 }
 
