@@ -282,13 +282,29 @@ void build_symbolic(const Domain& d, int basis, int nq_u, int nq_v, HostGEP& g) 
       });
   });
 
-  // ---- per row: sort by (col, code), unique columns = upper pattern
+  // ---- per row: sort by (col, code), unique columns = upper pattern. A row's items arrive in ascending
+  // code order (thread ranges, blocks and each block's (p, q) loops all ascend), so the sort is by
+  // (col, arrival index): one 64-bit key per item and a gather. A row that does not arrive ordered (the
+  // check is one pass) takes the two-key sort instead; both give the same order.
   std::vector<int64_t> ucnt(n, 0);
   parallel_for(n, [&](int64_t r0, int64_t r1) {
+    std::vector<uint64_t> key;
+    std::vector<Item> tmp;
     for (int64_t r = r0; r < r1; r++) {
       Item* a = items + bptr[r];
       Item* z = items + bptr[r + 1];
-      std::sort(a, z, [](const Item& x, const Item& y) { return x.col != y.col ? x.col < y.col : x.code < y.code; });
+      const int64_t len = z - a;
+      bool ordered = true;
+      for (int64_t q = 1; q < len && ordered; q++) ordered = a[q - 1].code < a[q].code;
+      if (!ordered) {
+        std::sort(a, z, [](const Item& x, const Item& y) { return x.col != y.col ? x.col < y.col : x.code < y.code; });
+      } else if (len > 1) {
+        key.resize(len);
+        tmp.assign(a, z);
+        for (int64_t q = 0; q < len; q++) key[q] = ((uint64_t)(uint32_t)a[q].col << 32) | (uint64_t)q;
+        std::sort(key.begin(), key.end());
+        for (int64_t q = 0; q < len; q++) a[q] = tmp[key[q] & 0xffffffffu];
+      }
       int64_t u = 0;
       for (Item* it = a; it < z; it++)
         if (it == a || it->col != (it - 1)->col) u++;
