@@ -85,3 +85,12 @@ def test_assembly_records_cover_the_pattern(plan):
     covered[acsr] = True
     covered[tpos[acsr]] = True
     assert np.all(covered)
+
+
+def test_plan_is_deterministic(plan):
+    """The threaded analysis gives the same plan every time (the solves' bitwise reproducibility rests on
+    it: the assembly maps fix the order in which entries enter the fronts)."""
+    dom, p, _ = plan
+    q = fg.factor_plan(dom)
+    for k in p:
+        assert np.array_equal(p[k], q[k]), k
